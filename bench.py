@@ -1,0 +1,411 @@
+#!/usr/bin/env python3
+"""Search throughput of the GB300 LSH engine on the integer-feature workload.
+
+One step = one multiprobe k-NN search of Q queries against a resident index:
+query projection onto all L*M columns, multiprobe codes + bucket lookup, then
+candidate gather / dedup / distances / top-K. Default workload: N=1,000,000
+points of D=128 non-negative integer features stored as float32, L=16 tables,
+M=12 projections, W=16, Q=10,000 held-out queries, K=10, T=16 probes.
+
+value  : queries/s with queries already in HBM (device API), timed per step
+         with CUDA events on the launching stream; L2 is flushed (256 MB
+         write) between timed steps, outside the events.
+e2e    : queries/s through the reference-facing C ABI (culsh_search_run) with
+         host buffers: every step copies the queries in and the K x Q ids and
+         distances out.
+--impl reference : the CPU oracle (C++/OpenMP restatement of the reference
+         algorithm, all host threads) on the same workload; the reference itself
+         is CUDA-only and cannot be built for the Arm host of the GPU machine.
+Multi-GPU (torchrun): independent replicas, one per rank, no collective on the
+data path; the job value is world * Q * steps / max-over-ranks time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "QPS at recall@10≥0.90 (1M×128), BF16+rerank vs FP32; served p50/p99 ms"
+UNIT = "queries/s"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse_args(argv=None):
+    p = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["culsh", "reference"], default="culsh")
+    p.add_argument("--config", type=int, default=2, help="workload number (1-5), default 2")
+    p.add_argument("--n", type=int, default=None, help="override N (smaller parity / profiling cases)")
+    p.add_argument("--q", type=int, default=None, help="override Q")
+    p.add_argument("--K", type=int, default=None)
+    p.add_argument("--T", type=int, default=None)
+    p.add_argument("--recall-sample", type=int, default=200)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args(argv)
+
+
+# ---------------------------------------------------------------------------
+# multi-rank plumbing (replicas)
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def init_dist(world, backend):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    dist.init_process_group(backend=backend)
+    return dist
+
+
+def reduce_max(dist, value: float, device=None) -> float:
+    """Max of a per-rank float over all ranks (identity without a group)."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_throughput(units_per_rank: float, world: int, max_seconds: float) -> float:
+    """Whole-job throughput of `world` replicas, each processing `units_per_rank`."""
+    return units_per_rank * world / max_seconds
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id: str | None):
+        self.proc = None
+        self.path = None
+        self.gpu_id = gpu_id
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"]
+            if self.gpu_id:
+                cmd.insert(1, f"--id={self.gpu_id}")
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(cmd, stdout=self.out, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.out.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def hbm_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic(kernel: str, workload: str):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        e = d.get(workload, {}).get(kernel)
+        return None if e is None else float(e)
+    except (OSError, ValueError):
+        return None
+
+
+# ---------------------------------------------------------------------------
+# algorithmic bytes per stage (one launch over Q queries); see the design doc
+
+def stage_bytes(cfg, Q, K, T, KW, hits, nonunique, unique):
+    L, M, D = cfg["L"], cfg["M"], cfg["D"]
+    project = 4 * (Q * D + L * M * D + L * M + L * M * Q)
+    probe = 4 * L * M * Q + Q * L * T * (8 + 4) + hits * (4 * KW + 4) + 8 * Q
+    cand = 8 * Q + 4 * Q * L * T + 8 * hits + 4 * nonunique + 4 * D * unique + 4 * D * Q + 8 * K * Q
+    return {"project": project, "probe": probe, "candidates": cand}
+
+
+def recall_at_k(found, X, queries, K):
+    """Mean |found ∩ exact top-K| / K; exact top-K by FP64 brute force, ties to
+    the smaller id. -1 entries count as misses."""
+    Xd = X.astype(np.float64)
+    xx = np.einsum("ij,ij->i", Xd, Xd)
+    hit = 0
+    for c0 in range(0, queries.shape[0], 64):
+        Qd = queries[c0:c0 + 64].astype(np.float64)
+        dots = Xd @ Qd.T
+        for j in range(Qd.shape[0]):
+            d = xx - 2.0 * dots[:, j] + Qd[j] @ Qd[j]
+            part = np.argpartition(d, K)[:K]
+            kth = d[part].max()
+            cand = np.nonzero(d <= kth)[0]
+            exact = cand[np.lexsort((cand, d[cand]))][:K]
+            hit += len(set(exact.tolist()) & set(int(x) for x in found[c0 + j] if x >= 0))
+    return hit / (K * queries.shape[0])
+
+
+# ---------------------------------------------------------------------------
+
+def workload(args):
+    from culsh_gb300 import synth
+    X, Qm, A, b, cfg = synth.dataset(args.config, n=args.n, q=args.q)
+    K = args.K or cfg.K
+    T = args.T or cfg.T
+    d = dict(N=X.shape[0], D=cfg.D, L=cfg.L, M=cfg.M, W=cfg.W, Q=Qm.shape[0], K=K, T=T)
+    name = f"{cfg.name} N={d['N']} L={cfg.L} M={cfg.M} W={cfg.W:g} T={T} K={K} Q={d['Q']}"
+    return X, Qm, A, b, d, name
+
+
+def cpu_baseline(X, Qm, A, b, d, min_seconds=8.0):
+    import oracle
+    t0 = time.perf_counter()
+    idx = oracle.build_index(X, A, b, d["W"])
+    t_index = time.perf_counter() - t0
+    reps, el = 0, 0.0
+    while el < min_seconds or reps < 1:
+        t0 = time.perf_counter()
+        oracle.search(idx, X, Qm, d["K"], d["T"])
+        el += time.perf_counter() - t0
+        reps += 1
+    return {"value": reps * Qm.shape[0] / el, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+            "sample": f"{reps} x {Qm.shape[0]} queries of the same workload after a {t_index:.1f} s CPU index build",
+            "index_build_s": round(t_index, 3)}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    import oracle
+    X, Qm, A, b, d, name = workload(args)
+    t0 = time.perf_counter()
+    idx = oracle.build_index(X, A, b, d["W"])
+    t_index = time.perf_counter() - t0
+    # bounded sample per step: as many queries as take about half a second
+    t0 = time.perf_counter()
+    oracle.search(idx, X, Qm[:500], d["K"], d["T"])
+    per_q = max((time.perf_counter() - t0) / 500, 1e-7)
+    nq = int(min(Qm.shape[0], max(500, 0.5 / per_q)))
+    sample = Qm[:nq]
+    for _ in range(args.warmup):
+        oracle.search(idx, X, sample, d["K"], d["T"])
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.search(idx, X, sample, d["K"], d["T"])
+    el = time.perf_counter() - t0
+    v = args.steps * nq / el
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generator of the workload's distribution)",
+            "config": {"workload": name, **d, "sample_queries_per_step": nq},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+                             "sample": f"{nq} queries per step; CPU index build {t_index:.1f} s untimed"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference (cuLSH) is CUDA + cuBLAS + Thrust only; its algorithm runs here as the "
+                    "C++/OpenMP oracle port on the host cores"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_culsh(args):
+    import torch
+    rank, world, local_rank = dist_env()
+    torch.cuda.set_device(local_rank)
+    dist = init_dist(world, "nccl")
+    dev = torch.device("cuda", local_rank)
+    import culsh_gb300 as culsh
+    culsh.lib()
+
+    X, Qm, A, b, d, name = workload(args)
+    N, D, L, M, Q, K, T = d["N"], d["D"], d["L"], d["M"], d["Q"], d["K"], d["T"]
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+
+    # Index build (device-resident dataset, borrowed by the index).
+    Xt = torch.from_numpy(X).to(dev)
+    ht = culsh.HashTables()
+    ht.reset(N, D, L, M, d["W"], A=A, b=b)
+    ht.index_device(Xt.data_ptr(), sp)
+    build_ms = []
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        ht.index_device(Xt.data_ptr(), sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        build_ms.append(e0.elapsed_time(e1))
+
+    qt = torch.from_numpy(Qm).to(dev)
+    ids = torch.empty((Q, K), dtype=torch.int32, device=dev)
+    dists = torch.empty((Q, K), dtype=torch.float32, device=dev)
+    st = culsh.SearchTables()
+    st.reset(ht, K, T)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    for _ in range(args.warmup):
+        st.search_device(qt.data_ptr(), Q, ids.data_ptr(), dists.data_ptr(), sp)
+
+    gpu_id = None
+    try:
+        gpu_id = str(torch.cuda.get_device_properties(dev).uuid)
+        if not gpu_id.startswith("GPU-"):
+            gpu_id = "GPU-" + gpu_id
+    except Exception:
+        gpu_id = None
+    clocks = ClockSampler(gpu_id)
+    clocks.start()
+    events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    stages = {"project": [], "probe": [], "candidates": []}
+    launches = 0
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    for i in range(args.steps):
+        flush.fill_(i & 0xFF)
+        e0, e1 = events[i]
+        e0.record(stream)
+        st.search_device(qt.data_ptr(), Q, ids.data_ptr(), dists.data_ptr(), sp)
+        e1.record(stream)
+        pr = st.profile()
+        stages["project"].append(pr["project_ms"])
+        stages["probe"].append(pr["probe_ms"])
+        stages["candidates"].append(pr["candidates_ms"])
+        launches += pr["launches"]
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    clk = clocks.stop()
+    step_ms = [e0.elapsed_time(e1) for e0, e1 in events]
+    total_s = sum(step_ms) / 1e3
+    max_s = reduce_max(dist, total_s, dev)
+    value = aggregate_throughput(Q * args.steps, world, max_s)
+
+    # Totals for the algorithmic byte counts (outside the timed region).
+    uniq, nonuniq = st.getTotalCandidates_unique(), st.getTotalCandidates_nonUnique()
+    hits = sum(int((st.getQueryBuckets(l) >= 0).sum()) for l in range(L))
+    KW = st.profile()["key_words"]
+    sb = stage_bytes(d, Q, K, T, KW, hits, nonuniq, uniq)
+    med = {k: statistics.median(v) for k, v in stages.items()}
+    dom = max(med, key=med.get)
+    peak, peak_kind = hbm_peak()
+    achieved = sb[dom] / (med[dom] / 1e3) / 1e9
+    kernel_name = {"project": "k_project", "probe": "k_probe", "candidates": "k_candidates"}[dom]
+    roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 5), "traffic": ncu_traffic(kernel_name, name),
+                "kernel": kernel_name, "algorithmic_bytes": sb[dom], "peak_source": f"{peak_kind} hbm_gbs",
+                "stage_ms_median": {k: round(v, 4) for k, v in med.items()}}
+
+    # End to end through the reference-facing C ABI with host buffers.
+    e2e = None
+    if not args.no_e2e:
+        ht_h = culsh.HashTables()
+        ht_h.reset(N, D, L, M, d["W"], A=A, b=b)
+        ht_h.index(X)
+        st_h = culsh.SearchTables()
+        st_h.reset(ht_h, K, T)
+        for _ in range(args.warmup):
+            st_h.search(Qm, Q, X)
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            st_h.search(Qm, Q, X)
+        el = time.perf_counter() - t0
+        el_max = reduce_max(dist, el, dev)
+        host_ids = st_h.getKnnIds()
+        assert np.array_equal(host_ids, ids.cpu().numpy()), "host and device API results differ"
+        e2e = {"value": aggregate_throughput(Q * args.steps, world, el_max), "unit": UNIT,
+               "h2d_bytes_per_step": int(Qm.nbytes), "d2h_bytes_per_step": int(Q * K * 8),
+               "path": "culsh_search_run (C ABI, pageable host buffers)"}
+        del st_h, ht_h
+
+    found = ids.cpu().numpy()
+    ns = min(args.recall_sample, Q)
+    rec = recall_at_k(found[:ns], X, Qm[:ns], K) if ns > 0 else None
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(X, Qm, A, b, d)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * max_s / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded generator of the workload's distribution)",
+                "config": {"workload": name, **d, "form": "fp32 (canonical order, bit-exact)",
+                           "l2": "flushed by a 256 MB write between timed steps", "parallelism": "replicas"},
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+                "clocks": clk, "index_build_ms": round(statistics.median(build_ms), 3),
+                "recall_at_k": rec, "recall_sample": ns,
+                "selectivity": st.getSelectivity(), "candidates_unique_per_query": uniq / Q,
+                "candidates_nonunique_per_query": nonuniq / Q}
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main(argv=None):
+    args = parse_args(argv)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_culsh(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

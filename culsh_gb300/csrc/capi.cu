@@ -1,0 +1,1019 @@
+// Host orchestration and C ABI of libculsh.
+//
+// Mirrors the state and call sequence of cuLSH::HashTables
+// (cuLSH_HashTables.cu) and cuLSH::SearchTables (cuLSH_SearchTables.cu), with
+// the data kept resident on one GPU: index() uploads the dataset once and
+// builds every table with four kernels (projection, key packing, one radix
+// sort over all tables, run-length + hash), and search() runs the whole query
+// path in three launches. Host copies of the bucket arrays and query buckets
+// are produced lazily, only when a getter or save() needs them.
+#include <algorithm>
+#include <cerrno>
+#include <climits>
+#include <cmath>
+#include <cstdarg>
+#include <cstdlib>
+#include <cstdio>
+#include <cstring>
+#include <ctime>
+#include <string>
+#include <vector>
+
+#include "culsh.h"
+#include "culsh_internal.cuh"
+
+using namespace culsh;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CU_TRY(call)                                                                                   \
+    do {                                                                                               \
+        cudaError_t e_ = (call);                                                                       \
+        if (e_ != cudaSuccess)                                                                         \
+            return fail(e_ == cudaErrorMemoryAllocation ? CULSH_ERR_OUT_OF_MEMORY : CULSH_ERR_CUDA,    \
+                        "%s: %s", #call, cudaGetErrorString(e_));                                      \
+    } while (0)
+
+#define TRY(expr)                  \
+    do {                           \
+        int rc_ = (expr);          \
+        if (rc_ != CULSH_OK) return rc_; \
+    } while (0)
+
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    cudaError_t reserve(size_t cnt) {
+        if (cnt <= n && p) return cudaSuccess;
+        release();
+        const cudaError_t e = cudaMalloc(&p, std::max<size_t>(cnt, 1) * sizeof(T));
+        if (e == cudaSuccess) n = std::max<size_t>(cnt, 1);
+        else p = nullptr;
+        return e;
+    }
+    void swap(DevBuf& o) {
+        std::swap(p, o.p);
+        std::swap(n, o.n);
+    }
+};
+
+template <class T>
+struct PinBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    PinBuf() = default;
+    PinBuf(const PinBuf&) = delete;
+    PinBuf& operator=(const PinBuf&) = delete;
+    ~PinBuf() {
+        if (p) cudaFreeHost(p);
+    }
+    cudaError_t reserve(size_t cnt) {
+        if (cnt <= n && p) return cudaSuccess;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+        const cudaError_t e = cudaMallocHost(&p, std::max<size_t>(cnt, 1) * sizeof(T));
+        if (e == cudaSuccess) n = std::max<size_t>(cnt, 1);
+        return e;
+    }
+};
+
+inline uint64_t next_pow2(uint64_t v) {
+    uint64_t p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+inline double seconds_now() {
+    timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+
+}  // namespace
+
+struct culsh_index {
+    int N = 0, D = 0, L = 0, M = 0;
+    float W = 0.0f;
+    std::vector<float> A, b;   // [L][M][D] (A[l] column-major D x M), [L][M]
+    bool has_proj = false;
+
+    // index state
+    bool indexed = false, host_valid = false, dev_valid = false;
+    std::vector<uint32_t> buckets;   // [L]
+    std::vector<std::vector<uint32_t>> h_ids, h_starts, h_sizes;
+    std::vector<std::vector<float>> h_codes;
+
+    // device
+    cudaStream_t stream = nullptr;
+    DevBuf<float> X;               // owned dataset copy
+    const float* x_src = nullptr;  // host pointer the copy was made from
+    const float* x_borrow = nullptr;
+    DevBuf<float> dA, db;
+    bool proj_on_dev = false;
+    int KW = 1;
+    std::vector<int32_t> h_cmin, h_cmax;
+    std::vector<uint8_t> h_fbits;
+    std::vector<uint16_t> h_foff;
+    DevBuf<int32_t> cmin, cmax;
+    DevBuf<uint8_t> fbits;
+    DevBuf<uint16_t> foff;
+    DevBuf<uint32_t> ids, starts, sizes, ukeys;
+    std::vector<uint64_t> h_boff, h_hoff;
+    std::vector<uint32_t> h_hmask;
+    DevBuf<uint64_t> boff, hoff;
+    DevBuf<uint32_t> hmask;
+    DevBuf<unsigned long long> hslots;
+    DevBuf<float> dcodes;
+    DevBuf<int> err;
+
+    // build workspace (kept across builds)
+    DevBuf<int32_t> ws_codes, ws_pmin, ws_pmax;
+    DevBuf<uint32_t> ws_keys[2], ws_vals, ws_hist, ws_base, ws_status, ws_tcnt, ws_toff, ws_nb;
+
+    ~culsh_index() {
+        if (stream) cudaStreamDestroy(stream);
+    }
+    const float* dev_x() const { return x_borrow ? x_borrow : (X.p ? X.p : nullptr); }
+};
+
+struct culsh_search {
+    culsh_index* ix = nullptr;
+    int K = 0, T = 1, Q = 0, L = 0;
+    bool searched = false;
+    unsigned long long tot_unique = 0, tot_nonunique = 0;
+    culsh_times times{};
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    int launches = 0, deferred_queries = 0;
+    bool host_copy_timed = false;
+    DevBuf<float> dq, vals, od;
+    DevBuf<int32_t> qb, oids;
+    DevBuf<unsigned long long> cnu, cu, stats;
+    DevBuf<int> deferred;
+    DevBuf<uint32_t> arena;
+    PinBuf<int32_t> h_ids, h_qb;
+    PinBuf<float> h_d;
+    PinBuf<unsigned long long> h_stats;
+    bool qb_host_valid = false;
+
+    ~culsh_search() {
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+int ensure_stream(cudaStream_t* st) {
+    if (!*st) CU_TRY(cudaStreamCreateWithFlags(st, cudaStreamNonBlocking));
+    return CULSH_OK;
+}
+
+int check_params(int N, int D, int L, int M, float W) {
+    // cuLSH_HashTables.cu:70 checkParameters: all positive.
+    if (!(N > 0 && D > 0 && L > 0 && M > 0 && W > 0.0f))
+        return fail(CULSH_ERR_INVALID_ARGUMENT,
+                    "Projection parameters must be positive! (N, D, L, M, W) = (%d, %d, %d, %d, %g)", N, D, L, M,
+                    (double)W);
+    if (!std::isfinite(W)) return fail(CULSH_ERR_INVALID_ARGUMENT, "W must be finite");
+    if (N > CULSH_MAX_N) return fail(CULSH_ERR_CAPACITY, "N = %d exceeds the supported maximum %d", N, CULSH_MAX_N);
+    if (M > CULSH_MAX_M) return fail(CULSH_ERR_CAPACITY, "M = %d exceeds the supported maximum %d", M, CULSH_MAX_M);
+    return CULSH_OK;
+}
+
+void clear_index_state(culsh_index* ix) {
+    ix->indexed = ix->host_valid = ix->dev_valid = false;
+    ix->buckets.clear();
+    ix->h_ids.clear();
+    ix->h_starts.clear();
+    ix->h_sizes.clear();
+    ix->h_codes.clear();
+    ix->x_src = nullptr;
+    ix->x_borrow = nullptr;
+    ix->proj_on_dev = false;
+}
+
+int upload_projection(culsh_index* ix, cudaStream_t st) {
+    if (ix->proj_on_dev) return CULSH_OK;
+    const size_t LM = (size_t)ix->L * ix->M;
+    CU_TRY(ix->dA.reserve(LM * ix->D));
+    CU_TRY(ix->db.reserve(LM));
+    CU_TRY(cudaMemcpyAsync(ix->dA.p, ix->A.data(), sizeof(float) * LM * ix->D, cudaMemcpyHostToDevice, st));
+    CU_TRY(cudaMemcpyAsync(ix->db.p, ix->b.data(), sizeof(float) * LM, cudaMemcpyHostToDevice, st));
+    ix->proj_on_dev = true;
+    return CULSH_OK;
+}
+
+int read_err_flag(culsh_index* ix, cudaStream_t st, const char* what) {
+    int h = 0;
+    CU_TRY(cudaMemcpyAsync(&h, ix->err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CU_TRY(cudaStreamSynchronize(st));
+    if (h & kErrNonFinite) return fail(CULSH_ERR_NUMERIC, "%s: a projection is not finite (NaN/Inf in the data?)", what);
+    if (h & kErrCodeRange) return fail(CULSH_ERR_NUMERIC, "%s: a bucket code exceeds the int32 range", what);
+    if (h & kErrNotIntegral) return fail(CULSH_ERR_FORMAT, "%s: a bucket code is not an integer", what);
+    if (h & kErrSpin) return fail(CULSH_ERR_DEVICE, "%s: a device-side wait gave up", what);
+    if (h & kErrHashFull) return fail(CULSH_ERR_DEVICE, "%s: hash table insert ran out of slots", what);
+    return CULSH_OK;
+}
+
+// Bit widths and offsets of each column's field: column 0 most significant.
+int compute_layout(culsh_index* ix, int* passes) {
+    const int L = ix->L, M = ix->M;
+    ix->h_fbits.assign((size_t)L * M, 0);
+    ix->h_foff.assign((size_t)L * M, 0);
+    int smax = 0;
+    for (int l = 0; l < L; ++l) {
+        int off = 0;
+        for (int m = M - 1; m >= 0; --m) {
+            const int c = l * M + m;
+            const int64_t range = (int64_t)ix->h_cmax[c] - (int64_t)ix->h_cmin[c];
+            int bits = 0;
+            while (bits < 63 && (range >> bits) != 0) ++bits;
+            if (bits > 32) return fail(CULSH_ERR_CAPACITY, "code range of table %d column %d needs %d bits", l, m, bits);
+            ix->h_fbits[c] = (uint8_t)bits;
+            ix->h_foff[c] = (uint16_t)off;
+            off += bits;
+        }
+        smax = std::max(smax, off);
+    }
+    if (smax > 32 * kMaxKW)
+        return fail(CULSH_ERR_CAPACITY, "bucket codes need %d key bits per table, more than the supported %d", smax,
+                    32 * kMaxKW);
+    ix->KW = std::max(1, (smax + 31) / 32);
+    *passes = (smax + 7) / 8;
+    return CULSH_OK;
+}
+
+int upload_layout(culsh_index* ix, cudaStream_t st) {
+    const size_t LM = (size_t)ix->L * ix->M;
+    CU_TRY(ix->fbits.reserve(LM));
+    CU_TRY(ix->foff.reserve(LM));
+    CU_TRY(ix->cmin.reserve(LM));
+    CU_TRY(ix->cmax.reserve(LM));
+    CU_TRY(cudaMemcpyAsync(ix->fbits.p, ix->h_fbits.data(), LM, cudaMemcpyHostToDevice, st));
+    CU_TRY(cudaMemcpyAsync(ix->foff.p, ix->h_foff.data(), LM * 2, cudaMemcpyHostToDevice, st));
+    CU_TRY(cudaMemcpyAsync(ix->cmin.p, ix->h_cmin.data(), LM * 4, cudaMemcpyHostToDevice, st));
+    CU_TRY(cudaMemcpyAsync(ix->cmax.p, ix->h_cmax.data(), LM * 4, cudaMemcpyHostToDevice, st));
+    return CULSH_OK;
+}
+
+// Hash tables over the unique keys, load factor between 1/4 and 1/2.
+int build_hash(culsh_index* ix, cudaStream_t st) {
+    const int L = ix->L;
+    ix->h_hoff.assign(L + 1, 0);
+    ix->h_hmask.assign(L, 0);
+    int64_t maxB = 0;
+    for (int l = 0; l < L; ++l) {
+        const uint64_t B = ix->h_boff[l + 1] - ix->h_boff[l];
+        const uint64_t cap = next_pow2(std::max<uint64_t>(2 * B, 2));
+        ix->h_hmask[l] = (uint32_t)(cap - 1);
+        ix->h_hoff[l + 1] = ix->h_hoff[l] + cap;
+        maxB = std::max<int64_t>(maxB, (int64_t)B);
+    }
+    CU_TRY(ix->hoff.reserve(L + 1));
+    CU_TRY(ix->hmask.reserve(L));
+    CU_TRY(ix->hslots.reserve(ix->h_hoff[L]));
+    CU_TRY(cudaMemcpyAsync(ix->hoff.p, ix->h_hoff.data(), 8 * (L + 1), cudaMemcpyHostToDevice, st));
+    CU_TRY(cudaMemcpyAsync(ix->hmask.p, ix->h_hmask.data(), 4 * L, cudaMemcpyHostToDevice, st));
+    CU_TRY(cudaMemsetAsync(ix->hslots.p, 0xFF, 8 * ix->h_hoff[L], st));
+    CU_TRY(launch_hash_build(ix->boff.p, ix->ukeys.p, L, ix->KW, maxB, ix->hoff.p, ix->hmask.p, ix->hslots.p,
+                             ix->err.p, st));
+    return CULSH_OK;
+}
+
+// Index build from a device-resident dataset (cuLSH_HashTables.cu:486-520).
+int build_device(culsh_index* ix, const float* dX, cudaStream_t st, FILE* dbg) {
+    const int N = ix->N, D = ix->D, L = ix->L, M = ix->M, LM = L * M;
+    const double t0 = seconds_now();
+    TRY(upload_projection(ix, st));
+    CU_TRY(ix->err.reserve(1));
+    CU_TRY(cudaMemsetAsync(ix->err.p, 0, sizeof(int), st));
+    const int gx = project_grid_x(N);
+    CU_TRY(ix->ws_codes.reserve((size_t)LM * N));
+    CU_TRY(ix->ws_pmin.reserve((size_t)gx * LM));
+    CU_TRY(ix->ws_pmax.reserve((size_t)gx * LM));
+    CU_TRY(ix->cmin.reserve(LM));
+    CU_TRY(ix->cmax.reserve(LM));
+    CU_TRY(launch_project_fp32(dX, N, D, ix->dA.p, ix->db.p, LM, ix->W, ix->ws_codes.p, nullptr, ix->ws_pmin.p,
+                               ix->ws_pmax.p, ix->err.p, st));
+    CU_TRY(launch_minmax_reduce(ix->ws_pmin.p, ix->ws_pmax.p, gx, LM, ix->cmin.p, ix->cmax.p, st));
+    ix->h_cmin.resize(LM);
+    ix->h_cmax.resize(LM);
+    CU_TRY(cudaMemcpyAsync(ix->h_cmin.data(), ix->cmin.p, 4 * LM, cudaMemcpyDeviceToHost, st));
+    CU_TRY(cudaMemcpyAsync(ix->h_cmax.data(), ix->cmax.p, 4 * LM, cudaMemcpyDeviceToHost, st));
+    TRY(read_err_flag(ix, st, "index"));
+    int passes = 0;
+    TRY(compute_layout(ix, &passes));
+    TRY(upload_layout(ix, st));
+    if (dbg)
+        fprintf(dbg, "[HashTables::index]\tprojected %d points onto %d tables x %d columns; %d key words, %d sort passes\n",
+                N, L, M, ix->KW, passes);
+
+    // Pack keys and sort all tables at once.
+    const size_t LN = (size_t)L * N;
+    CU_TRY(ix->ws_keys[0].reserve(LN * ix->KW));
+    CU_TRY(ix->ws_keys[1].reserve(LN * ix->KW));
+    CU_TRY(ix->ws_vals.reserve(LN));
+    CU_TRY(ix->ids.reserve(LN));
+    CU_TRY(launch_pack_keys(ix->ws_codes.p, N, L, M, ix->KW, ix->cmin.p, ix->fbits.p, ix->foff.p, ix->ws_keys[0].p,
+                            ix->ids.p, st));
+    const int hp = std::max(passes, 1);
+    CU_TRY(ix->ws_hist.reserve((size_t)L * hp * 256));
+    CU_TRY(ix->ws_base.reserve((size_t)L * hp * 256));
+    CU_TRY(ix->ws_status.reserve(sort_status_words(N, L)));
+    SortBuffers sb;
+    sb.keys[0] = ix->ws_keys[0].p;
+    sb.keys[1] = ix->ws_keys[1].p;
+    sb.vals[0] = ix->ids.p;
+    sb.vals[1] = ix->ws_vals.p;
+    sb.hist = ix->ws_hist.p;
+    sb.base = ix->ws_base.p;
+    sb.status = ix->ws_status.p;
+    sb.err = ix->err.p;
+    bool alt = false;
+    CU_TRY(run_segmented_sort(sb, N, L, ix->KW, passes, &alt, st));
+    const uint32_t* skeys = ix->ws_keys[alt ? 1 : 0].p;
+    if (alt) ix->ids.swap(ix->ws_vals);
+
+    // Run-length bucketing.
+    const int tiles = (N + 4095) / 4096;
+    CU_TRY(ix->ws_tcnt.reserve((size_t)L * tiles));
+    CU_TRY(ix->ws_toff.reserve((size_t)L * tiles));
+    CU_TRY(ix->ws_nb.reserve(L));
+    CU_TRY(launch_rl_count(skeys, N, L, ix->KW, ix->ws_tcnt.p, ix->ws_toff.p, ix->ws_nb.p, st));
+    ix->buckets.assign(L, 0);
+    CU_TRY(cudaMemcpyAsync(ix->buckets.data(), ix->ws_nb.p, 4 * L, cudaMemcpyDeviceToHost, st));
+    CU_TRY(cudaStreamSynchronize(st));
+    ix->h_boff.assign(L + 1, 0);
+    int64_t maxB = 0;
+    for (int l = 0; l < L; ++l) {
+        ix->h_boff[l + 1] = ix->h_boff[l] + ix->buckets[l];
+        maxB = std::max<int64_t>(maxB, ix->buckets[l]);
+    }
+    const uint64_t totB = ix->h_boff[L];
+    CU_TRY(ix->boff.reserve(L + 1));
+    CU_TRY(cudaMemcpyAsync(ix->boff.p, ix->h_boff.data(), 8 * (L + 1), cudaMemcpyHostToDevice, st));
+    CU_TRY(ix->starts.reserve(totB));
+    CU_TRY(ix->sizes.reserve(totB));
+    CU_TRY(ix->ukeys.reserve(totB * ix->KW));
+    CU_TRY(launch_rl_write(skeys, N, L, ix->KW, ix->ws_toff.p, ix->boff.p, ix->starts.p, ix->ukeys.p, st));
+    CU_TRY(launch_bucket_sizes(ix->boff.p, ix->starts.p, N, L, maxB, ix->sizes.p, st));
+    TRY(build_hash(ix, st));
+    TRY(read_err_flag(ix, st, "index"));
+    ix->indexed = ix->dev_valid = true;
+    ix->host_valid = false;
+    if (dbg) {
+        for (int l = 0; l < L; ++l)
+            fprintf(dbg, "[HashTables::index]\ttable %d/%d -----> %u distinct buckets\n", l + 1, L, ix->buckets[l]);
+        fprintf(dbg, "[HashTables::index]\tbuilt in %.3f ms\n", 1e3 * (seconds_now() - t0));
+    }
+    return CULSH_OK;
+}
+
+// Host copies of the bucket arrays (getters, save) from the device index.
+int ensure_host(culsh_index* ix) {
+    if (ix->host_valid) return CULSH_OK;
+    if (!ix->dev_valid) return fail(CULSH_ERR_STATE, "Pointers to bucket objects are null. Have you performed indexing???");
+    TRY(ensure_stream(&ix->stream));
+    cudaStream_t st = ix->stream;
+    const int L = ix->L, N = ix->N, M = ix->M;
+    int64_t maxB = 0;
+    for (int l = 0; l < L; ++l) maxB = std::max<int64_t>(maxB, ix->buckets[l]);
+    CU_TRY(ix->dcodes.reserve(ix->h_boff[L] * M));
+    CU_TRY(launch_decode_codes(ix->boff.p, ix->ukeys.p, L, M, ix->KW, maxB, ix->cmin.p, ix->fbits.p, ix->foff.p,
+                               ix->dcodes.p, st));
+    ix->h_ids.assign(L, {});
+    ix->h_starts.assign(L, {});
+    ix->h_sizes.assign(L, {});
+    ix->h_codes.assign(L, {});
+    for (int l = 0; l < L; ++l) {
+        const uint64_t B = ix->buckets[l], bo = ix->h_boff[l];
+        ix->h_ids[l].resize(N);
+        ix->h_starts[l].resize(B);
+        ix->h_sizes[l].resize(B);
+        ix->h_codes[l].resize(B * M);
+        CU_TRY(cudaMemcpyAsync(ix->h_ids[l].data(), ix->ids.p + (size_t)l * N, 4 * (size_t)N, cudaMemcpyDeviceToHost, st));
+        CU_TRY(cudaMemcpyAsync(ix->h_starts[l].data(), ix->starts.p + bo, 4 * B, cudaMemcpyDeviceToHost, st));
+        CU_TRY(cudaMemcpyAsync(ix->h_sizes[l].data(), ix->sizes.p + bo, 4 * B, cudaMemcpyDeviceToHost, st));
+        CU_TRY(cudaMemcpyAsync(ix->h_codes[l].data(), ix->dcodes.p + bo * M, 4 * B * M, cudaMemcpyDeviceToHost, st));
+    }
+    CU_TRY(cudaStreamSynchronize(st));
+    ix->host_valid = true;
+    return CULSH_OK;
+}
+
+// Device index from host arrays (after load()).
+int ensure_device(culsh_index* ix, cudaStream_t st) {
+    if (ix->dev_valid) return upload_projection(ix, st);
+    if (!ix->host_valid) return fail(CULSH_ERR_STATE, "No index: have you performed indexing or loaded a file???");
+    const int L = ix->L, N = ix->N, M = ix->M, LM = L * M;
+    TRY(upload_projection(ix, st));
+    CU_TRY(ix->err.reserve(1));
+    CU_TRY(cudaMemsetAsync(ix->err.p, 0, sizeof(int), st));
+    ix->h_boff.assign(L + 1, 0);
+    int64_t maxB = 0;
+    for (int l = 0; l < L; ++l) {
+        ix->h_boff[l + 1] = ix->h_boff[l] + ix->buckets[l];
+        maxB = std::max<int64_t>(maxB, ix->buckets[l]);
+    }
+    const uint64_t totB = ix->h_boff[L];
+    CU_TRY(ix->ids.reserve((size_t)L * N));
+    CU_TRY(ix->boff.reserve(L + 1));
+    CU_TRY(ix->starts.reserve(totB));
+    CU_TRY(ix->sizes.reserve(totB));
+    CU_TRY(ix->dcodes.reserve(totB * M));
+    CU_TRY(cudaMemcpyAsync(ix->boff.p, ix->h_boff.data(), 8 * (L + 1), cudaMemcpyHostToDevice, st));
+    for (int l = 0; l < L; ++l) {
+        const uint64_t B = ix->buckets[l], bo = ix->h_boff[l];
+        CU_TRY(cudaMemcpyAsync(ix->ids.p + (size_t)l * N, ix->h_ids[l].data(), 4 * (size_t)N, cudaMemcpyHostToDevice, st));
+        CU_TRY(cudaMemcpyAsync(ix->starts.p + bo, ix->h_starts[l].data(), 4 * B, cudaMemcpyHostToDevice, st));
+        CU_TRY(cudaMemcpyAsync(ix->sizes.p + bo, ix->h_sizes[l].data(), 4 * B, cudaMemcpyHostToDevice, st));
+        CU_TRY(cudaMemcpyAsync(ix->dcodes.p + bo * M, ix->h_codes[l].data(), 4 * B * M, cudaMemcpyHostToDevice, st));
+    }
+    ix->h_cmin.assign(LM, INT_MAX);
+    ix->h_cmax.assign(LM, INT_MIN);
+    CU_TRY(ix->cmin.reserve(LM));
+    CU_TRY(ix->cmax.reserve(LM));
+    CU_TRY(cudaMemcpyAsync(ix->cmin.p, ix->h_cmin.data(), 4 * LM, cudaMemcpyHostToDevice, st));
+    CU_TRY(cudaMemcpyAsync(ix->cmax.p, ix->h_cmax.data(), 4 * LM, cudaMemcpyHostToDevice, st));
+    CU_TRY(launch_codes_minmax(ix->boff.p, ix->dcodes.p, L, M, maxB, ix->cmin.p, ix->cmax.p, ix->err.p, st));
+    CU_TRY(cudaMemcpyAsync(ix->h_cmin.data(), ix->cmin.p, 4 * LM, cudaMemcpyDeviceToHost, st));
+    CU_TRY(cudaMemcpyAsync(ix->h_cmax.data(), ix->cmax.p, 4 * LM, cudaMemcpyDeviceToHost, st));
+    TRY(read_err_flag(ix, st, "load"));
+    int passes = 0;
+    TRY(compute_layout(ix, &passes));
+    TRY(upload_layout(ix, st));
+    CU_TRY(ix->ukeys.reserve(totB * ix->KW));
+    CU_TRY(launch_pack_from_codes(ix->boff.p, ix->dcodes.p, L, M, ix->KW, maxB, ix->cmin.p, ix->fbits.p, ix->foff.p,
+                                  ix->ukeys.p, st));
+    TRY(build_hash(ix, st));
+    TRY(read_err_flag(ix, st, "load"));
+    ix->dev_valid = true;
+    return CULSH_OK;
+}
+
+LookupView lookup_view(const culsh_index* ix) {
+    LookupView lv;
+    lv.L = ix->L;
+    lv.M = ix->M;
+    lv.KW = ix->KW;
+    lv.cmin = ix->cmin.p;
+    lv.cmax = ix->cmax.p;
+    lv.fbits = ix->fbits.p;
+    lv.foff = ix->foff.p;
+    lv.boff = ix->boff.p;
+    lv.starts = ix->starts.p;
+    lv.sizes = ix->sizes.p;
+    lv.ukeys = ix->ukeys.p;
+    lv.hslots = ix->hslots.p;
+    lv.hoff = ix->hoff.p;
+    lv.hmask = ix->hmask.p;
+    return lv;
+}
+
+constexpr size_t kArenaInitialWords = size_t(1) << 24;   // 64 MB of overflow hash sets
+
+// Upper bound on the overflow arena, in 32-bit words. CULSH_ARENA_WORDS lowers
+// it (admission tests force the deferral and out-of-memory paths with it).
+size_t arena_cap_words() {
+    const char* e = getenv("CULSH_ARENA_WORDS");
+    if (e) {
+        const long long v = atoll(e);
+        if (v > 0) return (size_t)v;
+    }
+    return ~size_t(0);
+}
+
+// The query path on device buffers (cuLSH_SearchTables.cu:197-463).
+int search_device(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* d_d, cudaStream_t st) {
+    culsh_index* ix = s->ix;
+    const int L = ix->L, M = ix->M, D = ix->D, K = s->K, T = s->T, LM = L * M;
+    const float* dX = ix->dev_x();
+    if (!dX) return fail(CULSH_ERR_STATE, "the dataset is not on the device");
+    for (auto& e : s->ev)
+        if (!e) CU_TRY(cudaEventCreate(&e));
+    CU_TRY(s->vals.reserve((size_t)LM * Q));
+    CU_TRY(s->qb.reserve((size_t)L * Q * T));
+    CU_TRY(s->cnu.reserve(Q));
+    CU_TRY(s->cu.reserve(Q));
+    CU_TRY(s->stats.reserve(4));
+    CU_TRY(s->deferred.reserve(2 * (size_t)Q));
+    CU_TRY(s->h_stats.reserve(4));
+    const size_t cap_words = arena_cap_words();
+    const size_t init_words = std::min(kArenaInitialWords, cap_words);
+    if (s->arena.n < init_words || s->arena.n > cap_words) {
+        s->arena.release();
+        CU_TRY(s->arena.reserve(init_words));
+    }
+    CU_TRY(cudaMemsetAsync(s->cnu.p, 0, 8 * (size_t)Q, st));
+    CU_TRY(cudaMemsetAsync(s->stats.p, 0, 8 * 4, st));
+    s->launches = 0;
+    s->deferred_queries = 0;
+    s->host_copy_timed = false;
+    CU_TRY(cudaEventRecord(s->ev[0], st));
+    CU_TRY(launch_project_fp32(dQ, Q, D, ix->dA.p, ix->db.p, LM, ix->W, nullptr, s->vals.p, nullptr, nullptr, nullptr, st));
+    CU_TRY(cudaEventRecord(s->ev[1], st));
+    ProbeArgs pa;
+    pa.vals = s->vals.p;
+    pa.Q = Q;
+    pa.T = T;
+    pa.lv = lookup_view(ix);
+    pa.qbuckets = s->qb.p;
+    pa.cnu = s->cnu.p;
+    CU_TRY(launch_probe(pa, st));
+    CU_TRY(cudaEventRecord(s->ev[2], st));
+    s->launches += 2;
+    CandArgs ca;
+    ca.X = dX;
+    ca.N = ix->N;
+    ca.D = D;
+    ca.L = L;
+    ca.T = T;
+    ca.Q = Q;
+    ca.K = K;
+    ca.queries = dQ;
+    ca.qbuckets = s->qb.p;
+    ca.boff = ix->boff.p;
+    ca.starts = ix->starts.p;
+    ca.sizes = ix->sizes.p;
+    ca.ids = ix->ids.p;
+    ca.cnu = s->cnu.p;
+    ca.out_ids = d_ids;
+    ca.out_d = d_d;
+    ca.cu = s->cu.p;
+    ca.totals = s->stats.p;
+    ca.arena = s->arena.p;
+    ca.arena_words = s->arena.n;
+    ca.arena_top = s->stats.p + 2;
+    ca.deferred = s->deferred.p;
+    ca.n_deferred = reinterpret_cast<unsigned int*>(s->stats.p + 3);
+    ca.qlist = nullptr;
+    ca.nq = Q;
+    CU_TRY(launch_candidates(ca, st));
+    s->launches += 1;
+    CU_TRY(cudaEventRecord(s->ev[3], st));
+    CU_TRY(cudaMemcpyAsync(s->h_stats.p, s->stats.p, 8 * 4, cudaMemcpyDeviceToHost, st));
+    CU_TRY(cudaStreamSynchronize(st));
+    unsigned int ndef = (unsigned int)(s->h_stats.p[3] & 0xffffffffu);
+    if (ndef) {
+        // Queries whose candidate sets did not fit the arena: admit them in
+        // chunks that fit free device memory (cuLSH_SearchTables.cu:282-306).
+        std::vector<int> dl(ndef);
+        std::vector<unsigned long long> cnu(Q);
+        CU_TRY(cudaMemcpyAsync(dl.data(), s->deferred.p, 4 * (size_t)ndef, cudaMemcpyDeviceToHost, st));
+        CU_TRY(cudaMemcpyAsync(cnu.data(), s->cnu.p, 8 * (size_t)Q, cudaMemcpyDeviceToHost, st));
+        CU_TRY(cudaStreamSynchronize(st));
+        std::sort(dl.begin(), dl.end());
+        s->deferred_queries = (int)ndef;
+        size_t need_max = 0, need_all = 0;
+        for (int q : dl) {
+            need_max = std::max(need_max, cand_arena_words(cnu[q]));
+            need_all += cand_arena_words(cnu[q]);
+        }
+        size_t freeb = 0, totalb = 0;
+        CU_TRY(cudaMemGetInfo(&freeb, &totalb));
+        size_t avail_words = (freeb + 4 * s->arena.n > (size_t)(64 << 20)) ? (freeb + 4 * s->arena.n - (64 << 20)) / 4 : 0;
+        avail_words = std::min(avail_words, cap_words);
+        if (need_max > avail_words) {
+            for (int q : dl)
+                if (cand_arena_words(cnu[q]) == need_max)
+                    return fail(CULSH_ERR_OUT_OF_MEMORY,
+                                "Cannot load all candidates for computation of knn ids of query %d/%d...", q + 1, Q);
+        }
+        const size_t want = std::min(need_all, avail_words);
+        if (want > s->arena.n) {
+            s->arena.release();
+            CU_TRY(s->arena.reserve(want));
+        }
+        size_t i = 0;
+        while (i < dl.size()) {
+            size_t j = i, words = 0;
+            while (j < dl.size() && words + cand_arena_words(cnu[dl[j]]) <= s->arena.n) words += cand_arena_words(cnu[dl[j++]]);
+            CU_TRY(cudaMemcpyAsync(s->deferred.p, dl.data() + i, 4 * (j - i), cudaMemcpyHostToDevice, st));
+            CU_TRY(cudaMemsetAsync(s->stats.p + 2, 0, 16, st));
+            CandArgs cb = ca;
+            cb.arena = s->arena.p;
+            cb.arena_words = s->arena.n;
+            cb.qlist = s->deferred.p;
+            cb.nq = (int)(j - i);
+            cb.deferred = s->deferred.p + (j - i);  // never written: the chunk fits
+            CU_TRY(launch_candidates(cb, st));
+            s->launches += 1;
+            CU_TRY(cudaMemcpyAsync(s->h_stats.p, s->stats.p, 8 * 4, cudaMemcpyDeviceToHost, st));
+            CU_TRY(cudaStreamSynchronize(st));
+            if ((s->h_stats.p[3] & 0xffffffffu) != 0) return fail(CULSH_ERR_DEVICE, "candidate admission failed");
+            i = j;
+        }
+    }
+    s->tot_unique = s->h_stats.p[0];
+    s->tot_nonunique = s->h_stats.p[1];
+    return CULSH_OK;
+}
+
+}  // namespace
+
+// ============================================================================
+extern "C" {
+
+const char* culsh_last_error(void) { return g_err.c_str(); }
+int culsh_version(void) { return 10000; }
+
+int culsh_index_create(culsh_index** out) {
+    if (!out) return fail(CULSH_ERR_INVALID_ARGUMENT, "null output pointer");
+    *out = new (std::nothrow) culsh_index();
+    return *out ? CULSH_OK : fail(CULSH_ERR_OUT_OF_MEMORY, "host allocation failed");
+}
+
+void culsh_index_destroy(culsh_index* ix) { delete ix; }
+
+static int reset_common(culsh_index* ix, int N, int D, int L, int M, float W) {
+    if (!ix) return fail(CULSH_ERR_INVALID_ARGUMENT, "null index");
+    TRY(check_params(N, D, L, M, W));
+    clear_index_state(ix);
+    ix->N = N;
+    ix->D = D;
+    ix->L = L;
+    ix->M = M;
+    ix->W = W;
+    ix->A.assign((size_t)L * M * D, 0.0f);
+    ix->b.assign((size_t)L * M, 0.0f);
+    ix->has_proj = false;
+    return CULSH_OK;
+}
+
+int culsh_index_reset_random(culsh_index* ix, int N, int D, int L, int M, float W, unsigned long long seed, FILE* dbg) {
+    TRY(reset_common(ix, N, D, L, M, W));
+    TRY(ensure_stream(&ix->stream));
+    cudaStream_t st = ix->stream;
+    const size_t nA = (size_t)L * M * D, nu = (size_t)L * M;
+    DevBuf<float> dA, du;
+    CU_TRY(dA.reserve(nA));
+    CU_TRY(du.reserve(nu));
+    CU_TRY(launch_random_projection(dA.p, du.p, (int64_t)nA, (int64_t)nu, seed, st));
+    CU_TRY(cudaMemcpyAsync(ix->A.data(), dA.p, 4 * nA, cudaMemcpyDeviceToHost, st));
+    CU_TRY(cudaMemcpyAsync(ix->b.data(), du.p, 4 * nu, cudaMemcpyDeviceToHost, st));
+    CU_TRY(cudaStreamSynchronize(st));
+    // cuLSH_HashTables.cu:169-171: b = (u - min u) * W per table.
+    for (int l = 0; l < L; ++l) {
+        float* bl = ix->b.data() + (size_t)l * M;
+        const float mn = *std::min_element(bl, bl + M);
+        for (int m = 0; m < M; ++m) bl[m] = (bl[m] - mn) * W;
+    }
+    ix->has_proj = true;
+    if (dbg)
+        fprintf(dbg, "[HashTables::reset]\tIndexing structure reset with parameters (N, D, L, M, W) = (%d, %d, %d, %d, %.2f), and random matrices [A] & vectors [b].\n",
+                N, D, L, M, W);
+    return CULSH_OK;
+}
+
+int culsh_index_reset(culsh_index* ix, int N, int D, int L, int M, float W, const float* const* A,
+                      const float* const* b, FILE* dbg) {
+    TRY(reset_common(ix, N, D, L, M, W));
+    if (!A || !b) return fail(CULSH_ERR_INVALID_ARGUMENT, "Pointers to matrices [A] and/or vectors [b] are null.");
+    for (int l = 0; l < L; ++l) {
+        if (!A[l] || !b[l]) return fail(CULSH_ERR_INVALID_ARGUMENT, "A[%d] or b[%d] is null", l, l);
+        std::memcpy(ix->A.data() + (size_t)l * M * D, A[l], sizeof(float) * (size_t)M * D);
+        std::memcpy(ix->b.data() + (size_t)l * M, b[l], sizeof(float) * M);
+    }
+    ix->has_proj = true;
+    if (dbg)
+        fprintf(dbg, "[HashTables::reset]\tIndexing structure reset with parameters (N, D, L, M, W) = (%d, %d, %d, %d, %.2f), matrices [A] & vectors [b] have been manually set.\n",
+                N, D, L, M, W);
+    return CULSH_OK;
+}
+
+static int precheck_build(culsh_index* ix) {
+    if (!ix) return fail(CULSH_ERR_INVALID_ARGUMENT, "null index");
+    if (!(ix->N > 0 && ix->D > 0 && ix->L > 0 && ix->M > 0 && ix->W > 0.0f))
+        return fail(CULSH_ERR_STATE, "Parameters must be positive. Have you reset the index structure properly???");
+    if (!ix->has_proj)
+        return fail(CULSH_ERR_STATE,
+                    "Pointers to projection matrices [A] and vectors [b] must be valid. Have you reset the index structure properly???");
+    return CULSH_OK;
+}
+
+int culsh_index_build(culsh_index* ix, const float* X, FILE* dbg) {
+    TRY(precheck_build(ix));
+    if (!X) return fail(CULSH_ERR_INVALID_ARGUMENT, "null dataset");
+    TRY(ensure_stream(&ix->stream));
+    cudaStream_t st = ix->stream;
+    clear_index_state(ix);
+    CU_TRY(ix->X.reserve((size_t)ix->N * ix->D));
+    CU_TRY(cudaMemcpyAsync(ix->X.p, X, sizeof(float) * (size_t)ix->N * ix->D, cudaMemcpyHostToDevice, st));
+    ix->x_src = X;
+    return build_device(ix, ix->X.p, st, dbg);
+}
+
+int culsh_index_build_device(culsh_index* ix, const float* d_X, void* stream) {
+    TRY(precheck_build(ix));
+    if (!d_X) return fail(CULSH_ERR_INVALID_ARGUMENT, "null dataset");
+    TRY(ensure_stream(&ix->stream));
+    cudaStream_t st = stream ? (cudaStream_t)stream : ix->stream;
+    clear_index_state(ix);
+    ix->x_borrow = d_X;
+    const int rc = build_device(ix, d_X, st, nullptr);
+    if (rc == CULSH_OK && stream) CU_TRY(cudaStreamSynchronize(st));
+    return rc;
+}
+
+int culsh_index_save(culsh_index* ix, const char* path, FILE* dbg) {
+    if (!ix || !path) return fail(CULSH_ERR_INVALID_ARGUMENT, "null argument");
+    if (dbg) fprintf(dbg, "[HashTables::save]\tSaving indexing structure to file \"%s\"...\n", path);
+    if (!ix->has_proj)
+        return fail(CULSH_ERR_STATE, "Pointers to matrices [A] and/or vectors [b] are null. Have you reset the index structure properly???");
+    if (!ix->indexed) return fail(CULSH_ERR_STATE, "Pointers to bucket objects are null. Have you performed indexing???");
+    TRY(ensure_host(ix));
+    FILE* fp = fopen(path, "wb");
+    if (!fp)
+        return fail(CULSH_ERR_IO, "Could not create file \"%s\" in order to store the hash tables...", path);
+    // Layout of cuLSH_HashTables.cu:415-433.
+    const int L = ix->L, M = ix->M, D = ix->D, N = ix->N;
+    bool ok = fwrite(&ix->N, 4, 1, fp) == 1 && fwrite(&ix->D, 4, 1, fp) == 1 && fwrite(&ix->L, 4, 1, fp) == 1 &&
+              fwrite(&ix->M, 4, 1, fp) == 1 && fwrite(&ix->W, 4, 1, fp) == 1;
+    for (int l = 0; ok && l < L; ++l)
+        ok = fwrite(ix->A.data() + (size_t)l * M * D, 4, (size_t)M * D, fp) == (size_t)M * D &&
+             fwrite(ix->b.data() + (size_t)l * M, 4, M, fp) == (size_t)M;
+    ok = ok && fwrite(ix->buckets.data(), 4, L, fp) == (size_t)L;
+    for (int l = 0; ok && l < L; ++l) {
+        const size_t B = ix->buckets[l];
+        ok = fwrite(ix->h_ids[l].data(), 4, N, fp) == (size_t)N && fwrite(ix->h_starts[l].data(), 4, B, fp) == B &&
+             fwrite(ix->h_sizes[l].data(), 4, B, fp) == B && fwrite(ix->h_codes[l].data(), 4, B * M, fp) == B * M;
+    }
+    ok = !ferror(fp) && ok;
+    ok = (fclose(fp) == 0) && ok;
+    if (!ok) return fail(CULSH_ERR_IO, "writing \"%s\" failed", path);
+    return CULSH_OK;
+}
+
+int culsh_index_load(culsh_index* ix, const char* path, FILE* dbg) {
+    if (!ix || !path) return fail(CULSH_ERR_INVALID_ARGUMENT, "null argument");
+    if (dbg) fprintf(dbg, "[HashTables::reset]\tLoading indexing structure from file \"%s\"...\n", path);
+    FILE* fp = fopen(path, "rb");
+    if (!fp)
+        return fail(CULSH_ERR_IO,
+                    "Could not open file \"%s\" in order to load the hash tables, or file does not exist...", path);
+    struct Closer {
+        FILE* f;
+        ~Closer() { fclose(f); }
+    } closer{fp};
+    int hdr[4];
+    float W;
+    if (fread(hdr, 4, 4, fp) != 4 || fread(&W, 4, 1, fp) != 1)
+        return fail(CULSH_ERR_FORMAT, "\"%s\": truncated header", path);
+    const int N = hdr[0], D = hdr[1], L = hdr[2], M = hdr[3];
+    {
+        const int rc = check_params(N, D, L, M, W);
+        if (rc != CULSH_OK) return fail(CULSH_ERR_FORMAT, "\"%s\": %s", path, g_err.c_str());
+    }
+    // The file size must match the header before anything large is allocated.
+    if (fseek(fp, 0, SEEK_END) != 0) return fail(CULSH_ERR_IO, "\"%s\": seek failed", path);
+    const long long fsize = ftell(fp);
+    const long long fixed = 20 + 4ll * L * ((long long)D * M + M) + 4ll * L + 4ll * L * N;
+    if (fsize < fixed) return fail(CULSH_ERR_FORMAT, "\"%s\": file is truncated (%lld < %lld bytes)", path, fsize, fixed);
+    fseek(fp, 20, SEEK_SET);
+    TRY(reset_common(ix, N, D, L, M, W));
+    for (int l = 0; l < L; ++l) {
+        if (fread(ix->A.data() + (size_t)l * M * D, 4, (size_t)M * D, fp) != (size_t)M * D ||
+            fread(ix->b.data() + (size_t)l * M, 4, M, fp) != (size_t)M)
+            return fail(CULSH_ERR_FORMAT, "\"%s\": truncated projection", path);
+    }
+    ix->has_proj = true;
+    ix->buckets.assign(L, 0);
+    if (fread(ix->buckets.data(), 4, L, fp) != (size_t)L) return fail(CULSH_ERR_FORMAT, "\"%s\": truncated bucket counts", path);
+    long long expect = fixed;
+    for (int l = 0; l < L; ++l) {
+        if (ix->buckets[l] == 0 || ix->buckets[l] > (unsigned)N)
+            return fail(CULSH_ERR_FORMAT, "\"%s\": table %d has %u buckets for %d points", path, l, ix->buckets[l], N);
+        expect += 4ll * ix->buckets[l] * (2 + M);
+    }
+    if (fsize != expect) return fail(CULSH_ERR_FORMAT, "\"%s\": size %lld does not match its header (%lld)", path, fsize, expect);
+    ix->h_ids.assign(L, {});
+    ix->h_starts.assign(L, {});
+    ix->h_sizes.assign(L, {});
+    ix->h_codes.assign(L, {});
+    for (int l = 0; l < L; ++l) {
+        const size_t B = ix->buckets[l];
+        ix->h_ids[l].resize(N);
+        ix->h_starts[l].resize(B);
+        ix->h_sizes[l].resize(B);
+        ix->h_codes[l].resize(B * M);
+        if (fread(ix->h_ids[l].data(), 4, N, fp) != (size_t)N || fread(ix->h_starts[l].data(), 4, B, fp) != B ||
+            fread(ix->h_sizes[l].data(), 4, B, fp) != B || fread(ix->h_codes[l].data(), 4, B * M, fp) != B * M)
+            return fail(CULSH_ERR_FORMAT, "\"%s\": truncated table %d", path, l);
+        // Consistency: buckets tile [0, N) in order and ids are in range.
+        uint64_t pos = 0;
+        for (size_t j = 0; j < B; ++j) {
+            if (ix->h_starts[l][j] != pos || ix->h_sizes[l][j] == 0)
+                return fail(CULSH_ERR_FORMAT, "\"%s\": table %d bucket %zu is inconsistent", path, l, j);
+            pos += ix->h_sizes[l][j];
+        }
+        if (pos != (uint64_t)N) return fail(CULSH_ERR_FORMAT, "\"%s\": table %d buckets cover %llu of %d points", path, l,
+                                            (unsigned long long)pos, N);
+        for (int i = 0; i < N; ++i)
+            if (ix->h_ids[l][i] >= (unsigned)N) return fail(CULSH_ERR_FORMAT, "\"%s\": table %d id out of range", path, l);
+    }
+    ix->indexed = ix->host_valid = true;
+    ix->dev_valid = false;
+    if (dbg)
+        fprintf(dbg, "[HashTables::load]\tIndexing structure loaded from file \"%s\", (N, D, L, M, W) = (%d, %d, %d, %d, %.2f)\n",
+                path, N, D, L, M, W);
+    return CULSH_OK;
+}
+
+void culsh_index_params(const culsh_index* ix, int* N, int* D, int* L, int* M, float* W) {
+    if (N) *N = ix ? ix->N : 0;
+    if (D) *D = ix ? ix->D : 0;
+    if (L) *L = ix ? ix->L : 0;
+    if (M) *M = ix ? ix->M : 0;
+    if (W) *W = ix ? ix->W : 0.0f;
+}
+
+const float* culsh_index_A(culsh_index* ix, int table) {
+    if (!ix || !ix->has_proj || table < 0 || table >= ix->L) return nullptr;
+    return ix->A.data() + (size_t)table * ix->M * ix->D;
+}
+const float* culsh_index_b(culsh_index* ix, int table) {
+    if (!ix || !ix->has_proj || table < 0 || table >= ix->L) return nullptr;
+    return ix->b.data() + (size_t)table * ix->M;
+}
+unsigned culsh_index_bucket_count(culsh_index* ix, int table) {
+    if (!ix || !ix->indexed || table < 0 || table >= ix->L) return 0;
+    return ix->buckets[table];
+}
+const unsigned* culsh_index_bucket_counts(culsh_index* ix) {
+    if (!ix || !ix->indexed) return nullptr;
+    return ix->buckets.data();
+}
+#define HOST_GETTER(name, member)                                                     \
+    if (!ix || !ix->indexed || table < 0 || table >= ix->L) return nullptr;           \
+    if (ensure_host(ix) != CULSH_OK) return nullptr;                                  \
+    return ix->member[table].data();
+const unsigned* culsh_index_total_indices(culsh_index* ix, int table) { HOST_GETTER(total_indices, h_ids) }
+const unsigned* culsh_index_starting_indices(culsh_index* ix, int table) { HOST_GETTER(starting_indices, h_starts) }
+const unsigned* culsh_index_sizes(culsh_index* ix, int table) { HOST_GETTER(sizes, h_sizes) }
+const float* culsh_index_codes(culsh_index* ix, int table) { HOST_GETTER(codes, h_codes) }
+#undef HOST_GETTER
+
+int culsh_search_create(culsh_search** out) {
+    if (!out) return fail(CULSH_ERR_INVALID_ARGUMENT, "null output pointer");
+    *out = new (std::nothrow) culsh_search();
+    return *out ? CULSH_OK : fail(CULSH_ERR_OUT_OF_MEMORY, "host allocation failed");
+}
+
+void culsh_search_destroy(culsh_search* s) { delete s; }
+
+int culsh_search_reset(culsh_search* s, culsh_index* ix, int K, int T) {
+    if (!s) return fail(CULSH_ERR_INVALID_ARGUMENT, "null search");
+    s->ix = ix;
+    s->L = ix ? ix->L : 0;
+    s->K = K;
+    s->T = T;
+    s->Q = 0;
+    s->searched = false;
+    s->qb_host_valid = false;
+    s->tot_unique = s->tot_nonunique = 0;
+    s->times = culsh_times{};
+    return CULSH_OK;
+}
+
+static int precheck_search(culsh_search* s, int Q) {
+    if (!s) return fail(CULSH_ERR_INVALID_ARGUMENT, "null search");
+    if (!s->ix) return fail(CULSH_ERR_STATE, "No indexing structure has been associated with searching structure...");
+    if (Q <= 0 || s->L <= 0 || s->K <= 0 || s->T <= 0)
+        return fail(CULSH_ERR_INVALID_ARGUMENT,
+                    "Integer parameters must be all positive. Have you reset the indexing structure properly before assigning it to this searching structure???");
+    if (s->L != s->ix->L) return fail(CULSH_ERR_STATE, "the index changed since SearchTables::reset");
+    if (s->K > CULSH_MAX_K) return fail(CULSH_ERR_CAPACITY, "K = %d exceeds the supported maximum %d", s->K, CULSH_MAX_K);
+    if (s->T > CULSH_MAX_T) return fail(CULSH_ERR_CAPACITY, "T = %d exceeds the supported maximum %d", s->T, CULSH_MAX_T);
+    if (!s->ix->indexed) return fail(CULSH_ERR_STATE, "the index structure has not been indexed or loaded");
+    return CULSH_OK;
+}
+
+int culsh_search_run(culsh_search* s, const float* queries, int Q, const float* dataset, FILE* dbg) {
+    TRY(precheck_search(s, Q));
+    if (!queries) return fail(CULSH_ERR_INVALID_ARGUMENT, "null queries");
+    culsh_index* ix = s->ix;
+    TRY(ensure_stream(&s->stream));
+    cudaStream_t st = s->stream;
+    s->searched = false;
+    s->qb_host_valid = false;
+    const double t0 = seconds_now();
+    TRY(ensure_device(ix, st));
+    if (dataset && !ix->x_borrow && !(ix->X.p && ix->x_src == dataset)) {
+        CU_TRY(ix->X.reserve((size_t)ix->N * ix->D));
+        CU_TRY(cudaMemcpyAsync(ix->X.p, dataset, sizeof(float) * (size_t)ix->N * ix->D, cudaMemcpyHostToDevice, st));
+        ix->x_src = dataset;
+    }
+    if (!ix->dev_x()) return fail(CULSH_ERR_INVALID_ARGUMENT, "null dataset and no dataset on the device");
+    const int D = ix->D, K = s->K;
+    CU_TRY(s->dq.reserve((size_t)Q * D));
+    CU_TRY(s->oids.reserve((size_t)Q * K));
+    CU_TRY(s->od.reserve((size_t)Q * K));
+    CU_TRY(s->h_ids.reserve((size_t)Q * K));
+    CU_TRY(s->h_d.reserve((size_t)Q * K));
+    CU_TRY(cudaMemcpyAsync(s->dq.p, queries, sizeof(float) * (size_t)Q * D, cudaMemcpyHostToDevice, st));
+    if (dbg) fprintf(dbg, "[SearchTables::search]\tPerforming searching. (Q, K, T) = (%d, %d, %d)\n", Q, K, s->T);
+    TRY(search_device(s, s->dq.p, Q, s->oids.p, s->od.p, st));
+    CU_TRY(cudaMemcpyAsync(s->h_ids.p, s->oids.p, 4 * (size_t)Q * K, cudaMemcpyDeviceToHost, st));
+    CU_TRY(cudaMemcpyAsync(s->h_d.p, s->od.p, 4 * (size_t)Q * K, cudaMemcpyDeviceToHost, st));
+    CU_TRY(cudaEventRecord(s->ev[4], st));
+    CU_TRY(cudaStreamSynchronize(st));
+    s->host_copy_timed = true;
+    float ms[3] = {0, 0, 0};
+    cudaEventElapsedTime(&ms[0], s->ev[0], s->ev[2]);
+    cudaEventElapsedTime(&ms[1], s->ev[2], s->ev[3]);
+    cudaEventElapsedTime(&ms[2], s->ev[3], s->ev[4]);
+    s->times = culsh_times{ms[0] / 1e3f, 0.f, 0.f, 0.f, ms[1] / 1e3f, ms[2] / 1e3f};
+    s->Q = Q;
+    s->searched = true;
+    if (dbg)
+        fprintf(dbg, "[SearchTables::search]\tNon-unique: %llu, unique: %llu, selectivity: %.2f%% (%.3f ms)\n",
+                s->tot_nonunique, s->tot_unique, culsh_search_selectivity(s) * 100.0, 1e3 * (seconds_now() - t0));
+    return CULSH_OK;
+}
+
+int culsh_search_run_device(culsh_search* s, const float* d_queries, int Q, int* d_ids, float* d_dists, void* stream) {
+    TRY(precheck_search(s, Q));
+    if (!d_queries || !d_ids || !d_dists) return fail(CULSH_ERR_INVALID_ARGUMENT, "null device buffer");
+    TRY(ensure_stream(&s->stream));
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
+    s->searched = false;
+    s->qb_host_valid = false;
+    TRY(ensure_device(s->ix, st));
+    TRY(search_device(s, d_queries, Q, d_ids, d_dists, st));
+    s->Q = Q;
+    s->searched = false;   // results live in the caller's device buffers
+    return CULSH_OK;
+}
+
+const int* culsh_search_knn_ids(culsh_search* s) { return (s && s->searched) ? s->h_ids.p : nullptr; }
+const float* culsh_search_knn_distances(culsh_search* s) { return (s && s->searched) ? s->h_d.p : nullptr; }
+
+const int* culsh_search_query_buckets(culsh_search* s, int table) {
+    if (!s || !s->ix || s->Q <= 0 || table < 0 || table >= s->L || !s->qb.p) return nullptr;
+    if (!s->qb_host_valid) {
+        const size_t n = (size_t)s->L * s->Q * s->T;
+        if (s->h_qb.reserve(n) != cudaSuccess) return nullptr;
+        cudaStream_t st = s->stream;
+        if (cudaMemcpyAsync(s->h_qb.p, s->qb.p, 4 * n, cudaMemcpyDeviceToHost, st) != cudaSuccess) return nullptr;
+        if (cudaStreamSynchronize(st) != cudaSuccess) return nullptr;
+        s->qb_host_valid = true;
+    }
+    return s->h_qb.p + (size_t)table * s->Q * s->T;
+}
+
+// cuLSH_SearchTables.cu:83: unique / N / Q.
+float culsh_search_selectivity(culsh_search* s) {
+    if (!s || !s->ix || !s->ix->N || !s->Q) return 0.0f;
+    return (float)((double)s->tot_unique / (double)s->ix->N / (double)s->Q);
+}
+// cuLSH_SearchTables.cu:86: (nonUnique - unique) / unique.
+float culsh_search_nonunique_percentage(culsh_search* s) {
+    if (!s || !s->tot_unique) return 0.0f;
+    return (float)((double)(s->tot_nonunique - s->tot_unique) / (double)s->tot_unique);
+}
+unsigned long long culsh_search_total_unique(culsh_search* s) { return s ? s->tot_unique : 0; }
+unsigned long long culsh_search_total_nonunique(culsh_search* s) { return s ? s->tot_nonunique : 0; }
+void culsh_search_times(culsh_search* s, culsh_times* out) {
+    if (out) *out = s ? s->times : culsh_times{};
+}
+
+int culsh_search_profile_get(culsh_search* s, culsh_search_profile* out) {
+    if (!s || !out) return fail(CULSH_ERR_INVALID_ARGUMENT, "null argument");
+    *out = culsh_search_profile{};
+    if (!s->ev[0] || s->Q <= 0) return fail(CULSH_ERR_STATE, "no search has run");
+    CU_TRY(cudaEventSynchronize(s->ev[3]));
+    CU_TRY(cudaEventElapsedTime(&out->project_ms, s->ev[0], s->ev[1]));
+    CU_TRY(cudaEventElapsedTime(&out->probe_ms, s->ev[1], s->ev[2]));
+    CU_TRY(cudaEventElapsedTime(&out->candidates_ms, s->ev[2], s->ev[3]));
+    out->launches = s->launches;
+    out->deferred_queries = s->deferred_queries;
+    out->key_words = s->ix ? s->ix->KW : 0;
+    return CULSH_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,184 @@
+// Internal declarations shared by the CUDA translation units of libculsh.
+//
+// Device data model of one index (all tables stacked, one allocation each):
+//   X        [N][D]  f32    dataset, point-contiguous (the reference's D x N column-major)
+//   A        [L*M][D] f32   projection columns; column (l,m) = A[l][m*D .. m*D+D)
+//   b        [L*M]   f32
+//   cmin/cmax[L*M]   i32    per (table, column) code range
+//   fbits/foff[L*M]         bit width / bit offset of each column's field in the packed key
+//   ids      [L][N]  u32    point ids sorted by (code row, id): the reference's totalIndices
+//   boff     [L+1]   u64    bucket offsets: buckets of table l are [boff[l], boff[l+1])
+//   starts/sizes [sum B]    bucket start (within the table's ids) and size
+//   ukeys    [sum B][KW]    packed key of each bucket (column 0 in the most significant bits)
+//   hslots   [sum H]  u64   open-addressing hash (bucket index | fingerprint << 32)
+//   hoff     [L+1]   u64    slot offsets;  hmask[L] u32 power-of-two capacity - 1
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace culsh {
+
+constexpr int kMaxM = 64;     // projection columns per table
+constexpr int kMaxKW = 8;     // packed key words (256 bits)
+constexpr int kMaxT = 256;    // probes per table
+constexpr int kMaxK = 2048;   // neighbours per query
+constexpr unsigned long long kEmptySlot = ~0ull;
+
+// Device error flags (bit values OR-ed into an int in device memory).
+enum DevErr : int {
+    kErrNonFinite = 1,     // projection produced NaN/Inf
+    kErrCodeRange = 2,     // |code| >= 2^31
+    kErrSpin = 4,          // a bounded wait gave up
+    kErrHashFull = 8,      // hash insert ran out of probes
+    kErrNotIntegral = 16,  // a loaded bucket code is not an integer
+};
+
+// Public 32-bit mixer ("lowbias32", C. Wellons, public domain).
+__host__ __device__ __forceinline__ uint32_t mix32(uint32_t h) {
+    h ^= h >> 16;
+    h *= 0x7feb352du;
+    h ^= h >> 15;
+    h *= 0x846ca68bu;
+    h ^= h >> 16;
+    return h;
+}
+
+__host__ __device__ __forceinline__ uint32_t key_hash(const uint32_t* k, int KW, uint32_t seed) {
+    uint32_t h = seed;
+    for (int w = 0; w < KW; ++w) h = mix32(h ^ k[w]) + 0x9e3779b9u * (uint32_t)(w + 1);
+    return mix32(h);
+}
+
+constexpr uint32_t kSeedSlot = 0x2545f491u;
+constexpr uint32_t kSeedFp = 0x68e31da4u;
+
+// Place a field of `bits` bits (<= 32) at bit offset `off` of a little-endian
+// multi-word key.
+__host__ __device__ __forceinline__ void key_put(uint32_t* key, int off, int bits, uint32_t val) {
+    const int w = off >> 5, s = off & 31;
+    key[w] |= val << s;
+    if (s != 0 && s + bits > 32) key[w + 1] |= val >> (32 - s);
+}
+
+__host__ __device__ __forceinline__ uint32_t key_get(const uint32_t* key, int off, int bits) {
+    if (bits == 0) return 0;
+    const int w = off >> 5, s = off & 31;
+    uint64_t v = key[w] >> s;
+    if (s != 0 && s + bits > 32) v |= (uint64_t)key[w + 1] << (32 - s);
+    return bits == 32 ? (uint32_t)v : (uint32_t)(v & ((1ull << bits) - 1));
+}
+
+// Per-table key layout and lookup structures (device pointers).
+struct LookupView {
+    int L, M, KW;
+    const int32_t* cmin;
+    const int32_t* cmax;
+    const uint8_t* fbits;
+    const uint16_t* foff;
+    const uint64_t* boff;
+    const uint32_t* starts;
+    const uint32_t* sizes;
+    const uint32_t* ukeys;
+    const unsigned long long* hslots;
+    const uint64_t* hoff;
+    const uint32_t* hmask;
+};
+
+// ---------------------------------------------------------------------------
+// Launchers (each returns cudaGetLastError() after the launch).
+
+// Canonical FP32 projection of n_pts points onto the LM stacked columns.
+// codes != nullptr: floored codes [LM][n_pts] + per-block min/max partials
+// [grid_x][LM]; vals != nullptr: unfloored values [LM][n_pts].
+cudaError_t launch_project_fp32(const float* X, int64_t n_pts, int D, const float* A, const float* b, int LM,
+                                float W, int32_t* codes, float* vals, int32_t* pmin, int32_t* pmax, int* err,
+                                cudaStream_t st);
+int project_grid_x(int64_t n_pts);
+cudaError_t launch_minmax_reduce(const int32_t* pmin, const int32_t* pmax, int nparts, int LM, int32_t* cmin,
+                                 int32_t* cmax, cudaStream_t st);
+
+// Key packing from int codes [LM][N] into SoA keys [KW][L*N] and identity values.
+cudaError_t launch_pack_keys(const int32_t* codes, int64_t N, int L, int M, int KW, const int32_t* cmin,
+                             const uint8_t* fbits, const uint16_t* foff, uint32_t* keys, uint32_t* vals,
+                             cudaStream_t st);
+
+// Onesweep segmented LSD radix sort of L segments of N (key, value) pairs.
+// Sorts bits [0, 8*passes) of the KW-word keys. Buffers are ping-ponged; on
+// return *result_in_alt tells whether the sorted data sits in the alt buffers.
+struct SortBuffers {
+    uint32_t* keys[2];   // [KW][L*N] each
+    uint32_t* vals[2];   // [L*N] each
+    uint32_t* hist;      // [L][passes][256]
+    uint32_t* base;      // [L][passes][256]
+    uint32_t* status;    // [L*tiles][256] + counter
+    int* err;
+};
+size_t sort_status_words(int64_t N, int L);
+cudaError_t run_segmented_sort(SortBuffers& sb, int64_t N, int L, int KW, int passes, bool* result_in_alt,
+                               cudaStream_t st);
+
+// Run-length bucketing of sorted keys. Two phases: count (per table bucket
+// totals, written to nb[L]) and write (starts, ukeys).
+cudaError_t launch_rl_count(const uint32_t* keys, int64_t N, int L, int KW, uint32_t* tile_cnt, uint32_t* tile_off,
+                            uint32_t* nb, cudaStream_t st);
+cudaError_t launch_rl_write(const uint32_t* keys, int64_t N, int L, int KW, const uint32_t* tile_off,
+                            const uint64_t* boff, uint32_t* starts, uint32_t* ukeys, cudaStream_t st);
+cudaError_t launch_bucket_sizes(const uint64_t* boff, const uint32_t* starts, int64_t N, int L, int64_t maxB,
+                                uint32_t* sizes, cudaStream_t st);
+cudaError_t launch_hash_build(const uint64_t* boff, const uint32_t* ukeys, int L, int KW, int64_t maxB,
+                              const uint64_t* hoff, const uint32_t* hmask, unsigned long long* hslots, int* err,
+                              cudaStream_t st);
+// Bucket codes [M][B_l] per table (float, the reference's layout) decoded from ukeys.
+cudaError_t launch_decode_codes(const uint64_t* boff, const uint32_t* ukeys, int L, int M, int KW, int64_t maxB,
+                                const int32_t* cmin, const uint8_t* fbits, const uint16_t* foff, float* codes,
+                                cudaStream_t st);
+// From loaded float bucket codes: per (l,m) min/max + integrality check, then ukeys.
+cudaError_t launch_codes_minmax(const uint64_t* boff, const float* codes, int L, int M, int64_t maxB,
+                                int32_t* cmin, int32_t* cmax, int* err, cudaStream_t st);
+cudaError_t launch_pack_from_codes(const uint64_t* boff, const float* codes, int L, int M, int KW, int64_t maxB,
+                                   const int32_t* cmin, const uint8_t* fbits, const uint16_t* foff, uint32_t* ukeys,
+                                   cudaStream_t st);
+
+// Random projection (seeded counter-based generator): A ~ N(0,1), u ~ U(0,1].
+cudaError_t launch_random_projection(float* A, float* u, int64_t nA, int64_t nu, unsigned long long seed,
+                                     cudaStream_t st);
+
+// Query side.
+struct ProbeArgs {
+    const float* vals;         // [L*M][Q] unfloored projections
+    int Q, T;
+    LookupView lv;
+    int32_t* qbuckets;         // [L][Q*T]
+    unsigned long long* cnu;   // [Q] non-unique candidate counts (accumulated)
+};
+cudaError_t launch_probe(const ProbeArgs& a, cudaStream_t st);
+
+struct CandArgs {
+    const float* X;
+    int64_t N;
+    int D, L, T, Q, K;
+    const float* queries;              // [Q][D]
+    const int32_t* qbuckets;           // [L][Q*T]
+    const uint64_t* boff;
+    const uint32_t* starts;
+    const uint32_t* sizes;
+    const uint32_t* ids;               // [L][N]
+    const unsigned long long* cnu;     // [Q]
+    int32_t* out_ids;                  // [Q][K]
+    float* out_d;                      // [Q][K]
+    unsigned long long* cu;            // [Q] unique counts
+    unsigned long long* totals;        // [2]: sum unique, sum non-unique
+    uint32_t* arena;                   // overflow hash sets for large candidate sets
+    unsigned long long arena_words;
+    unsigned long long* arena_top;
+    int* deferred;                     // [Q] list of queries that did not fit the arena
+    unsigned int* n_deferred;
+    const int* qlist;                  // optional subset of queries (nullptr = all)
+    int nq;
+};
+int cand_smem_capacity();              // candidates handled in shared memory per query
+cudaError_t launch_candidates(const CandArgs& a, cudaStream_t st);
+size_t cand_arena_words(unsigned long long nonunique);
+
+}  // namespace culsh

@@ -1,0 +1,142 @@
+/*
+ * culsh.h - C ABI of libculsh, a GB300-native (sm_103a) Euclidean LSH index
+ * and k-nearest-neighbour search with the behaviour of cuLSH (ariskag/cuLSH).
+ *
+ * Plain C: opaque handles, plain pointers and sizes, int status codes. Every
+ * entry point replaces one member of the reference's header-only C++ classes
+ * cuLSH::HashTables (cuLSH_HashTables.cu) and cuLSH::SearchTables
+ * (cuLSH_SearchTables.cu); the citation beside each one names the member.
+ * The drop-in C++ classes in cuLSH.h are thin inline wrappers over this ABI.
+ *
+ * Conventions (identical to the reference):
+ *   dataset X  : D x N float, column-major (point n is X[n*D .. n*D+D))
+ *   queries    : D x Q float, column-major
+ *   A[l]       : D x M float, column-major (column m is A[l][m*D .. m*D+D)); b[l]: M floats
+ *   knn ids    : K x Q int, column-major (query q is ids[q*K .. q*K+K)), -1 = no neighbour
+ *   knn dists  : K x Q float, SQUARED Euclidean distances, FLT_MAX = no neighbour
+ *   query buckets of table l: Q x T int, entry q*T+t (probe t of query q), -1 = no bucket
+ *
+ * Status codes: 0 on success, a CULSH_ERR_* value otherwise; culsh_last_error()
+ * returns the message of the last failure on the calling thread.
+ * Objects are not thread-safe; calls on one object are synchronous.
+ */
+#ifndef CULSH_C_ABI_H
+#define CULSH_C_ABI_H
+
+#include <stdio.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CULSH_OK 0
+#define CULSH_ERR_INVALID_ARGUMENT 1 /* a parameter is out of its domain               */
+#define CULSH_ERR_STATE 2            /* call order violated (e.g. search before index)  */
+#define CULSH_ERR_CUDA 3             /* a CUDA runtime call failed                       */
+#define CULSH_ERR_OUT_OF_MEMORY 4    /* host or device allocation failed / admission    */
+#define CULSH_ERR_IO 5               /* file could not be opened, read or written        */
+#define CULSH_ERR_NUMERIC 6          /* non-finite projection or code beyond int32       */
+#define CULSH_ERR_CAPACITY 7         /* size beyond a documented limit of this library   */
+#define CULSH_ERR_DEVICE 8           /* a device-side bounded wait or insert gave up     */
+#define CULSH_ERR_FORMAT 9           /* index file truncated or inconsistent             */
+
+/* Limits of this implementation (the reference has the memory limits only). */
+#define CULSH_MAX_M 64      /* projection columns per table               */
+#define CULSH_MAX_T 256     /* probes per table and query                 */
+#define CULSH_MAX_K 2048    /* neighbours per query                       */
+#define CULSH_MAX_N ((1 << 30) - 1)
+
+typedef struct culsh_index culsh_index;   /* cuLSH::HashTables  (cuLSH_HashTables.cu:51-108)  */
+typedef struct culsh_search culsh_search; /* cuLSH::SearchTables (cuLSH_SearchTables.cu:42-107) */
+
+/* cuLSH::SearchTables::timesStruct (cuLSH_SearchTables.cu:44-52), seconds. */
+typedef struct culsh_times {
+    float buckets;   /* query projection, multiprobe codes and bucket lookup           */
+    float collect;   /* fused into `distances` (0)                                       */
+    float sort;      /* fused into `distances` (0)                                       */
+    float unique;    /* fused into `distances` (0)                                       */
+    float distances; /* candidate gather, dedup, distances and top-K (one fused kernel)  */
+    float knn;       /* copy of the K x Q results back to the host                       */
+} culsh_times;
+
+const char* culsh_last_error(void);
+int culsh_version(void);
+
+/* ---- HashTables ---------------------------------------------------------- */
+int culsh_index_create(culsh_index** out);          /* HashTables::HashTables  cuLSH_HashTables.cu:111-119 */
+void culsh_index_destroy(culsh_index* ix);          /* HashTables::~HashTables cuLSH_HashTables.cu:78 */
+
+/* HashTables::reset(N,D,L,M,W,dbg) cuLSH_HashTables.cu:190-210: random A ~ N(0,1),
+ * b = W*(u - min u), u ~ U(0,1] per table, from a seeded counter-based generator
+ * (the reference seeds cuRAND with time(0)). */
+int culsh_index_reset_random(culsh_index* ix, int N, int D, int L, int M, float W, unsigned long long seed,
+                             FILE* dbg);
+/* HashTables::reset(N,D,L,M,W,A,b,dbg) cuLSH_HashTables.cu:213-241: A and b are copied. */
+int culsh_index_reset(culsh_index* ix, int N, int D, int L, int M, float W, const float* const* A,
+                      const float* const* b, FILE* dbg);
+/* HashTables::index(matrix,dbg) cuLSH_HashTables.cu:486-520. X (host, D x N) is
+ * copied to the device and kept there for later searches. */
+int culsh_index_build(culsh_index* ix, const float* X, FILE* dbg);
+/* Device-resident variant of index(): d_X is a device pointer that stays
+ * borrowed (not copied) until the next build, reset or destroy. stream: a
+ * cudaStream_t, NULL = the object's own stream. */
+int culsh_index_build_device(culsh_index* ix, const float* d_X, void* stream);
+/* HashTables::save / load cuLSH_HashTables.cu:395-483 (identical file layout);
+ * HashTables::reset(filename,dbg) cuLSH_HashTables.cu:243-249 is load(). */
+int culsh_index_save(culsh_index* ix, const char* path, FILE* dbg);
+int culsh_index_load(culsh_index* ix, const char* path, FILE* dbg);
+
+/* Getters cuLSH_HashTables.cu:89-103. Pointers stay valid until the next
+ * reset/index/load/destroy; NULL (or 0) when unset. */
+void culsh_index_params(const culsh_index* ix, int* N, int* D, int* L, int* M, float* W);
+const float* culsh_index_A(culsh_index* ix, int table);
+const float* culsh_index_b(culsh_index* ix, int table);
+unsigned culsh_index_bucket_count(culsh_index* ix, int table);
+const unsigned* culsh_index_bucket_counts(culsh_index* ix);
+const unsigned* culsh_index_total_indices(culsh_index* ix, int table);
+const unsigned* culsh_index_starting_indices(culsh_index* ix, int table);
+const unsigned* culsh_index_sizes(culsh_index* ix, int table);
+const float* culsh_index_codes(culsh_index* ix, int table);
+
+/* ---- SearchTables -------------------------------------------------------- */
+int culsh_search_create(culsh_search** out);        /* SearchTables::SearchTables  cuLSH_SearchTables.cu:112-122 */
+void culsh_search_destroy(culsh_search* s);         /* SearchTables::~SearchTables cuLSH_SearchTables.cu:74 */
+/* SearchTables::reset(hashtables,K,T) cuLSH_SearchTables.cu:127-139 (ix is not owned). */
+int culsh_search_reset(culsh_search* s, culsh_index* ix, int K, int T);
+/* SearchTables::search(queries,Q,dataset,dbg) cuLSH_SearchTables.cu:197-463.
+ * dataset must be the indexed dataset; when it is the pointer given to
+ * culsh_index_build (or NULL after a build) the device copy is reused. */
+int culsh_search_run(culsh_search* s, const float* queries, int Q, const float* dataset, FILE* dbg);
+/* Device-resident variant: d_queries (D x Q) in device memory, results written
+ * to the caller's device buffers d_ids / d_dists (K x Q). */
+int culsh_search_run_device(culsh_search* s, const float* d_queries, int Q, int* d_ids, float* d_dists,
+                            void* stream);
+
+/* Getters cuLSH_SearchTables.cu:83-105. */
+const int* culsh_search_knn_ids(culsh_search* s);
+const float* culsh_search_knn_distances(culsh_search* s);
+const int* culsh_search_query_buckets(culsh_search* s, int table);
+float culsh_search_selectivity(culsh_search* s);
+float culsh_search_nonunique_percentage(culsh_search* s);
+unsigned long long culsh_search_total_unique(culsh_search* s);
+unsigned long long culsh_search_total_nonunique(culsh_search* s);
+void culsh_search_times(culsh_search* s, culsh_times* out);
+
+/* Measurement aid with no counterpart in the reference: device time of each
+ * stage of the last search (CUDA events on the launching stream) and the
+ * number of kernels it launched. */
+typedef struct culsh_search_profile {
+    float project_ms;    /* query projection onto all L*M columns             */
+    float probe_ms;      /* multiprobe codes + hash lookup + non-unique counts */
+    float candidates_ms; /* gather + dedup + distances + top-K (incl. re-runs) */
+    int launches;        /* kernels launched by libculsh in the last search    */
+    int deferred_queries;/* queries re-run after growing the overflow arena    */
+    int key_words;       /* 32-bit words of a packed bucket key (index layout) */
+} culsh_search_profile;
+int culsh_search_profile_get(culsh_search* s, culsh_search_profile* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CULSH_C_ABI_H */

@@ -1,0 +1,460 @@
+// CPU ORACLE for the Euclidean LSH index build and search of cuLSH.
+//
+// TEST INFRASTRUCTURE ONLY. This file is the checker, never the product:
+// only tests/, __graft_entry__.smoke() and the cpu_baseline leg of bench.py
+// may load it. The product path (culsh_gb300/) never links or calls it.
+//
+// It restates, in plain sequential C++ (OpenMP only across independent
+// points, queries and tables), the algorithm of the reference library
+// ariskag/cuLSH. Every function cites the reference file:line it follows.
+//
+// Parity status: UNPINNED against the reference build. The reference ships no
+// tests, golden vectors or fixtures, and its only implementation is CUDA +
+// cuBLAS + Thrust, which cannot run on a machine without a GPU; its sources do
+// not travel to the GPU machine. The restatement is instead pinned by
+// hand-traced known-answer cases derived from reading the reference code
+// (tests/test_oracle_kat.py) and by an independent line-by-line Python
+// transliteration of the reference's multiprobe and top-K kernels
+// (tests/refsim.py).
+//
+// Canonical arithmetic (the reference's cuBLAS summation order is unspecified,
+// so this order is defined here and the CUDA kernels reproduce it bit-exactly):
+//   projection  v = fl( fl( fma-chain_{d=0..D-1}(x_d * a_d) ) - b ) / W    (true divide)
+//   code        floorf(v)
+//   distance    8 lane partials s_j = fma-chain over columns j, j+8, ...;
+//               then (s0+s4, s1+s5, s2+s6, s3+s7) -> (t0+t2, t1+t3) -> sum
+//
+// Build: oracle/Makefile (g++ -O2 -fopenmp -ffp-contract=off).
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+// cuLSH_Indexing.cu:43-51 (cublasSgemm X'*A), cuLSH_Kernels.cu:40-49 (-b),
+// cuLSH_Kernels.cu:55-64 (/W). The dot product uses the canonical sequential
+// fused-multiply-add order defined in the header.
+inline float project_one(const float* x, const float* a, int D, float b, float W) {
+    float acc = 0.0f;
+    for (int d = 0; d < D; ++d) acc = std::fmaf(x[d], a[d], acc);
+    const float shifted = acc - b;
+    return shifted / W;
+}
+
+// Lexicographic comparison of two code rows, column 0 most significant: the
+// order produced by the stable LSD sort over columns M-1..0 in
+// cuLSH_Indexing.cu:86-90 (and cuLSH_Querying.cu:47-53).
+inline int cmp_rows(const float* P, int64_t stride, int M, int64_t a, int64_t b) {
+    for (int m = 0; m < M; ++m) {
+        const float x = P[m * stride + a], y = P[m * stride + b];
+        if (x < y) return -1;
+        if (x > y) return 1;
+    }
+    return 0;
+}
+
+// Number of heap levels, ceil(log2(n)) for n >= 1, as computed by
+// __float2int_ru(log2f(n)) in cuLSH_Kernels.cu:202 and :419 (exact for the
+// integer arguments used there).
+inline int ceil_log2(int n) {
+    int l = 0;
+    while ((1 << l) < n) ++l;
+    return l;
+}
+
+// cuLSH_Kernels.cu:144-175 balanceHeap_deltas: max-heap sift-down on delta
+// indices where an empty slot (-1) ranks above every delta.
+void sift_deltas(int* perm, const float* dl, int total, int levels) {
+    int parent = 0;
+    for (int level = 0; level < levels - 1; ++level) {
+        const int left = parent * 2 + 1, right = left + 1;
+        int mx = parent;
+        if (left < total && perm[left] == -1) {
+            mx = left;
+        } else if (right < total && perm[right] == -1) {
+            mx = right;
+        } else {
+            if (left < total && dl[perm[left]] > dl[perm[mx]]) mx = left;
+            if (right < total && dl[perm[right]] > dl[perm[mx]]) mx = right;
+        }
+        if (mx == parent) break;
+        std::swap(perm[parent], perm[mx]);
+        parent = mx;
+    }
+}
+
+// cuLSH_Kernels.cu:356-398 balanceHeap_knnIds: max-heap on (distance, id).
+void sift_knn(float* heap, int* ids, int size, int levels) {
+    int parent = 0;
+    for (int level = 0; level < levels - 1; ++level) {
+        const int left = parent * 2 + 1, right = left + 1;
+        int mx = parent;
+        float diff;
+        if (left < size && (diff = heap[left] - heap[parent]) >= 0) {
+            if (diff > 0 || ids[left] > ids[parent]) mx = left;
+        }
+        if (right < size && (diff = heap[right] - heap[mx]) >= 0) {
+            if (diff > 0 || ids[right] > ids[mx]) mx = right;
+        }
+        if (mx == parent) break;
+        std::swap(heap[parent], heap[mx]);
+        std::swap(ids[parent], ids[mx]);
+        parent = mx;
+    }
+}
+
+// cuLSH_Kernels.cu:301-348 kernel_calculateDistances: squared L2 with 8
+// strided lane partials (fused by nvcc into FMAs) and a fixed tree.
+inline float dist_p4(const float* q, const float* x, int D) {
+    float s[8];
+    for (int j = 0; j < 8; ++j) {
+        float acc = 0.0f;
+        for (int c = j; c < D; c += 8) {
+            const float diff = q[c] - x[c];
+            acc = std::fmaf(diff, diff, acc);
+        }
+        s[j] = acc;
+    }
+    const float t0 = s[0] + s[4], t1 = s[1] + s[5], t2 = s[2] + s[6], t3 = s[3] + s[7];
+    const float u0 = t0 + t2, u1 = t1 + t3;
+    return u0 + u1;
+}
+
+}  // namespace
+
+extern "C" {
+
+int oracle_num_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+void oracle_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
+// Unfloored projection of n_pts points for all L*M stacked columns.
+//   X   [n_pts][D]   (the reference's D x N column-major matrix)
+//   A   [L][M][D]    (A[l] is D x M column-major, tables concatenated)
+//   b   [L][M]
+//   out [L*M][n_pts] (column (l,m) contiguous, the reference's N x M layout per table)
+// cuLSH_Indexing.cu:27-66 projectMatrix, once per table at index time
+// (cuLSH_Indexing.cu:204-211) and at query time (cuLSH_Querying.cu:191-197).
+void oracle_project(const float* X, int64_t n_pts, int D, const float* A, const float* b,
+                    int L, int M, float W, float* out) {
+    const int LM = L * M;
+#pragma omp parallel for schedule(static)
+    for (int64_t n = 0; n < n_pts; ++n) {
+        const float* x = X + n * D;
+        for (int c = 0; c < LM; ++c) out[(int64_t)c * n_pts + n] = project_one(x, A + (int64_t)c * D, D, b[c], W);
+    }
+}
+
+// Bucketing of one table from its floored codes P [M][N] (column-major).
+// cuLSH_Indexing.cu:71-93 (row sort), :98-144 (bucket boundaries and sizes),
+// :237-247 (unique code rows), :250-271 (host outputs).
+// Outputs: ids[N] (totalIndices), starts[B], sizes[B], codes[M][B] (col-major).
+// Returns B.
+int64_t oracle_bucket_table(const float* P, int64_t N, int M, uint32_t* ids, uint32_t* starts,
+                            uint32_t* sizes, float* codes) {
+    std::vector<uint32_t> perm((size_t)N);
+    std::iota(perm.begin(), perm.end(), 0u);
+    std::stable_sort(perm.begin(), perm.end(), [&](uint32_t a, uint32_t b) {
+        return cmp_rows(P, N, M, a, b) < 0;
+    });
+    int64_t B = 0;
+    for (int64_t i = 0; i < N; ++i) {
+        ids[i] = perm[i];
+        if (i == 0 || cmp_rows(P, N, M, perm[i - 1], perm[i]) != 0) starts[B++] = (uint32_t)i;
+    }
+    for (int64_t j = 0; j < B; ++j) {
+        sizes[j] = (uint32_t)((j + 1 < B ? (int64_t)starts[j + 1] : N) - (int64_t)starts[j]);
+        for (int m = 0; m < M; ++m) codes[(int64_t)m * B + j] = P[(int64_t)m * N + perm[starts[j]]];
+    }
+    return B;
+}
+
+// Full index build (cuLSH_HashTables.cu:486-520 index(), per table
+// cuLSH_Indexing.cu:181-274). Per-table outputs are packed at fixed strides:
+// ids at l*N, starts/sizes at l*N, codes at l*N*M with column stride B_l.
+void oracle_index(const float* X, int N, int D, int L, int M, float W, const float* A, const float* b,
+                  uint32_t* buckets, uint32_t* ids, uint32_t* starts, uint32_t* sizes, float* codes) {
+    std::vector<float> v((size_t)L * M * N);
+    oracle_project(X, N, D, A, b, L, M, W, v.data());
+    for (size_t i = 0; i < v.size(); ++i) v[i] = std::floor(v[i]);  // cuLSH_Kernels.cu:91-101
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int l = 0; l < L; ++l) {
+        const int64_t off = (int64_t)l * N;
+        buckets[l] = (uint32_t)oracle_bucket_table(v.data() + (int64_t)l * M * N, N, M, ids + off, starts + off,
+                                                   sizes + off, codes + off * M);
+    }
+}
+
+// Multiprobe codes of one query for one table from its unfloored projection
+// v[M]. Output rows[T][M] (row 0 is the home code).
+// cuLSH_Kernels.cu:266-289 kernel_calculateDeltas (deltas: [0,M) down, [M,2M) up),
+// cuLSH_Kernels.cu:188-257 kernel_calculateProbingCodes (heap selection of at
+// most 64 smallest deltas, heap sort, then T-1 shift/expand steps with a
+// linear minimum search). Bit masks are 64-bit here; the reference's 32-bit
+// `1 << i` (cuLSH_Kernels.cu:237,242,247) is undefined for i >= 31 and only
+// reachable when M >= 16.
+void oracle_probe_one(const float* v, int M, int T, float* rows) {
+    std::vector<float> dl(2 * M);
+    for (int m = 0; m < M; ++m) {
+        const float fl = std::floor(v[m]);
+        const float down = v[m] - fl;
+        rows[m] = fl;
+        dl[m] = down;
+        dl[m + M] = 1.0f - down;
+    }
+    if (T <= 1) return;  // cuLSH_Querying.cu:211-217: T == 1 only floors
+    const int maxT = std::min(2 * M, 64);
+    const int levels = ceil_log2(2 * M + 1);
+    int perm[64];
+    for (int i = 0; i < maxT; ++i) perm[i] = -1;
+    for (int i = 0; i < 2 * M; ++i) {
+        if (perm[0] == -1 || dl[i] < dl[perm[0]]) {
+            perm[0] = i;
+            sift_deltas(perm, dl.data(), maxT, levels);
+        }
+    }
+    for (int i = maxT - 1; i > 0; --i) {
+        std::swap(perm[0], perm[i]);
+        sift_deltas(perm, dl.data(), i, levels);
+    }
+    std::vector<uint64_t> comb(T);
+    std::vector<float> cd(T);
+    comb[0] = 1;
+    cd[0] = dl[perm[0]];
+    int size = 1;
+    for (int t = 1; t < T; ++t) {
+        float mn = FLT_MAX;
+        int mi = 0;
+        for (int i = 0; i < size; ++i) {
+            if (cd[i] < mn) {
+                mi = i;
+                mn = cd[i];
+            }
+        }
+        uint64_t probe = comb[mi];
+        float* row = rows + (int64_t)t * M;
+        for (int m = 0; m < M; ++m) row[m] = rows[m];
+        int top = 0;
+        for (int i = 0; i < 64; ++i) {
+            if (probe & (1ull << i)) {
+                row[perm[i] % M] += (perm[i] >= M) ? 1.0f : -1.0f;
+                top = i;
+            }
+        }
+        if (top < maxT - 1) {
+            probe |= 1ull << (top + 1);
+            mn = mn + dl[perm[top + 1]];
+            comb[mi] = probe;
+            cd[mi] = mn;
+            probe -= 1ull << top;
+            mn = mn - dl[perm[top]];
+            comb[size] = probe;
+            cd[size] = mn;
+            ++size;
+        }
+    }
+}
+
+// Exact-code bucket lookup: the sort-merge of cuLSH_Querying.cu:124-165
+// (stable row sort of bucket codes followed by query codes, predecessor scan,
+// then kernel_findMatchingBuckets_evaluate cuLSH_Kernels.cu:124-138) returns
+// the index of the bucket whose code row equals the probe row, else -1.
+// Bucket rows are unique and lexicographically sorted, so a binary search
+// gives the same answer.
+int32_t oracle_lookup_one(const float* row, const float* codes, int64_t B, int M) {
+    int64_t lo = 0, hi = B;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) / 2;
+        int c = 0;
+        for (int m = 0; m < M && c == 0; ++m) {
+            const float x = codes[(int64_t)m * B + mid];
+            c = (x < row[m]) ? -1 : (x > row[m]) ? 1 : 0;
+        }
+        if (c == 0) return (int32_t)mid;
+        if (c < 0) lo = mid + 1;
+        else hi = mid;
+    }
+    return -1;
+}
+
+// Top-K of one query's unique candidates (ids ascending, with distances).
+//   tie_mode 0: ascending (distance, id); ties go to the smaller id.
+//   tie_mode 1: the reference's own heap (cuLSH_Kernels.cu:406-456): candidates
+//               visited in descending id order, strict '<' against the root of a
+//               max-heap ordered by (distance, id), then heap-sorted.
+// Entries at or above FLT_MAX (and NaN) never enter, as in the reference.
+// Output padding is (-1, FLT_MAX) (cuLSH_Querying.cu:243-246).
+void oracle_topk(const uint32_t* cand, const float* dist, int64_t C, int K, int tie_mode, int32_t* oid, float* od) {
+    if (tie_mode == 1) {
+        for (int k = 0; k < K; ++k) {
+            od[k] = FLT_MAX;
+            oid[k] = -1;
+        }
+        const int lv = ceil_log2(K + 1);
+        for (int64_t i = C - 1; i >= 0; --i) {
+            if (dist[i] < od[0]) {
+                od[0] = dist[i];
+                oid[0] = (int32_t)cand[i];
+                sift_knn(od, oid, K, lv);
+            }
+        }
+        for (int i = K - 1; i >= 1; --i) {
+            std::swap(od[0], od[i]);
+            std::swap(oid[0], oid[i]);
+            sift_knn(od, oid, i, ceil_log2(i + 1));
+        }
+        return;
+    }
+    std::vector<std::pair<float, uint32_t>> pr;
+    pr.reserve((size_t)C);
+    for (int64_t i = 0; i < C; ++i)
+        if (dist[i] < FLT_MAX) pr.emplace_back(dist[i], cand[i]);
+    const size_t kk = std::min<size_t>((size_t)K, pr.size());
+    std::partial_sort(pr.begin(), pr.begin() + kk, pr.end());
+    for (int k = 0; k < K; ++k) {
+        if ((size_t)k < kk) {
+            od[k] = pr[k].first;
+            oid[k] = (int32_t)pr[k].second;
+        } else {
+            od[k] = FLT_MAX;
+            oid[k] = -1;
+        }
+    }
+}
+
+// Full search (cuLSH_SearchTables.cu:197-463).
+// tie_mode selects the top-K semantics of oracle_topk.
+// Outputs:
+//   qbuckets [L][Q*T]  matched bucket per probe or -1 (getQueryBuckets)
+//   knn_ids  [Q][K], knn_dists [Q][K] (squared), padding (-1, FLT_MAX)
+//   nonunique[Q], unique[Q] candidate counts (cuLSH_SearchTables.cu:250-255, :354-363)
+void oracle_search(const float* X, int N, int D, int L, int M, float W, const float* A, const float* b,
+                   const uint32_t* buckets, const uint32_t* ids, const uint32_t* starts, const uint32_t* sizes,
+                   const float* codes, const float* queries, int Q, int K, int T, int tie_mode,
+                   int32_t* qbuckets, int32_t* knn_ids, float* knn_dists, uint64_t* nonunique,
+                   uint64_t* unique) {
+    const int LM = L * M;
+    std::vector<float> v((size_t)LM * Q);
+    oracle_project(queries, Q, D, A, b, L, M, W, v.data());
+#pragma omp parallel
+    {
+        std::vector<float> vq(M), rows((size_t)T * M);
+        std::vector<uint32_t> cand;
+        std::vector<float> dist;
+#pragma omp for schedule(dynamic, 16)
+        for (int q = 0; q < Q; ++q) {
+            uint64_t nu = 0;
+            cand.clear();
+            for (int l = 0; l < L; ++l) {
+                for (int m = 0; m < M; ++m) vq[m] = v[(int64_t)(l * M + m) * Q + q];
+                oracle_probe_one(vq.data(), M, T, rows.data());
+                const int64_t B = buckets[l];
+                const float* cl = codes + (int64_t)l * N * M;
+                for (int t = 0; t < T; ++t) {
+                    const int32_t bk = oracle_lookup_one(rows.data() + (int64_t)t * M, cl, B, M);
+                    qbuckets[(int64_t)l * Q * T + (int64_t)q * T + t] = bk;
+                    if (bk >= 0) {
+                        const uint32_t st = starts[(int64_t)l * N + bk], sz = sizes[(int64_t)l * N + bk];
+                        nu += sz;
+                        const uint32_t* src = ids + (int64_t)l * N + st;
+                        cand.insert(cand.end(), src, src + sz);
+                    }
+                }
+            }
+            std::sort(cand.begin(), cand.end());  // cuLSH_SearchTables.cu:346-360
+            cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+            nonunique[q] = nu;
+            unique[q] = cand.size();
+            const float* qv = queries + (int64_t)q * D;
+            dist.resize(cand.size());
+            for (size_t i = 0; i < cand.size(); ++i) dist[i] = dist_p4(qv, X + (int64_t)cand[i] * D, D);
+            oracle_topk(cand.data(), dist.data(), (int64_t)cand.size(), K, tie_mode, knn_ids + (int64_t)q * K,
+                        knn_dists + (int64_t)q * K);
+        }
+    }
+}
+
+// Squared L2 distance of one pair in the canonical (reference kernel) order.
+float oracle_distance(const float* q, const float* x, int D) { return dist_p4(q, x, D); }
+
+// Exact kNN in FP64 for recall: ascending (distance, id), squared distances.
+void oracle_exact_knn(const float* X, int N, int D, const float* queries, int Q, int K, int32_t* ids,
+                      double* dists) {
+#pragma omp parallel
+    {
+        std::vector<std::pair<double, int32_t>> pr((size_t)N);
+#pragma omp for schedule(dynamic, 4)
+        for (int q = 0; q < Q; ++q) {
+            const float* qv = queries + (int64_t)q * D;
+            for (int n = 0; n < N; ++n) {
+                const float* x = X + (int64_t)n * D;
+                double s = 0.0;
+                for (int d = 0; d < D; ++d) {
+                    const double t = (double)qv[d] - (double)x[d];
+                    s += t * t;
+                }
+                pr[n] = {s, n};
+            }
+            const int kk = std::min(K, N);
+            std::partial_sort(pr.begin(), pr.begin() + kk, pr.end());
+            for (int k = 0; k < K; ++k) {
+                ids[(int64_t)q * K + k] = k < kk ? pr[k].second : -1;
+                dists[(int64_t)q * K + k] = k < kk ? pr[k].first : INFINITY;
+            }
+        }
+    }
+}
+
+// Index file in the reference layout (cuLSH_HashTables.cu:395-438):
+// int N, D, L, M; float W; per table A[l] (D*M), b[l] (M); unsigned buckets[L];
+// per table totalIndices (N), startingIndices (B), sizes (B), codes (B*M).
+int oracle_save(const char* path, int N, int D, int L, int M, float W, const float* A, const float* b,
+                const uint32_t* buckets, const uint32_t* ids, const uint32_t* starts, const uint32_t* sizes,
+                const float* codes) {
+    FILE* fp = std::fopen(path, "wb");
+    if (!fp) return 1;
+    int ok = 1;
+    ok &= std::fwrite(&N, 4, 1, fp) == 1;
+    ok &= std::fwrite(&D, 4, 1, fp) == 1;
+    ok &= std::fwrite(&L, 4, 1, fp) == 1;
+    ok &= std::fwrite(&M, 4, 1, fp) == 1;
+    ok &= std::fwrite(&W, 4, 1, fp) == 1;
+    for (int l = 0; l < L; ++l) {
+        ok &= std::fwrite(A + (int64_t)l * D * M, 4, (size_t)D * M, fp) == (size_t)D * M;
+        ok &= std::fwrite(b + (int64_t)l * M, 4, (size_t)M, fp) == (size_t)M;
+    }
+    ok &= std::fwrite(buckets, 4, (size_t)L, fp) == (size_t)L;
+    for (int l = 0; l < L; ++l) {
+        const size_t B = buckets[l];
+        ok &= std::fwrite(ids + (int64_t)l * N, 4, (size_t)N, fp) == (size_t)N;
+        ok &= std::fwrite(starts + (int64_t)l * N, 4, B, fp) == B;
+        ok &= std::fwrite(sizes + (int64_t)l * N, 4, B, fp) == B;
+        ok &= std::fwrite(codes + (int64_t)l * N * M, 4, B * M, fp) == B * M;
+    }
+    ok &= std::fclose(fp) == 0;
+    return ok ? 0 : 1;
+}
+
+}  // extern "C"

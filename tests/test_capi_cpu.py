@@ -1,0 +1,217 @@
+"""Host-side checks of libculsh that need no GPU: the library loads and exports
+every entry point of include/culsh.h, the index file layout round-trips
+byte for byte, corrupt files and bad arguments fail with the right status,
+compute without a GPU fails loudly, and the drop-in C++ header compiles and
+links."""
+
+import os
+import re
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, ROOT, cuda_device_count, load_case
+
+HEADER = os.path.join(ROOT, "include", "culsh.h")
+INDEX_BIN = os.path.join(GOLDEN, "odd_d13.index.bin")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(culsh_[A-Za-z_0-9]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(culsh):
+    names = declared_functions()
+    assert len(names) >= 30
+    lib = culsh.lib()
+    for n in names:
+        assert hasattr(lib, n), n
+    assert sorted(culsh.ABI) == names, "python bindings must cover the header exactly"
+    assert culsh.lib().culsh_version() >= 10000
+
+
+def test_nm_lists_the_exports(culsh):
+    nm = shutil.which("nm")
+    if nm is None:
+        pytest.skip("nm not available")
+    out = subprocess.run([nm, "-D", "--defined-only", culsh.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\bT (culsh_[A-Za-z_0-9]+)", out))
+    assert set(declared_functions()) <= exported
+
+
+def test_load_getters_and_byte_identical_save(culsh, tmp_path):
+    c = load_case("odd_d13")
+    ht = culsh.HashTables()
+    ht.load(INDEX_BIN)
+    L, M, D = c["A"].shape
+    assert (ht.getN(), ht.getD(), ht.getL(), ht.getM()) == (c["X"].shape[0], D, L, M)
+    assert ht.getW() == float(c["W"])
+    np.testing.assert_array_equal(ht.getBuckets(), c["buckets"])
+    for l in range(L):
+        np.testing.assert_array_equal(ht.getA(l), c["A"][l])
+        np.testing.assert_array_equal(ht.getb(l), c["b"][l])
+        assert ht.getBuckets(l) == c["buckets"][l]
+        np.testing.assert_array_equal(ht.getBuckets_totalIndices(l), c[f"ids_{l}"])
+        np.testing.assert_array_equal(ht.getBuckets_startingIndices(l), c[f"starts_{l}"])
+        np.testing.assert_array_equal(ht.getBuckets_sizes(l), c[f"sizes_{l}"])
+        np.testing.assert_array_equal(ht.getBuckets_codes(l), c[f"codes_{l}"])
+    out = tmp_path / "again.bin"
+    ht.save(str(out))
+    assert out.read_bytes() == open(INDEX_BIN, "rb").read()
+    ht2 = culsh.HashTables()
+    ht2.reset(str(out))   # reset(filename) is load()
+    np.testing.assert_array_equal(ht2.getBuckets_codes(1), c["codes_1"])
+
+
+def _expect(culsh, code, fn, *a, **k):
+    with pytest.raises(culsh.CulshError) as ei:
+        fn(*a, **k)
+    assert ei.value.code == code, str(ei.value)
+    return str(ei.value)
+
+
+def test_corrupt_index_files_are_rejected(culsh, tmp_path):
+    raw = open(INDEX_BIN, "rb").read()
+    ht = culsh.HashTables()
+    _expect(culsh, culsh.ERR_IO, ht.load, str(tmp_path / "missing.bin"))
+    p = tmp_path / "t.bin"
+    p.write_bytes(raw[:10])
+    _expect(culsh, culsh.ERR_FORMAT, ht.load, str(p))
+    p.write_bytes(raw[:-4])
+    _expect(culsh, culsh.ERR_FORMAT, ht.load, str(p))
+    p.write_bytes(raw + b"\0\0\0\0")
+    _expect(culsh, culsh.ERR_FORMAT, ht.load, str(p))
+    bad = bytearray(raw)
+    bad[12:16] = np.int32(0).tobytes()      # M = 0
+    p.write_bytes(bytes(bad))
+    _expect(culsh, culsh.ERR_FORMAT, ht.load, str(p))
+    # Break the first bucket start of table 0 (must be 0).
+    c = load_case("odd_d13")
+    N = c["X"].shape[0]
+    L, M, D = c["A"].shape
+    off = 20 + 4 * L * (D * M + M) + 4 * L + 4 * N
+    bad = bytearray(raw)
+    bad[off:off + 4] = np.uint32(5).tobytes()
+    p.write_bytes(bytes(bad))
+    _expect(culsh, culsh.ERR_FORMAT, ht.load, str(p))
+    # An id out of range.
+    bad = bytearray(raw)
+    bad[20 + 4 * L * (D * M + M) + 4 * L: 24 + 4 * L * (D * M + M) + 4 * L] = np.uint32(N + 7).tobytes()
+    p.write_bytes(bytes(bad))
+    _expect(culsh, culsh.ERR_FORMAT, ht.load, str(p))
+    # A valid load still works afterwards.
+    ht.load(INDEX_BIN)
+    assert ht.getL() == L
+
+
+def test_parameter_and_state_errors(culsh):
+    ht = culsh.HashTables()
+    A = np.zeros((1, 2, 3), np.float32)
+    b = np.zeros((1, 2), np.float32)
+    _expect(culsh, culsh.ERR_INVALID_ARGUMENT, ht.reset, 10, 3, 1, 0, 1.0, A=A[:, :0], b=b[:, :0])
+    _expect(culsh, culsh.ERR_INVALID_ARGUMENT, ht.reset, 10, 3, 1, 2, -1.0, A=A, b=b)
+    _expect(culsh, culsh.ERR_INVALID_ARGUMENT, ht.reset, 0, 3, 1, 2, 1.0, A=A, b=b)
+    big = np.zeros((1, 65, 3), np.float32)
+    _expect(culsh, culsh.ERR_CAPACITY, ht.reset, 10, 3, 1, 65, 1.0, A=big, b=np.zeros((1, 65), np.float32))
+    _expect(culsh, culsh.ERR_CAPACITY, ht.reset, 1 << 30, 3, 1, 2, 1.0, A=A, b=b)
+    fresh = culsh.HashTables()
+    _expect(culsh, culsh.ERR_STATE, fresh.index, np.zeros(0, np.float32))
+    _expect(culsh, culsh.ERR_STATE, fresh.save, "/nonexistent/x.bin")
+    st = culsh.SearchTables()
+    _expect(culsh, culsh.ERR_STATE, st.search_device, 0, 1, 0, 0)  # no index attached
+    ht.reset(10, 3, 1, 2, 1.0, A=A, b=b)
+    st.reset(ht, 5, 1)
+    _expect(culsh, culsh.ERR_STATE, st.search, np.zeros((1, 3), np.float32), 1, None)  # not indexed
+    loaded = culsh.HashTables()
+    loaded.load(INDEX_BIN)
+    st.reset(loaded, 0, 1)
+    _expect(culsh, culsh.ERR_INVALID_ARGUMENT, st.search, np.zeros((1, 13), np.float32), 1, None)
+    st.reset(loaded, culsh.MAX_K + 1, 1)
+    _expect(culsh, culsh.ERR_CAPACITY, st.search, np.zeros((1, 13), np.float32), 1, None)
+    st.reset(loaded, 5, culsh.MAX_T + 1)
+    _expect(culsh, culsh.ERR_CAPACITY, st.search, np.zeros((1, 13), np.float32), 1, None)
+
+
+@pytest.mark.skipif(cuda_device_count() > 0, reason="checks the no-GPU behaviour")
+def test_compute_without_gpu_fails_loudly(culsh):
+    c = load_case("odd_d13")
+    ht = culsh.HashTables()
+    ht.load(INDEX_BIN)
+    st = culsh.SearchTables()
+    st.reset(ht, 5, 2)
+    msg = _expect(culsh, culsh.ERR_CUDA, st.search, c["queries"], None, c["X"])
+    assert "device" in msg.lower() or "cuda" in msg.lower()
+    assert st.getKnnIds() is None
+    L, M, D = c["A"].shape
+    ht2 = culsh.HashTables()
+    ht2.reset(c["X"].shape[0], D, L, M, float(c["W"]), A=c["A"], b=c["b"])
+    _expect(culsh, culsh.ERR_CUDA, ht2.index, c["X"])
+
+
+DROPIN_SRC = r"""
+#include <cstdio>
+#include <cstdlib>
+#include <string>
+#include <vector>
+#include "cuLSH.h"
+// Reads: N D L M W Q K T, then A (L*D*M), b (L*M), X (N*D), queries (Q*D) as raw float32
+// from argv[1]; writes ids (Q*K int32), dists (Q*K f32), per-table query buckets,
+// and the index file to argv[2], argv[2].index.
+int main(int argc, char** argv) {
+    if (argc != 3) return 2;
+    FILE* f = fopen(argv[1], "rb");
+    int hdr[8]; float W;
+    if (fread(hdr, 4, 5, f) != 5) return 3;
+    W = *reinterpret_cast<float*>(&hdr[4]);
+    if (fread(&hdr[5], 4, 3, f) != 3) return 3;
+    const int N = hdr[0], D = hdr[1], L = hdr[2], M = hdr[3], Q = hdr[5], K = hdr[6], T = hdr[7];
+    std::vector<std::vector<float>> A(L, std::vector<float>(D * M)), b(L, std::vector<float>(M));
+    std::vector<float*> Ap(L), bp(L);
+    for (int l = 0; l < L; ++l) { if (fread(A[l].data(), 4, D * M, f) != (size_t)(D * M)) return 3; Ap[l] = A[l].data(); }
+    for (int l = 0; l < L; ++l) { if (fread(b[l].data(), 4, M, f) != (size_t)M) return 3; bp[l] = b[l].data(); }
+    std::vector<float> X((size_t)N * D), q((size_t)Q * D);
+    if (fread(X.data(), 4, X.size(), f) != X.size() || fread(q.data(), 4, q.size(), f) != q.size()) return 3;
+    fclose(f);
+    cuLSH::HashTables hashtables;
+    cuLSH::SearchTables searchtables;
+    if (!hashtables.reset(N, D, L, M, W, Ap.data(), bp.data())) return 4;
+    if (!hashtables.index(X.data())) return 5;
+    searchtables.reset(&hashtables, K, T);
+    if (!searchtables.search(q.data(), Q, X.data())) return 6;
+    std::string out = argv[2];
+    FILE* o = fopen(out.c_str(), "wb");
+    fwrite(searchtables.getKnnIds(), 4, (size_t)Q * K, o);
+    fwrite(searchtables.getKnnDistances(), 4, (size_t)Q * K, o);
+    for (int l = 0; l < L; ++l) fwrite(searchtables.getQueryBuckets(l), 4, (size_t)Q * T, o);
+    unsigned tot[2] = {searchtables.getTotalCandidates_unique(), searchtables.getTotalCandidates_nonUnique()};
+    fwrite(tot, 4, 2, o);
+    fclose(o);
+    cuLSH::SearchTables::timesStruct times;
+    searchtables.getTimes(&times);
+    printf("selectivity %f nonunique %f distances %f\n", searchtables.getSelectivity(),
+           searchtables.getNonUniquePercentage(), times.distances);
+    if (!hashtables.save((out + ".index").c_str())) return 7;
+    if (hashtables.getBuckets_totalIndices(0)[0] >= (unsigned)N) return 8;
+    return 0;
+}
+"""
+
+
+def build_dropin(culsh, tmp_path):
+    src = tmp_path / "dropin.cpp"
+    src.write_text(DROPIN_SRC)
+    exe = tmp_path / "dropin"
+    libdir = os.path.dirname(culsh.LIB_PATH)
+    cmd = ["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe),
+           "-L", libdir, "-lculsh", f"-Wl,-rpath,{libdir}"]
+    subprocess.run(cmd, check=True)
+    return exe
+
+
+def test_dropin_header_compiles_and_links(culsh, tmp_path):
+    exe = build_dropin(culsh, tmp_path)
+    assert exe.exists()

@@ -1,0 +1,236 @@
+"""Parity of the CUDA path (through the C ABI) against the CPU oracle.
+
+Bucket codes, bucket contents, query buckets and kNN ids are compared bit for
+bit; kNN (squared) distances must agree within 1e-5 relative (the kernels
+reproduce the reference's lane order, so they are in fact identical, which
+test_distances_bit_exact checks separately). Runs on a GB300 only.
+"""
+
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden_cases, load_case
+
+pytestmark = pytest.mark.gpu
+
+DIST_RTOL = 1e-5
+
+
+def build_index(culsh, c):
+    L, M, D = c["A"].shape
+    ht = culsh.HashTables()
+    ht.reset(c["X"].shape[0], D, L, M, float(c["W"]), A=c["A"], b=c["b"])
+    ht.index(c["X"])
+    return ht
+
+
+def check_index(ht, c):
+    L = c["A"].shape[0]
+    np.testing.assert_array_equal(ht.getBuckets(), c["buckets"])
+    for l in range(L):
+        np.testing.assert_array_equal(ht.getBuckets_totalIndices(l), c[f"ids_{l}"], err_msg=f"table {l}")
+        np.testing.assert_array_equal(ht.getBuckets_startingIndices(l), c[f"starts_{l}"], err_msg=f"table {l}")
+        np.testing.assert_array_equal(ht.getBuckets_sizes(l), c[f"sizes_{l}"], err_msg=f"table {l}")
+        np.testing.assert_array_equal(ht.getBuckets_codes(l), c[f"codes_{l}"], err_msg=f"table {l}")
+
+
+def check_search(st, c):
+    L = c["A"].shape[0]
+    K, T = int(c["K"]), int(c["T"])
+    Q = c["queries"].shape[0]
+    np.testing.assert_array_equal(st.getKnnIds(), c["knn_ids"])
+    np.testing.assert_allclose(st.getKnnDistances(), c["knn_dists"], rtol=DIST_RTOL, atol=0)
+    for l in range(L):
+        np.testing.assert_array_equal(st.getQueryBuckets(l), c["qbuckets"][l].reshape(Q, T))
+    assert st.getTotalCandidates_unique() == int(c["unique"].sum())
+    assert st.getTotalCandidates_nonUnique() == int(c["nonunique"].sum())
+    N = c["X"].shape[0]
+    assert st.getSelectivity() == pytest.approx(c["unique"].sum() / N / Q, rel=1e-6)
+    assert K == st.K
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_index_matches_oracle(culsh, name):
+    c = load_case(name)
+    check_index(build_index(culsh, c), c)
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_search_matches_oracle(culsh, name):
+    c = load_case(name)
+    ht = build_index(culsh, c)
+    st = culsh.SearchTables()
+    st.reset(ht, int(c["K"]), int(c["T"]))
+    st.search(c["queries"], dataset=c["X"])
+    check_search(st, c)
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_distances_bit_exact(culsh, name):
+    c = load_case(name)
+    ht = build_index(culsh, c)
+    st = culsh.SearchTables()
+    st.reset(ht, int(c["K"]), int(c["T"]))
+    st.search(c["queries"], dataset=c["X"])
+    np.testing.assert_array_equal(st.getKnnDistances(), c["knn_dists"])
+
+
+def test_save_matches_oracle_file_bytes(culsh, tmp_path):
+    c = load_case("odd_d13")
+    ht = build_index(culsh, c)
+    out = tmp_path / "gpu.index.bin"
+    ht.save(str(out))
+    assert out.read_bytes() == open(os.path.join(GOLDEN, "odd_d13.index.bin"), "rb").read()
+
+
+@pytest.mark.parametrize("name", ["odd_d13", "heavy", "int_dups"])
+def test_loaded_index_searches_identically(culsh, name, tmp_path):
+    c = load_case(name)
+    ht = build_index(culsh, c)
+    path = tmp_path / "x.bin"
+    ht.save(str(path))
+    ht2 = culsh.HashTables()
+    ht2.reset(str(path))
+    st = culsh.SearchTables()
+    st.reset(ht2, int(c["K"]), int(c["T"]))
+    st.search(c["queries"], dataset=c["X"])
+    check_search(st, c)
+
+
+def test_repeated_search_and_reset(culsh):
+    c = load_case("mix_d16_t8")
+    ht = build_index(culsh, c)
+    st = culsh.SearchTables()
+    for _ in range(2):
+        st.reset(ht, int(c["K"]), int(c["T"]))
+        st.search(c["queries"], dataset=c["X"])
+        check_search(st, c)
+    # a second index() on the same object rebuilds identically
+    ht.index(c["X"])
+    check_index(ht, c)
+    # fewer queries after more: buffers are reused
+    st.reset(ht, int(c["K"]), int(c["T"]))
+    st.search(c["queries"][:3], dataset=c["X"])
+    np.testing.assert_array_equal(st.getKnnIds(), c["knn_ids"][:3])
+
+
+def test_device_api_matches_host_api(culsh):
+    torch = pytest.importorskip("torch")
+    c = load_case("int_dups")
+    L, M, D = c["A"].shape
+    X = torch.from_numpy(c["X"]).cuda()
+    q = torch.from_numpy(c["queries"]).cuda()
+    K, T = int(c["K"]), int(c["T"])
+    ht = culsh.HashTables()
+    ht.reset(c["X"].shape[0], D, L, M, float(c["W"]), A=c["A"], b=c["b"])
+    stream = torch.cuda.current_stream().cuda_stream
+    ht.index_device(X.data_ptr(), stream)
+    check_index(ht, c)
+    ids = torch.empty((q.shape[0], K), dtype=torch.int32, device="cuda")
+    d = torch.empty((q.shape[0], K), dtype=torch.float32, device="cuda")
+    st = culsh.SearchTables()
+    st.reset(ht, K, T)
+    st.search_device(q.data_ptr(), q.shape[0], ids.data_ptr(), d.data_ptr(), stream)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(ids.cpu().numpy(), c["knn_ids"])
+    np.testing.assert_array_equal(d.cpu().numpy(), c["knn_dists"])
+
+
+def test_overflow_arena_and_deferred_admission(culsh, monkeypatch):
+    """Candidate sets larger than shared memory use the global arena; with a
+    tiny arena the queries are deferred and admitted in chunks; with an arena
+    smaller than one query's set the search fails like the reference's
+    admission check (cuLSH_SearchTables.cu:303-306)."""
+    c = load_case("heavy")
+    assert int(c["nonunique"].max()) > 2048
+    ht = build_index(culsh, c)
+    st = culsh.SearchTables()
+    st.reset(ht, int(c["K"]), int(c["T"]))
+    st.search(c["queries"], dataset=c["X"])
+    check_search(st, c)
+    words_one = 1
+    while words_one < 2 * int(c["nonunique"].max()):
+        words_one *= 2
+    words_one += int(c["nonunique"].max())
+    monkeypatch.setenv("CULSH_ARENA_WORDS", str(words_one + 100))   # one large query at a time
+    st.search(c["queries"], dataset=c["X"])
+    check_search(st, c)
+    monkeypatch.setenv("CULSH_ARENA_WORDS", "1000")
+    with pytest.raises(culsh.CulshError) as ei:
+        st.search(c["queries"], dataset=c["X"])
+    assert ei.value.code == culsh.ERR_OUT_OF_MEMORY and "Cannot load all candidates" in str(ei.value)
+    monkeypatch.delenv("CULSH_ARENA_WORDS")
+    st.search(c["queries"], dataset=c["X"])
+    check_search(st, c)
+
+
+def test_nonfinite_data_is_rejected(culsh):
+    c = load_case("odd_d13")
+    X = c["X"].copy()
+    X[17, 3] = np.nan
+    L, M, D = c["A"].shape
+    ht = culsh.HashTables()
+    ht.reset(X.shape[0], D, L, M, float(c["W"]), A=c["A"], b=c["b"])
+    with pytest.raises(culsh.CulshError) as ei:
+        ht.index(X)
+    assert ei.value.code == culsh.ERR_NUMERIC
+
+
+def test_random_projection_reset(culsh):
+    ht = culsh.HashTables()
+    ht.reset(5000, 32, 3, 7, 2.5, seed=1234)
+    A = np.stack([ht.getA(l) for l in range(3)])
+    b = np.stack([ht.getb(l) for l in range(3)])
+    assert A.shape == (3, 7, 32) and b.shape == (3, 7)
+    assert abs(A.mean()) < 0.15 and 0.85 < A.std() < 1.15
+    assert np.all(b >= 0) and np.all(b.min(axis=1) == 0) and np.all(b < 2.5)
+    ht2 = culsh.HashTables()
+    ht2.reset(5000, 32, 3, 7, 2.5, seed=1234)
+    np.testing.assert_array_equal(ht2.getA(2), A[2])
+    X = np.random.default_rng(0).normal(0, 3, (5000, 32)).astype(np.float32)
+    ht.index(X)
+    st = culsh.SearchTables()
+    st.reset(ht, 5, 3)
+    st.search(X[:50], dataset=X)
+    ids = st.getKnnIds()
+    assert np.all(ids[:, 0] == np.arange(50))     # every query point finds itself first
+
+
+def test_dropin_cpp_program(culsh, tmp_path):
+    """The drop-in C++ header, used exactly like the reference's cuLSH.h."""
+    from test_capi_cpu import build_dropin
+    c = load_case("int_dups")
+    exe = build_dropin(culsh, tmp_path)
+    L, M, D = c["A"].shape
+    N, Q = c["X"].shape[0], c["queries"].shape[0]
+    K, T = int(c["K"]), int(c["T"])
+    inp = tmp_path / "in.bin"
+    with open(inp, "wb") as f:
+        f.write(np.array([N, D, L, M], np.int32).tobytes())
+        f.write(np.float32(c["W"]).tobytes())
+        f.write(np.array([Q, K, T], np.int32).tobytes())
+        for l in range(L):
+            f.write(c["A"][l].tobytes())
+        for l in range(L):
+            f.write(c["b"][l].tobytes())
+        f.write(c["X"].tobytes())
+        f.write(c["queries"].tobytes())
+    out = tmp_path / "out.bin"
+    r = subprocess.run([str(exe), str(inp), str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    raw = np.fromfile(out, np.uint8)
+    ids = raw[: Q * K * 4].view(np.int32).reshape(Q, K)
+    d = raw[Q * K * 4: Q * K * 8].view(np.float32).reshape(Q, K)
+    np.testing.assert_array_equal(ids, c["knn_ids"])
+    np.testing.assert_array_equal(d, c["knn_dists"])
+    qb = raw[Q * K * 8: Q * K * 8 + L * Q * T * 4].view(np.int32).reshape(L, Q * T)
+    np.testing.assert_array_equal(qb, c["qbuckets"])
+    tot = raw[-8:].view(np.uint32)
+    assert tot.tolist() == [int(c["unique"].sum()), int(c["nonunique"].sum())]
+    oracle_file = tmp_path / "oracle.bin"
+    import oracle
+    oracle.build_index(c["X"], c["A"], c["b"], float(c["W"])).save(str(oracle_file))
+    assert open(str(out) + ".index", "rb").read() == oracle_file.read_bytes()
