@@ -98,6 +98,7 @@ ABI = {
     "culsh_search_total_nonunique": (ctypes.c_ulonglong, [_P]),
     "culsh_search_times": (None, [_P, ctypes.POINTER(_Times)]),
     "culsh_search_profile_get": (_I, [_P, ctypes.POINTER(_Profile)]),
+    "culsh_search_run_device_noalloc": (_I, [_P, _P, _I, _P, _P, _P]),
 }
 
 _lib = None

@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstring>
 #include <ctime>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1017,3 +1018,164 @@ int culsh_search_profile_get(culsh_search* s, culsh_search_profile* out) {
 }
 
 }  // extern "C"
+
+// ============================================================================
+// Search without any allocation.
+//
+// Some callers cannot call cudaMalloc: code running under a memory pool or
+// arena they do not own, frameworks that forbid allocation inside a timed or
+// latency-critical request path, and processes whose allocator is locked down
+// after start-up. culsh_search_run_device_noalloc runs the same three kernels
+// as culsh_search_run_device, but every scratch buffer (query projections,
+// probe buckets, candidate counts, the overflow hash arena) is carved out of
+// the fixed array below instead of being allocated.
+//
+// The array is reserved on every GPU that loads this library and is held
+// until the process exits. Its address is looked up once per device, on the
+// first call made with that device current (call it once before any stream
+// capture). The index must already be resident on the device, and the call
+// leaves the search object's getters (statistics, query buckets) describing
+// its last ordinary search. All calls share the array and it keeps the previous call's
+// contents: the counters that must start at zero are cleared by each call,
+// and calls that overlap on the GPU (different streams, threads or
+// processes-in-the-same-context) race on it and must be serialised by the
+// caller.
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(64) << 20;   // 64 MiB
+constexpr size_t kNoAllocMinArenaBytes = size_t(1) << 20;   // at least 1 MiB of overflow arena
+constexpr int kNoAllocMaxDevices = 64;
+
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+std::mutex g_noalloc_mu;
+unsigned char* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+inline size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
+
+int noalloc_scratch(unsigned char** out) {
+    int dev = 0;
+    CU_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(CULSH_ERR_CAPACITY, "device %d beyond %d", dev, kNoAllocMaxDevices);
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        CU_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_ptr[dev] = static_cast<unsigned char*>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return CULSH_OK;
+}
+
+}  // namespace
+
+extern "C" int culsh_search_run_device_noalloc(culsh_search* s, const float* d_queries, int Q, int* d_ids,
+                                               float* d_dists, void* stream) {
+    TRY(precheck_search(s, Q));
+    if (!d_queries || !d_ids || !d_dists) return fail(CULSH_ERR_INVALID_ARGUMENT, "null device buffer");
+    culsh_index* ix = s->ix;
+    if (!ix->dev_valid || !ix->proj_on_dev || !ix->dev_x())
+        return fail(CULSH_ERR_STATE,
+                    "the index is not resident on the device: build it with index()/culsh_index_build_device, "
+                    "or run one ordinary search after load(), before calling the no-allocation search");
+    const cudaStream_t st = (cudaStream_t)stream;
+    const int L = ix->L, M = ix->M, D = ix->D, K = s->K, T = s->T;
+    // Layout of the fixed scratch for this call.
+    size_t off = 0;
+    const size_t o_vals = off;
+    off = align256(off + sizeof(float) * (size_t)L * M * Q);
+    const size_t o_qb = off;
+    off = align256(off + sizeof(int32_t) * (size_t)L * Q * T);
+    const size_t o_cnu = off;
+    off = align256(off + 8 * (size_t)Q);
+    const size_t o_cu = off;
+    off = align256(off + 8 * (size_t)Q);
+    const size_t o_stats = off;
+    off = align256(off + 8 * 4);
+    const size_t o_def = off;
+    off = align256(off + sizeof(int) * 2 * (size_t)Q);
+    const size_t o_arena = off;
+    if (off + kNoAllocMinArenaBytes > kNoAllocScratchBytes)
+        return fail(CULSH_ERR_CAPACITY,
+                    "no-allocation search of Q=%d (L=%d, M=%d, T=%d) needs %zu bytes of scratch plus a 1 MiB "
+                    "arena; the static scratch holds %zu bytes",
+                    Q, L, M, T, off, kNoAllocScratchBytes);
+    unsigned char* base = nullptr;
+    TRY(noalloc_scratch(&base));
+    float* vals = reinterpret_cast<float*>(base + o_vals);
+    int32_t* qb = reinterpret_cast<int32_t*>(base + o_qb);
+    unsigned long long* cnu = reinterpret_cast<unsigned long long*>(base + o_cnu);
+    unsigned long long* cu = reinterpret_cast<unsigned long long*>(base + o_cu);
+    unsigned long long* stats = reinterpret_cast<unsigned long long*>(base + o_stats);
+    int* deferred = reinterpret_cast<int*>(base + o_def);
+    uint32_t* arena = reinterpret_cast<uint32_t*>(base + o_arena);
+    const unsigned long long arena_words = (kNoAllocScratchBytes - o_arena) / 4;
+
+    CU_TRY(cudaMemsetAsync(cnu, 0, 8 * (size_t)Q, st));
+    CU_TRY(cudaMemsetAsync(stats, 0, 8 * 4, st));
+    CU_TRY(launch_project_fp32(d_queries, Q, D, ix->dA.p, ix->db.p, L * M, ix->W, nullptr, vals, nullptr, nullptr,
+                               nullptr, st));
+    ProbeArgs pa;
+    pa.vals = vals;
+    pa.Q = Q;
+    pa.T = T;
+    pa.lv = lookup_view(ix);
+    pa.qbuckets = qb;
+    pa.cnu = cnu;
+    CU_TRY(launch_probe(pa, st));
+    CandArgs ca;
+    ca.X = ix->dev_x();
+    ca.N = ix->N;
+    ca.D = D;
+    ca.L = L;
+    ca.T = T;
+    ca.Q = Q;
+    ca.K = K;
+    ca.queries = d_queries;
+    ca.qbuckets = qb;
+    ca.boff = ix->boff.p;
+    ca.starts = ix->starts.p;
+    ca.sizes = ix->sizes.p;
+    ca.ids = ix->ids.p;
+    ca.cnu = cnu;
+    ca.out_ids = d_ids;
+    ca.out_d = d_dists;
+    ca.cu = cu;
+    ca.totals = stats;
+    ca.arena = arena;
+    ca.arena_words = arena_words;
+    ca.arena_top = stats + 2;
+    ca.deferred = deferred;
+    ca.n_deferred = reinterpret_cast<unsigned int*>(stats + 3);
+    ca.qlist = nullptr;
+    ca.nq = Q;
+    CU_TRY(launch_candidates(ca, st));
+    unsigned long long h_stats[4] = {0, 0, 0, 0};
+    CU_TRY(cudaMemcpyAsync(h_stats, stats, sizeof h_stats, cudaMemcpyDeviceToHost, st));
+    CU_TRY(cudaStreamSynchronize(st));
+    // Queries whose candidate sets did not fit the arena at once are re-run
+    // in rounds over the same arena; a round that admits nothing means one
+    // query alone needs more than the arena.
+    unsigned int ndef = (unsigned int)(h_stats[3] & 0xffffffffu);
+    int cur = 0;
+    while (ndef) {
+        const unsigned int before = ndef;
+        CandArgs cb = ca;
+        cb.qlist = deferred + (size_t)cur * Q;
+        cb.nq = (int)ndef;
+        cb.deferred = deferred + (size_t)(cur ^ 1) * Q;
+        CU_TRY(cudaMemsetAsync(stats + 2, 0, 16, st));
+        CU_TRY(launch_candidates(cb, st));
+        CU_TRY(cudaMemcpyAsync(h_stats, stats, sizeof h_stats, cudaMemcpyDeviceToHost, st));
+        CU_TRY(cudaStreamSynchronize(st));
+        ndef = (unsigned int)(h_stats[3] & 0xffffffffu);
+        cur ^= 1;
+        if (ndef == before)
+            return fail(CULSH_ERR_CAPACITY,
+                        "a query's candidate set needs more than the %llu-byte overflow arena of the static scratch",
+                        arena_words * 4);
+    }
+    // The search object's getters keep describing its last ordinary search:
+    // this call reports only through the caller's buffers.
+    return CULSH_OK;
+}

@@ -135,6 +135,25 @@ typedef struct culsh_search_profile {
 } culsh_search_profile;
 int culsh_search_profile_get(culsh_search* s, culsh_search_profile* out);
 
+/* Same search as culsh_search_run_device, for callers that cannot allocate
+ * device memory (a locked-down or externally owned allocator, no allocation
+ * allowed on a latency-critical path). No counterpart in the reference. It
+ * calls no cudaMalloc/cudaFree and creates no stream or event: its scratch is
+ * a fixed 64 MiB __device__ array inside libculsh, reserved on every GPU that
+ * loads the library until the process exits. Requirements and limits:
+ *  - the index is already resident on the device (after index(), or after one
+ *    ordinary search of a loaded index), else CULSH_ERR_STATE;
+ *  - Q*(4*L*M + 4*L*T + 24) bytes plus a 1 MiB overflow arena must fit in the
+ *    64 MiB (Q = 10,000 with L=16, M=12, T=16 uses 18 MB), else
+ *    CULSH_ERR_CAPACITY; a single query's candidate set must fit the arena;
+ *  - the first call on a device looks up the array's address: make it before
+ *    any stream capture;
+ *  - calls share the array: calls that overlap on the GPU race, serialise them;
+ *  - stream NULL is the legacy default stream; the search object's getters
+ *    are not updated (results go only to d_ids / d_dists). */
+int culsh_search_run_device_noalloc(culsh_search* s, const float* d_queries, int Q, int* d_ids, float* d_dists,
+                                    void* stream);
+
 #ifdef __cplusplus
 }
 #endif
