@@ -141,6 +141,7 @@ struct culsh_index {
     DevBuf<int32_t> cmin, cmax;
     DevBuf<uint8_t> fbits;
     DevBuf<uint16_t> foff;
+    DevBuf<unsigned long long> funit;   // [L*M][2]: 2^foff as two 64-bit words
     DevBuf<uint32_t> ids, starts, sizes, ukeys;
     std::vector<uint64_t> h_boff, h_hoff;
     std::vector<uint32_t> h_hmask;
@@ -279,6 +280,15 @@ int upload_layout(culsh_index* ix, cudaStream_t st) {
     CU_TRY(cudaMemcpyAsync(ix->foff.p, ix->h_foff.data(), LM * 2, cudaMemcpyHostToDevice, st));
     CU_TRY(cudaMemcpyAsync(ix->cmin.p, ix->h_cmin.data(), LM * 4, cudaMemcpyHostToDevice, st));
     CU_TRY(cudaMemcpyAsync(ix->cmax.p, ix->h_cmax.data(), LM * 4, cudaMemcpyHostToDevice, st));
+    std::vector<unsigned long long> unit(2 * LM, 0ull);
+    for (size_t c = 0; c < LM; ++c) {
+        const int off = ix->h_foff[c];
+        if (off < 64) unit[2 * c] = 1ull << off;
+        else if (off < 128) unit[2 * c + 1] = 1ull << (off - 64);
+    }
+    CU_TRY(ix->funit.reserve(2 * LM));
+    CU_TRY(cudaMemcpyAsync(ix->funit.p, unit.data(), 16 * LM, cudaMemcpyHostToDevice, st));
+    CU_TRY(cudaStreamSynchronize(st));   // `unit` is a pageable temporary
     return CULSH_OK;
 }
 
@@ -477,6 +487,14 @@ int ensure_device(culsh_index* ix, cudaStream_t st) {
     return CULSH_OK;
 }
 
+// Whether every code range of the index sits below 2^24 in magnitude (the
+// fast probe kernel's integer +-1 then equals the reference's float +-1).
+int small_codes(const culsh_index* ix) {
+    for (size_t i = 0; i < ix->h_cmin.size(); ++i)
+        if (ix->h_cmin[i] <= -(1 << 24) + 2 || ix->h_cmax[i] >= (1 << 24) - 2) return 0;
+    return 1;
+}
+
 LookupView lookup_view(const culsh_index* ix) {
     LookupView lv;
     lv.L = ix->L;
@@ -493,6 +511,7 @@ LookupView lookup_view(const culsh_index* ix) {
     lv.hslots = ix->hslots.p;
     lv.hoff = ix->hoff.p;
     lv.hmask = ix->hmask.p;
+    lv.funit = ix->funit.p;
     return lv;
 }
 
@@ -545,6 +564,7 @@ int search_device(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float
     pa.lv = lookup_view(ix);
     pa.qbuckets = s->qb.p;
     pa.cnu = s->cnu.p;
+    pa.small_codes = small_codes(ix);
     CU_TRY(launch_probe(pa, st));
     CU_TRY(cudaEventRecord(s->ev[2], st));
     s->launches += 2;
@@ -1122,6 +1142,7 @@ extern "C" int culsh_search_run_device_noalloc(culsh_search* s, const float* d_q
     pa.lv = lookup_view(ix);
     pa.qbuckets = qb;
     pa.cnu = cnu;
+    pa.small_codes = small_codes(ix);
     CU_TRY(launch_probe(pa, st));
     CandArgs ca;
     ca.X = ix->dev_x();

@@ -34,24 +34,27 @@ enum DevErr : int {
     kErrNotIntegral = 16,  // a loaded bucket code is not an integer
 };
 
-// Public 32-bit mixer ("lowbias32", C. Wellons, public domain).
-__host__ __device__ __forceinline__ uint32_t mix32(uint32_t h) {
-    h ^= h >> 16;
-    h *= 0x7feb352du;
-    h ^= h >> 15;
-    h *= 0x846ca68bu;
-    h ^= h >> 16;
+// splitmix64 finalizer (Steele, Lea, Flood, OOPSLA 2014; public domain).
+__host__ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+__host__ __device__ __forceinline__ uint32_t mix32(uint32_t h) { return (uint32_t)mix64(h); }
+
+constexpr uint64_t kHashSeed = 0x2545f4914f6cdd1dull;
+
+// 64-bit hash of a packed key of KW 32-bit words, folded as 64-bit chunks:
+// the low 32 bits pick the hash slot, the high 32 bits are the fingerprint.
+__host__ __device__ __forceinline__ uint64_t key_hash64(const uint32_t* k, int KW) {
+    uint64_t h = kHashSeed;
+    for (int w = 0; w < KW; w += 2) {
+        const uint64_t c = (uint64_t)k[w] | (w + 1 < KW ? (uint64_t)k[w + 1] << 32 : 0ull);
+        h = mix64(h ^ c);
+    }
     return h;
 }
-
-__host__ __device__ __forceinline__ uint32_t key_hash(const uint32_t* k, int KW, uint32_t seed) {
-    uint32_t h = seed;
-    for (int w = 0; w < KW; ++w) h = mix32(h ^ k[w]) + 0x9e3779b9u * (uint32_t)(w + 1);
-    return mix32(h);
-}
-
-constexpr uint32_t kSeedSlot = 0x2545f491u;
-constexpr uint32_t kSeedFp = 0x68e31da4u;
 
 // Place a field of `bits` bits (<= 32) at bit offset `off` of a little-endian
 // multi-word key.
@@ -83,6 +86,7 @@ struct LookupView {
     const unsigned long long* hslots;
     const uint64_t* hoff;
     const uint32_t* hmask;
+    const unsigned long long* funit;   // [L*M][2]: 2^foff as (low, high) 64-bit words
 };
 
 // ---------------------------------------------------------------------------
@@ -151,6 +155,7 @@ struct ProbeArgs {
     LookupView lv;
     int32_t* qbuckets;         // [L][Q*T]
     unsigned long long* cnu;   // [Q] non-unique candidate counts (accumulated)
+    int small_codes;           // every |cmin|, |cmax| < 2^24 - 2 (set by the host)
 };
 cudaError_t launch_probe(const ProbeArgs& a, cudaStream_t st);
 

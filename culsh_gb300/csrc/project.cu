@@ -19,39 +19,47 @@
 namespace culsh {
 namespace {
 
-constexpr int BN = 128;   // points per block tile
-constexpr int BC = 64;    // projection columns per block tile
-constexpr int BK = 16;    // dimensions per shared-memory stage
-constexpr int NT = 256;   // threads: 16 (points) x 16 (columns), each 8 x 4 outputs
+constexpr int NT = 256;   // threads: 16 (points) x 16 (columns), each PT x CT outputs
 
-template <bool kCodes>
+// Block tile BN = 16*PT points x BC = 16*CT columns, BK dimensions per
+// shared-memory stage. Index builds use PT = 8, CT = 4, BK = 16; query batches
+// use PT = 4, CT = 8, BK = 64 (fewer barriers and shared-memory loads per FMA,
+// enough blocks for ten thousand queries).
+template <bool kCodes, int PT, int CT, int BK>
 __global__ void __launch_bounds__(NT) k_project(const float* __restrict__ X, int64_t n_pts, int D,
                                                 const float* __restrict__ A, const float* __restrict__ b, int LM,
                                                 float W, int32_t* __restrict__ codes, float* __restrict__ vals,
                                                 int32_t* __restrict__ pmin, int32_t* __restrict__ pmax,
                                                 int* __restrict__ err) {
-    __shared__ __align__(16) float Xs[BK][BN];
-    __shared__ __align__(16) float As[BK][BC];
-    __shared__ uint32_t Cs[BC][BN + 1];
+    constexpr int BN = 16 * PT;
+    constexpr int BC = 16 * CT;
+    constexpr int kTileBytes = BK * (BN + BC) * 4;
+    constexpr int kStageBytes = BC * (BN + 1) * 4;
+    constexpr bool kUnion = kTileBytes >= kStageBytes;   // epilogue staging reuses the tiles
+    __shared__ __align__(16) unsigned char smem[kUnion ? kTileBytes : kTileBytes + kStageBytes];
+    float (*Xs)[BN] = reinterpret_cast<float (*)[BN]>(smem);
+    float (*As)[BC] = reinterpret_cast<float (*)[BC]>(smem + BK * BN * 4);
+    uint32_t (*Cs)[BN + 1] = reinterpret_cast<uint32_t (*)[BN + 1]>(smem + (kUnion ? 0 : kTileBytes));
 
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     const int64_t n0 = (int64_t)blockIdx.x * BN;
     const int c0 = blockIdx.y * BC;
     const bool vec = (D & 3) == 0;
 
-    float acc[8][4];
+    float acc[PT][CT];
 #pragma unroll
-    for (int i = 0; i < 8; ++i)
+    for (int i = 0; i < PT; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0f;
+        for (int j = 0; j < CT; ++j) acc[i][j] = 0.0f;
 
     for (int d0 = 0; d0 < D; d0 += BK) {
-        // X tile: 128 points x 16 dims, transposed into Xs[dim][point]. Zero
+        // X tile: BN points x BK dims, transposed into Xs[dim][point]. Zero
         // fill past D adds +-0 to a chain, which leaves it unchanged.
         if (vec) {
 #pragma unroll
-            for (int r = 0; r < 2; ++r) {
-                const int f = tid + NT * r, p = f & (BN - 1), dq = f >> 7;
+            for (int r = 0; r < (BN * BK / 4 + NT - 1) / NT; ++r) {
+                const int f = tid + NT * r, p = f % BN, dq = f / BN;
+                if (f >= BN * BK / 4) break;
                 const int64_t gn = n0 + p;
                 const int gd = d0 + dq * 4;
                 float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -63,31 +71,42 @@ __global__ void __launch_bounds__(NT) k_project(const float* __restrict__ X, int
             }
         } else {
 #pragma unroll
-            for (int r = 0; r < 8; ++r) {
-                const int f = tid + NT * r, p = f & (BN - 1), dd = f >> 7;
+            for (int r = 0; r < BN * BK / NT; ++r) {
+                const int f = tid + NT * r, p = f % BN, dd = f / BN;
                 const int64_t gn = n0 + p;
                 const int gd = d0 + dd;
                 Xs[dd][p] = (gn < n_pts && gd < D) ? __ldg(X + gn * D + gd) : 0.0f;
             }
         }
 #pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            const int f = tid + NT * r, c = f & (BC - 1), dd = f >> 6;
+        for (int r = 0; r < BC * BK / NT; ++r) {
+            const int f = tid + NT * r, c = f % BC, dd = f / BC;
             const int gc = c0 + c, gd = d0 + dd;
             As[dd][c] = (gc < LM && gd < D) ? __ldg(A + (int64_t)gc * D + gd) : 0.0f;
         }
         __syncthreads();
-#pragma unroll
+#pragma unroll 8
         for (int k = 0; k < BK; ++k) {
-            const float4 xa = *reinterpret_cast<const float4*>(&Xs[k][tx * 8]);
-            const float4 xb = *reinterpret_cast<const float4*>(&Xs[k][tx * 8 + 4]);
-            const float4 av = *reinterpret_cast<const float4*>(&As[k][ty * 4]);
-            const float xv[8] = {xa.x, xa.y, xa.z, xa.w, xb.x, xb.y, xb.z, xb.w};
-            const float aw[4] = {av.x, av.y, av.z, av.w};
+            float xv[PT];
 #pragma unroll
-            for (int i = 0; i < 8; ++i)
+            for (int i = 0; i < PT; i += 2) {
+                const float2 x2 = *reinterpret_cast<const float2*>(&Xs[k][tx * PT + i]);
+                xv[i] = x2.x;
+                xv[i + 1] = x2.y;
+            }
+            float aw[CT];
 #pragma unroll
-                for (int j = 0; j < 4; ++j) acc[i][j] = __fmaf_rn(xv[i], aw[j], acc[i][j]);
+            for (int j = 0; j < CT; j += 4) {
+                const float4 av = *reinterpret_cast<const float4*>(&As[k][ty * CT + j]);
+                aw[j] = av.x;
+                aw[j + 1] = av.y;
+                aw[j + 2] = av.z;
+                aw[j + 3] = av.w;
+            }
+#pragma unroll
+            for (int i = 0; i < PT; ++i)
+#pragma unroll
+                for (int j = 0; j < CT; ++j) acc[i][j] = __fmaf_rn(xv[i], aw[j], acc[i][j]);
         }
         __syncthreads();
     }
@@ -96,12 +115,12 @@ __global__ void __launch_bounds__(NT) k_project(const float* __restrict__ X, int
     // coalesced column-major stores.
     int bad = 0;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const int c = c0 + ty * 4 + j;
+    for (int j = 0; j < CT; ++j) {
+        const int c = c0 + ty * CT + j;
         const float bc = (c < LM) ? __ldg(b + c) : 0.0f;
         int32_t lo = INT_MAX, hi = INT_MIN;
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
+        for (int i = 0; i < PT; ++i) {
             const float v = __fdiv_rn(__fsub_rn(acc[i][j], bc), W);
             uint32_t bits;
             if (kCodes) {
@@ -114,7 +133,7 @@ __global__ void __launch_bounds__(NT) k_project(const float* __restrict__ X, int
                 } else {
                     code = (int32_t)f;
                 }
-                if (n0 + tx * 8 + i < n_pts && c < LM) {
+                if (n0 + tx * PT + i < n_pts && c < LM) {
                     lo = min(lo, code);
                     hi = max(hi, code);
                 }
@@ -122,7 +141,7 @@ __global__ void __launch_bounds__(NT) k_project(const float* __restrict__ X, int
             } else {
                 bits = __float_as_uint(v);
             }
-            Cs[ty * 4 + j][tx * 8 + i] = bits;
+            Cs[ty * CT + j][tx * PT + i] = bits;
         }
         if (kCodes) {
 #pragma unroll
@@ -138,10 +157,11 @@ __global__ void __launch_bounds__(NT) k_project(const float* __restrict__ X, int
     }
     if (kCodes && bad) atomicOr(err, bad);
     __syncthreads();
-    const int p = tid & (BN - 1);
+    constexpr int RPI = NT / BN;   // rows stored per iteration
+    const int p = tid % BN;
 #pragma unroll 4
-    for (int r = 0; r < BC / 2; ++r) {
-        const int row = r * 2 + (tid >> 7);
+    for (int r = 0; r < BC / RPI; ++r) {
+        const int row = r * RPI + tid / BN;
         const int c = c0 + row;
         if (c < LM && n0 + p < n_pts) {
             const int64_t o = (int64_t)c * n_pts + n0 + p;
@@ -187,17 +207,21 @@ __global__ void k_minmax_reduce(const int32_t* __restrict__ pmin, const int32_t*
 
 }  // namespace
 
-int project_grid_x(int64_t n_pts) { return (int)((n_pts + BN - 1) / BN); }
+// Index builds (codes) use 128-point tiles; query batches (values) use
+// 64-point tiles so that ten thousand queries still fill every SM.
+int project_grid_x(int64_t n_pts) { return (int)((n_pts + 127) / 128); }
 
 cudaError_t launch_project_fp32(const float* X, int64_t n_pts, int D, const float* A, const float* b, int LM,
                                 float W, int32_t* codes, float* vals, int32_t* pmin, int32_t* pmax, int* err,
                                 cudaStream_t st) {
     if (n_pts <= 0) return cudaSuccess;
-    const dim3 grid(project_grid_x(n_pts), (LM + BC - 1) / BC);
-    if (codes)
-        k_project<true><<<grid, NT, 0, st>>>(X, n_pts, D, A, b, LM, W, codes, nullptr, pmin, pmax, err);
-    else
-        k_project<false><<<grid, NT, 0, st>>>(X, n_pts, D, A, b, LM, W, nullptr, vals, nullptr, nullptr, err);
+    if (codes) {
+        k_project<true, 8, 4, 16><<<dim3(project_grid_x(n_pts), (LM + 63) / 64), NT, 0, st>>>(
+            X, n_pts, D, A, b, LM, W, codes, nullptr, pmin, pmax, err);
+    } else {
+        k_project<false, 4, 8, 64><<<dim3((unsigned)((n_pts + 63) / 64), (LM + 127) / 128), NT, 0, st>>>(
+            X, n_pts, D, A, b, LM, W, nullptr, vals, nullptr, nullptr, err);
+    }
     return cudaGetLastError();
 }
 

@@ -17,6 +17,7 @@
 // large sets), squared L2 distances are computed in the reference's lane order
 // from 16-byte loads, and each warp keeps a sorted top-K that the block merges.
 #include <cfloat>
+#include <cstdlib>
 
 #include "culsh_internal.cuh"
 
@@ -76,8 +77,9 @@ __device__ int32_t lookup_row(const LookupView& lv, int l, const float* row) {
         if (bits) key_put(key, __ldg(lv.foff + c), bits, (uint32_t)(ci - lo));
     }
     const uint32_t mask = __ldg(lv.hmask + l);
-    const uint32_t h = key_hash(key, KW, kSeedSlot);
-    const uint32_t fp = key_hash(key, KW, kSeedFp);
+    const uint64_t hh = key_hash64(key, KW);
+    const uint32_t h = (uint32_t)hh;
+    const uint32_t fp = (uint32_t)(hh >> 32);
     const unsigned long long* slots = lv.hslots + __ldg(lv.hoff + l);
     const uint64_t bo = __ldg(lv.boff + l);
     for (uint32_t p = 0; p <= mask; ++p) {
@@ -180,6 +182,311 @@ __global__ void __launch_bounds__(128) k_probe(ProbeArgs a) {
         }
     }
     if (cnu) atomicAdd(a.cnu + q, cnu);
+}
+
+
+// ---------------------------------------------------------------------------
+// Fast multiprobe path for the common shapes: M <= 32 columns, T <= 32
+// probes, packed keys of at most 128 bits and codes below 2^24 in magnitude
+// (so that the reference's float +-1 on a code equals integer +-1).
+//
+// The reference orders the 2M deltas with a heap sort (cuLSH_Kernels.cu:202-214).
+// When the deltas are pairwise distinct every correct sort yields that same
+// order, so the kernel ranks the M "down" deltas and takes the "up" deltas
+// (1 - down, a non-increasing function of down) in reverse, then merges the
+// two lists; any tie or NaN sends the thread through the reference's heap
+// procedure instead. The shift/expand enumeration then runs exactly as in
+// k_probe. A probe's key is the home key plus or minus one unit of each
+// perturbed column's field (packing is linear) in 128-bit modular arithmetic,
+// and column range validity is three bit masks. Slot loads are issued eight
+// at a time before any is consumed. Per-thread state lives in a strided
+// slice of shared memory. Results equal k_probe's exactly.
+constexpr int PF = 128;
+typedef unsigned __int128 u128;
+
+__device__ __forceinline__ u128 field_term(int64_t f, int off) { return ((u128)(__int128)f) << off; }
+
+struct FastProbeCtx {
+    u128 hkey;
+    uint64_t ok0, okUp, okDn, allM;
+    const uint8_t* enc;                 // sorted delta i -> column | (up << 7); strided slice
+    const unsigned long long* funit;    // this table's field units 2^foff (low, high)
+};
+
+__device__ __forceinline__ u128 unit_of(const unsigned long long* funit, int m) {
+    return ((u128)__ldg(funit + 2 * m + 1) << 64) | (u128)__ldg(funit + 2 * m);
+}
+
+// Key of a probe mask; returns false when a column leaves [cmin, cmax].
+__device__ __forceinline__ bool probe_key(const FastProbeCtx& c, uint64_t mask, u128& key) {
+    uint64_t up = 0, dn = 0;
+    for (uint64_t b = mask; b; b &= b - 1) {
+        const int e = c.enc[(__ffsll((long long)b) - 1) * PF];
+        if (e & 0x80) up |= 1ull << (e & 0x3f);
+        else dn |= 1ull << (e & 0x3f);
+    }
+    const uint64_t nu = up & ~dn, nd = dn & ~up;
+    if ((~(nu | nd) & c.allM & ~c.ok0) | (nu & ~c.okUp) | (nd & ~c.okDn)) return false;
+    u128 k = c.hkey;
+    for (uint64_t b = nu; b; b &= b - 1) k += unit_of(c.funit, __ffsll((long long)b) - 1);
+    for (uint64_t b = nd; b; b &= b - 1) k -= unit_of(c.funit, __ffsll((long long)b) - 1);
+    key = k;
+    return true;
+}
+
+__device__ __forceinline__ uint64_t key_hash128(u128 k, int KW) {
+    uint64_t h = mix64(kHashSeed ^ (uint64_t)k);
+    if (KW > 2) h = mix64(h ^ (uint64_t)(k >> 64));
+    return h;
+}
+
+__device__ __forceinline__ bool key_matches(const uint32_t* uk, u128 k, int KW) {
+    bool eq = __ldg(uk) == (uint32_t)k;
+    if (KW > 1) eq &= __ldg(uk + 1) == (uint32_t)(k >> 32);
+    if (KW > 2) eq &= __ldg(uk + 2) == (uint32_t)(k >> 64);
+    if (KW > 3) eq &= __ldg(uk + 3) == (uint32_t)(k >> 96);
+    return eq;
+}
+
+// The reference's heap selection + heap sort over a strided slice (used
+// only when deltas tie or are NaN). perm[] receives delta indices.
+__device__ void heap_order_strided(const float* dl, int8_t* perm, int M2, int maxT) {
+    const int levels = ceil_log2_dev(M2 + 1);
+    auto sift = [&](int total) {
+        int parent = 0;
+        for (int level = 0; level < levels - 1; ++level) {
+            const int left = parent * 2 + 1, right = left + 1;
+            int mx = parent;
+            const int pl = left < total ? perm[left * PF] : 0, pr = right < total ? perm[right * PF] : 0;
+            if (left < total && pl == -1) {
+                mx = left;
+            } else if (right < total && pr == -1) {
+                mx = right;
+            } else {
+                float best = dl[perm[parent * PF] * PF];
+                if (left < total && dl[pl * PF] > best) {
+                    mx = left;
+                    best = dl[pl * PF];
+                }
+                if (right < total && dl[pr * PF] > best) mx = right;
+            }
+            if (mx == parent) break;
+            const int8_t t = perm[parent * PF];
+            perm[parent * PF] = perm[mx * PF];
+            perm[mx * PF] = t;
+            parent = mx;
+        }
+    };
+    for (int i = 0; i < maxT; ++i) perm[i * PF] = -1;
+    for (int i = 0; i < M2; ++i) {
+        const int p0 = perm[0];
+        if (p0 == -1 || dl[i * PF] < dl[p0 * PF]) {
+            perm[0] = (int8_t)i;
+            sift(maxT);
+        }
+    }
+    for (int i = maxT - 1; i > 0; --i) {
+        const int8_t t = perm[0];
+        perm[0] = perm[i * PF];
+        perm[i * PF] = t;
+        sift(i);
+    }
+}
+
+template <typename MaskT>
+__global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
+    extern __shared__ __align__(16) unsigned char psm[];
+    const LookupView& lv = a.lv;
+    const int Q = a.Q, T = a.T, L = lv.L, M = lv.M, KW = lv.KW;
+    const int tid = threadIdx.x;
+    const int M2 = 2 * M;
+    // Strided per-thread slices: dl[2M] f32, cd[T] f32, comb[T] MaskT,
+    // enc[2M] u8 (sorted delta -> column | up << 7), ord[M] u8 (down order).
+    float* dl = reinterpret_cast<float*>(psm) + tid;
+    float* cd = dl + M2 * PF;
+    MaskT* comb = reinterpret_cast<MaskT*>(reinterpret_cast<float*>(psm) + (M2 + T) * PF) + tid;
+    uint8_t* enc = reinterpret_cast<uint8_t*>(reinterpret_cast<MaskT*>(
+                       reinterpret_cast<float*>(psm) + (M2 + T) * PF) + T * PF) + tid;
+    uint8_t* ord = enc + M2 * PF;
+    // sorted delta i (value of the column/direction it encodes)
+    auto sv = [&](int i) {
+        const int e = enc[i * PF];
+        return dl[((e & 0x3f) + ((e & 0x80) ? M : 0)) * PF];
+    };
+    const int64_t idx = (int64_t)blockIdx.x * PF + tid;
+    if (idx >= (int64_t)L * Q) return;   // no block-level synchronisation below
+    const int l = (int)(idx / Q), q = (int)(idx - (int64_t)l * Q);
+
+    FastProbeCtx c;
+    c.hkey = 0;
+    c.ok0 = c.okUp = c.okDn = 0;
+    c.allM = M >= 64 ? ~0ull : ((1ull << M) - 1);
+    c.enc = enc;
+    c.funit = lv.funit + 2 * l * M;
+    bool distinct = true;
+    for (int m = 0; m < M; ++m) {
+        const int col = l * M + m;
+        const float v = a.vals[(int64_t)col * Q + q];
+        const float f = floorf(v);
+        const float down = __fsub_rn(v, f);
+        const float up = __fsub_rn(1.0f, down);
+        dl[m * PF] = down;
+        dl[(m + M) * PF] = up;
+        distinct &= (down == down) && (up == up);
+        const int64_t lo = __ldg(lv.cmin + col), hi = __ldg(lv.cmax + col);
+        const int64_t h = (f >= -1.0e15f && f <= 1.0e15f) ? (int64_t)f : (int64_t)1 << 50;
+        c.ok0 |= (uint64_t)(h >= lo && h <= hi) << m;
+        c.okUp |= (uint64_t)(h + 1 >= lo && h + 1 <= hi) << m;
+        c.okDn |= (uint64_t)(h - 1 >= lo && h - 1 <= hi) << m;
+        c.hkey += field_term(h - lo, __ldg(lv.foff + col));
+    }
+
+    if (T > 1) {
+        // Rank the downs (ties or NaN fall back to the heap procedure).
+        for (int i = 0; i < M && distinct; ++i) {
+            const float di = dl[i * PF];
+            int r = 0;
+            for (int j = 0; j < M; ++j) {
+                const float dj = dl[j * PF];
+                r += dj < di;
+                distinct &= (j == i) | (dj != di);
+            }
+            ord[r * PF] = (uint8_t)i;
+        }
+        // Ups in reverse down order must be strictly increasing, then merge.
+        if (distinct) {
+            for (int k = 1; k < M && distinct; ++k)
+                distinct &= dl[(ord[(M - k) * PF] + M) * PF] < dl[(ord[(M - 1 - k) * PF] + M) * PF];
+        }
+        if (distinct) {
+            int id = 0, iu = M - 1;
+            for (int o = 0; o < M2; ++o) {
+                const float vd = id < M ? dl[ord[id * PF] * PF] : FLT_MAX;
+                const float vu = iu >= 0 ? dl[(ord[iu * PF] + M) * PF] : FLT_MAX;
+                const bool take_down = iu < 0 || (id < M && vd < vu);
+                if (id < M && iu >= 0 && vd == vu) {
+                    distinct = false;
+                    break;
+                }
+                const int m = take_down ? ord[id * PF] : ord[iu * PF];
+                enc[o * PF] = (uint8_t)(m | (take_down ? 0 : 0x80));
+                if (take_down) ++id;
+                else --iu;
+            }
+        }
+        if (!distinct) {
+            int8_t* perm = reinterpret_cast<int8_t*>(enc);
+            heap_order_strided(dl, perm, M2, M2);
+            for (int i = 0; i < M2; ++i) {
+                const int pm = perm[i * PF];
+                enc[i * PF] = (uint8_t)((pm % M) | (pm >= M ? 0x80 : 0));
+            }
+        }
+        comb[0] = 1;
+        cd[0] = sv(0);
+    }
+
+    // Probes: enumerate (cuLSH_Kernels.cu:216-255) in groups of eight, issue
+    // the group's slot loads, then resolve them.
+    const uint32_t hmask = __ldg(lv.hmask + l);
+    const unsigned long long* slots = lv.hslots + __ldg(lv.hoff + l);
+    const uint64_t bo = __ldg(lv.boff + l);
+    int32_t* qb = a.qbuckets + (int64_t)l * Q * T + (int64_t)q * T;
+    unsigned long long cnu = 0;
+    int size = 1;
+    constexpr int CH = 8;
+    for (int t0 = 0; t0 < T; t0 += CH) {
+        MaskT pm[CH];
+        unsigned long long slv[CH];
+        uint32_t hsv[CH], fpv[CH], valid = 0;
+#pragma unroll
+        for (int j = 0; j < CH; ++j) {
+            const int t = t0 + j;
+            pm[j] = 0;
+            slv[j] = kEmptySlot;
+            hsv[j] = fpv[j] = 0;
+            if (t < T) {
+                MaskT probe = 0;
+                if (t > 0) {
+                    float mn = FLT_MAX;
+                    int mi = 0;
+                    for (int i = 0; i < size; ++i) {
+                        const float x = cd[i * PF];
+                        if (x < mn) {
+                            mi = i;
+                            mn = x;
+                        }
+                    }
+                    probe = comb[mi * PF];
+                    const int top = 63 - __clzll((long long)(uint64_t)probe);
+                    if (top < M2 - 1) {
+                        const MaskT p1 = probe | ((MaskT)1 << (top + 1));
+                        const float m1 = __fadd_rn(mn, sv(top + 1));
+                        comb[mi * PF] = p1;
+                        cd[mi * PF] = m1;
+                        comb[size * PF] = p1 - ((MaskT)1 << top);
+                        cd[size * PF] = __fsub_rn(m1, sv(top));
+                        ++size;
+                    }
+                }
+                pm[j] = probe;
+                u128 k;
+                if (probe_key(c, probe, k)) {
+                    const uint64_t hh = key_hash128(k, KW);
+                    hsv[j] = (uint32_t)hh & hmask;
+                    fpv[j] = (uint32_t)(hh >> 32);
+                    slv[j] = __ldg(slots + hsv[j]);
+                    valid |= 1u << j;
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < CH; ++j) {
+            const int t = t0 + j;
+            if (t >= T) break;
+            int32_t res = -1;
+            if (valid & (1u << j)) {
+                unsigned long long sl = slv[j];
+                uint32_t h = hsv[j];
+                for (uint32_t p = 0; p <= hmask && sl != kEmptySlot; ++p) {
+                    if ((uint32_t)(sl >> 32) == fpv[j]) {
+                        u128 k;
+                        probe_key(c, pm[j], k);
+                        if (key_matches(lv.ukeys + (bo + (uint32_t)sl) * KW, k, KW)) {
+                            res = (int32_t)(uint32_t)sl;
+                            break;
+                        }
+                    }
+                    h = (h + 1) & hmask;
+                    sl = __ldg(slots + h);
+                }
+            }
+            qb[t] = res;
+            if (res >= 0) cnu += __ldg(lv.sizes + bo + res);
+        }
+    }
+    if (cnu) atomicAdd(a.cnu + q, cnu);
+}
+
+template <typename MaskT>
+cudaError_t launch_probe_fast_t(const ProbeArgs& a, cudaStream_t st) {
+    const int M2 = 2 * a.lv.M, T = a.T;
+    const size_t smem = (size_t)PF * ((M2 + T) * sizeof(float) + T * sizeof(MaskT) + M2 + a.lv.M);
+    static size_t configured = 0;
+    if (smem > 48 * 1024 && smem > configured) {
+        cudaError_t e =
+            cudaFuncSetAttribute(k_probe_fast<MaskT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = smem;
+    }
+    const int64_t n = (int64_t)a.lv.L * a.Q;
+    k_probe_fast<MaskT><<<(unsigned)((n + PF - 1) / PF), PF, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+// 32-bit masks when the 2M sorted deltas fit (M <= 16).
+cudaError_t launch_probe_fast(const ProbeArgs& a, cudaStream_t st) {
+    return a.lv.M <= 16 ? launch_probe_fast_t<uint32_t>(a, st) : launch_probe_fast_t<uint64_t>(a, st);
 }
 
 __device__ __forceinline__ bool lessp(float a, uint32_t ai, float b, uint32_t bi) {
@@ -403,6 +710,9 @@ __global__ void __launch_bounds__(CT) k_candidates(CandArgs a) {
 cudaError_t launch_probe(const ProbeArgs& a, cudaStream_t st) {
     const int64_t n = (int64_t)a.lv.L * a.Q;
     if (n <= 0) return cudaSuccess;
+    // CULSH_PROBE_GENERIC forces the general kernel (the tests run both).
+    const bool generic_only = getenv("CULSH_PROBE_GENERIC") != nullptr;
+    if (!generic_only && a.small_codes && a.lv.KW <= 4 && a.T <= 32 && a.lv.M <= 32) return launch_probe_fast(a, st);
     k_probe<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(a);
     return cudaGetLastError();
 }

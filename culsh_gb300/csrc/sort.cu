@@ -321,8 +321,9 @@ __global__ void k_hash_build(const uint64_t* __restrict__ boff, const uint32_t* 
     uint32_t k[kMaxKW];
     for (int w = 0; w < KW; ++w) k[w] = key[w];
     const uint32_t mask = hmask[l];
-    const uint32_t h = key_hash(k, KW, kSeedSlot);
-    const unsigned long long val = ((unsigned long long)key_hash(k, KW, kSeedFp) << 32) | (uint32_t)j;
+    const uint64_t hh = key_hash64(k, KW);
+    const uint32_t h = (uint32_t)hh;
+    const unsigned long long val = (hh & 0xffffffff00000000ull) | (uint32_t)j;
     unsigned long long* slots = hslots + hoff[l];
     for (uint32_t p = 0; p <= mask; ++p) {
         if (atomicCAS(&slots[(h + p) & mask], kEmptySlot, val) == kEmptySlot) return;

@@ -234,3 +234,16 @@ def test_dropin_cpp_program(culsh, tmp_path):
     import oracle
     oracle.build_index(c["X"], c["A"], c["b"], float(c["W"])).save(str(oracle_file))
     assert open(str(out) + ".index", "rb").read() == oracle_file.read_bytes()
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_search_general_probe_kernel(culsh, name, monkeypatch):
+    """The general multiprobe kernel (any M <= 64, T <= 256, keys <= 256 bits)
+    gives the same results as the fast path the other tests mostly take."""
+    monkeypatch.setenv("CULSH_PROBE_GENERIC", "1")
+    c = load_case(name)
+    ht = build_index(culsh, c)
+    st = culsh.SearchTables()
+    st.reset(ht, int(c["K"]), int(c["T"]))
+    st.search(c["queries"], dataset=c["X"])
+    check_search(st, c)
