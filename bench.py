@@ -287,6 +287,7 @@ def run_culsh(args):
         e1.record(stream)
         torch.cuda.synchronize()
         build_ms.append(e0.elapsed_time(e1))
+    build_profile = ht.profile()
 
     qt = torch.from_numpy(Qm).to(dev)
     ids = torch.empty((Q, K), dtype=torch.int32, device=dev)
@@ -390,6 +391,8 @@ def run_culsh(args):
                            "l2": "flushed by a 256 MB write between timed steps", "parallelism": "replicas"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
                 "clocks": clk, "index_build_ms": round(statistics.median(build_ms), 3),
+                "index_build_stages_ms": {k: (round(v, 4) if isinstance(v, float) else v)
+                                          for k, v in build_profile.items()},
                 "recall_at_k": rec, "recall_sample": ns,
                 "selectivity": st.getSelectivity(), "candidates_unique_per_query": uniq / Q,
                 "candidates_nonunique_per_query": nonuniq / Q}

@@ -56,6 +56,12 @@ class _Profile(ctypes.Structure):
                 ("launches", ctypes.c_int), ("deferred_queries", ctypes.c_int), ("key_words", ctypes.c_int)]
 
 
+class _IndexProfile(ctypes.Structure):
+    _fields_ = [("project_ms", ctypes.c_float), ("pack_ms", ctypes.c_float), ("sort_ms", ctypes.c_float),
+                ("bucket_ms", ctypes.c_float), ("total_ms", ctypes.c_float), ("tensor_cores", ctypes.c_int),
+                ("recomputed", ctypes.c_longlong), ("key_words", ctypes.c_int), ("sort_passes", ctypes.c_int)]
+
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _F = ctypes.c_float
@@ -84,6 +90,7 @@ ABI = {
     "culsh_index_starting_indices": (_UP, [_P, _I]),
     "culsh_index_sizes": (_UP, [_P, _I]),
     "culsh_index_codes": (_FP, [_P, _I]),
+    "culsh_index_profile_get": (_I, [_P, ctypes.POINTER(_IndexProfile)]),
     "culsh_search_create": (_I, [ctypes.POINTER(_P)]),
     "culsh_search_destroy": (None, [_P]),
     "culsh_search_reset": (_I, [_P, _P, _I, _I]),
@@ -222,6 +229,12 @@ class HashTables:
 
     def getBuckets_sizes(self, table):
         return _copy_out(lib().culsh_index_sizes(self._h, table), self.getBuckets(table), np.uint32)
+
+    def profile(self):
+        """Per-stage device milliseconds of the last device index build."""
+        p = _IndexProfile()
+        _check(lib().culsh_index_profile_get(self._h, ctypes.byref(p)))
+        return {n: getattr(p, n) for n, _ in _IndexProfile._fields_}
 
     def getBuckets_codes(self, table):
         B, M = self.getBuckets(table), self.getM()

@@ -153,9 +153,21 @@ struct culsh_index {
 
     // build workspace (kept across builds)
     DevBuf<int32_t> ws_codes, ws_pmin, ws_pmax;
+    DevBuf<uint16_t> ws_ah, ws_al, ws_xh, ws_xl;   // bf16 splits for the tensor-core projection
+    DevBuf<float> ws_anorm, ws_xnorm;
+    DevBuf<int> ws_tcflags;
+    DevBuf<unsigned long long> ws_relist;
+    DevBuf<unsigned int> ws_relist_cnt;
+    long long tc_recomputed = -1;   // codes recomputed after the tensor-core pass (-1: SIMT path)
+    int tc_need_lo = 0;
+    int sort_passes = 0;
+    cudaEvent_t bev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};   // build stage boundaries
+    bool built_once = false;
     DevBuf<uint32_t> ws_keys[2], ws_vals, ws_hist, ws_base, ws_status, ws_tcnt, ws_toff, ws_nb;
 
     ~culsh_index() {
+        for (auto& e : bev)
+            if (e) cudaEventDestroy(e);
         if (stream) cudaStreamDestroy(stream);
     }
     const float* dev_x() const { return x_borrow ? x_borrow : (X.p ? X.p : nullptr); }
@@ -316,22 +328,133 @@ int build_hash(culsh_index* ix, cudaStream_t st) {
     return CULSH_OK;
 }
 
+inline uint16_t bf16_bits_rn(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    const uint32_t bias = 0x7FFFu + ((u >> 16) & 1u);
+    return (uint16_t)((u + bias) >> 16);
+}
+inline float bf16_to_float(uint16_t h) {
+    const uint32_t u = (uint32_t)h << 16;
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+
+// Index projection on the tensor cores when the shape allows it. On success
+// ws_codes holds every code and cmin/cmax their ranges, exactly as the SIMT
+// kernel would produce; *done stays false when the caller must run the SIMT
+// kernel instead (shape not covered, CULSH_PROJECT_SIMT set, non-finite data,
+// a device wait gave up or the recomputation list overflowed).
+int project_tensor_cores(culsh_index* ix, const float* dX, cudaStream_t st, bool* done) {
+    *done = false;
+    ix->tc_recomputed = -1;
+    if (getenv("CULSH_PROJECT_SIMT")) return CULSH_OK;
+    const int N = ix->N, D = ix->D, LM = ix->L * ix->M;
+    int dev = 0, sms = 0, maxsm = 0, major = 0;
+    CU_TRY(cudaGetDevice(&dev));
+    CU_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CU_TRY(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    CU_TRY(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
+    if (major < 10) return CULSH_OK;
+    const TcPlan p = tc_plan(N, D, LM, sms, maxsm);
+    if (!p.ok) return CULSH_OK;
+    // Host split of the projection matrix and upper bounds of its column norms.
+    std::vector<uint16_t> ah((size_t)p.LMp * p.Dp, 0), al((size_t)p.LMp * p.Dp, 0);
+    std::vector<float> an(LM);
+    for (int c = 0; c < LM; ++c) {
+        double ss = 0.0;
+        for (int d = 0; d < D; ++d) {
+            const float v = ix->A[(size_t)c * D + d];
+            const uint16_t h = bf16_bits_rn(v);
+            ah[(size_t)c * p.Dp + d] = h;
+            al[(size_t)c * p.Dp + d] = bf16_bits_rn(v - bf16_to_float(h));
+            ss += (double)v * v;
+        }
+        an[c] = std::nextafter((float)(std::sqrt(ss) * (1.0 + 1e-6)), INFINITY);
+    }
+    CU_TRY(ix->ws_ah.reserve(ah.size()));
+    CU_TRY(ix->ws_al.reserve(al.size()));
+    CU_TRY(ix->ws_anorm.reserve(LM));
+    CU_TRY(cudaMemcpyAsync(ix->ws_ah.p, ah.data(), 2 * ah.size(), cudaMemcpyHostToDevice, st));
+    CU_TRY(cudaMemcpyAsync(ix->ws_al.p, al.data(), 2 * al.size(), cudaMemcpyHostToDevice, st));
+    CU_TRY(cudaMemcpyAsync(ix->ws_anorm.p, an.data(), 4 * LM, cudaMemcpyHostToDevice, st));
+    const size_t nx = (size_t)N * p.Dp;
+    CU_TRY(ix->ws_xh.reserve(nx));
+    CU_TRY(ix->ws_xl.reserve(nx));
+    CU_TRY(ix->ws_xnorm.reserve(N));
+    CU_TRY(ix->ws_tcflags.reserve(4));
+    CU_TRY(cudaMemsetAsync(ix->ws_tcflags.p, 0, 16, st));
+    CU_TRY(launch_split_rows(dX, N, D, p.Dp, ix->ws_xh.p, ix->ws_xl.p, ix->ws_xnorm.p, ix->ws_tcflags.p, st));
+    int flags = 0;
+    CU_TRY(cudaMemcpyAsync(&flags, ix->ws_tcflags.p, 4, cudaMemcpyDeviceToHost, st));
+    CU_TRY(cudaStreamSynchronize(st));
+    if (flags & 2) return CULSH_OK;   // non-finite data: the SIMT kernel reports it
+    const int need_lo = flags & 1;
+    // One recomputation region per CTA, sized for 1/6 of its codes.
+    const unsigned long long cap = ((unsigned long long)N * LM / 6) / p.grid + 4096;
+    CU_TRY(ix->ws_relist.reserve(cap * p.grid));
+    CU_TRY(ix->ws_relist_cnt.reserve(p.grid));
+    CU_TRY(ix->ws_pmin.reserve((size_t)p.grid * LM));
+    CU_TRY(ix->ws_pmax.reserve((size_t)p.grid * LM));
+    // Bound on |tensor-core sum - canonical FP32 chain| per unit of sum|x||a|
+    // (bounded by |x|_2 |a|_2): split residue, one rounding per summed
+    // product, the canonical chain's rounding; 1.25 margin.
+    const double u24 = std::ldexp(1.0, -24), u23 = std::ldexp(1.0, -23), u16 = std::ldexp(1.0, -16);
+    const double split = need_lo ? 3.02 * u16 : 1.01 * u16;
+    const double accum = ((need_lo ? 3.0 : 2.0) * D + 16) * u23;
+    const float kappa = (float)(1.25 * ((D + 2) * u24 + split + accum));
+    CU_TRY(launch_project_tc(p, need_lo, N, D, LM, ix->ws_xh.p, ix->ws_xl.p, ix->ws_ah.p, ix->ws_al.p, ix->db.p,
+                             ix->ws_anorm.p, ix->ws_xnorm.p, ix->W, kappa, ix->ws_codes.p, ix->ws_pmin.p, ix->ws_pmax.p,
+                             ix->ws_relist.p, cap, ix->ws_relist_cnt.p, ix->err.p, st));
+    CU_TRY(launch_minmax_reduce(ix->ws_pmin.p, ix->ws_pmax.p, p.grid, LM, ix->cmin.p, ix->cmax.p, st));
+    std::vector<unsigned int> cnt(p.grid);
+    int err = 0;
+    CU_TRY(cudaMemcpyAsync(cnt.data(), ix->ws_relist_cnt.p, 4 * p.grid, cudaMemcpyDeviceToHost, st));
+    CU_TRY(cudaMemcpyAsync(&err, ix->err.p, 4, cudaMemcpyDeviceToHost, st));
+    CU_TRY(cudaStreamSynchronize(st));
+    unsigned long long nre = 0;
+    bool overflow = false;
+    for (unsigned int c : cnt) {
+        nre += c;
+        overflow |= c > cap;
+    }
+    if (err != 0 || overflow) {
+        CU_TRY(cudaMemsetAsync(ix->err.p, 0, sizeof(int), st));
+        return CULSH_OK;   // fall back to the SIMT kernel
+    }
+    if (nre)
+        CU_TRY(launch_tc_recompute(dX, N, D, LM, ix->dA.p, ix->db.p, ix->W, ix->ws_relist.p, cap, ix->ws_relist_cnt.p,
+                                   p.grid, ix->ws_codes.p, ix->cmin.p, ix->cmax.p, ix->err.p, st));
+    ix->tc_recomputed = (long long)nre;
+    ix->tc_need_lo = need_lo;
+    *done = true;
+    return CULSH_OK;
+}
+
 // Index build from a device-resident dataset (cuLSH_HashTables.cu:486-520).
 int build_device(culsh_index* ix, const float* dX, cudaStream_t st, FILE* dbg) {
     const int N = ix->N, D = ix->D, L = ix->L, M = ix->M, LM = L * M;
     const double t0 = seconds_now();
+    for (auto& e : ix->bev)
+        if (!e) CU_TRY(cudaEventCreate(&e));
+    CU_TRY(cudaEventRecord(ix->bev[0], st));
     TRY(upload_projection(ix, st));
     CU_TRY(ix->err.reserve(1));
     CU_TRY(cudaMemsetAsync(ix->err.p, 0, sizeof(int), st));
-    const int gx = project_grid_x(N);
     CU_TRY(ix->ws_codes.reserve((size_t)LM * N));
-    CU_TRY(ix->ws_pmin.reserve((size_t)gx * LM));
-    CU_TRY(ix->ws_pmax.reserve((size_t)gx * LM));
     CU_TRY(ix->cmin.reserve(LM));
     CU_TRY(ix->cmax.reserve(LM));
-    CU_TRY(launch_project_fp32(dX, N, D, ix->dA.p, ix->db.p, LM, ix->W, ix->ws_codes.p, nullptr, ix->ws_pmin.p,
-                               ix->ws_pmax.p, ix->err.p, st));
-    CU_TRY(launch_minmax_reduce(ix->ws_pmin.p, ix->ws_pmax.p, gx, LM, ix->cmin.p, ix->cmax.p, st));
+    bool tc_done = false;
+    TRY(project_tensor_cores(ix, dX, st, &tc_done));
+    if (!tc_done) {
+        const int gx = project_grid_x(N);
+        CU_TRY(ix->ws_pmin.reserve((size_t)gx * LM));
+        CU_TRY(ix->ws_pmax.reserve((size_t)gx * LM));
+        CU_TRY(launch_project_fp32(dX, N, D, ix->dA.p, ix->db.p, LM, ix->W, ix->ws_codes.p, nullptr, ix->ws_pmin.p,
+                                   ix->ws_pmax.p, ix->err.p, st));
+        CU_TRY(launch_minmax_reduce(ix->ws_pmin.p, ix->ws_pmax.p, gx, LM, ix->cmin.p, ix->cmax.p, st));
+    }
     ix->h_cmin.resize(LM);
     ix->h_cmax.resize(LM);
     CU_TRY(cudaMemcpyAsync(ix->h_cmin.data(), ix->cmin.p, 4 * LM, cudaMemcpyDeviceToHost, st));
@@ -340,9 +463,12 @@ int build_device(culsh_index* ix, const float* dX, cudaStream_t st, FILE* dbg) {
     int passes = 0;
     TRY(compute_layout(ix, &passes));
     TRY(upload_layout(ix, st));
+    ix->sort_passes = passes;
+    CU_TRY(cudaEventRecord(ix->bev[1], st));
     if (dbg)
-        fprintf(dbg, "[HashTables::index]\tprojected %d points onto %d tables x %d columns; %d key words, %d sort passes\n",
-                N, L, M, ix->KW, passes);
+        fprintf(dbg, "[HashTables::index]\tprojected %d points onto %d tables x %d columns (%s, %lld codes recomputed); "
+                "%d key words, %d sort passes\n",
+                N, L, M, ix->tc_recomputed >= 0 ? "tensor cores" : "FP32 SIMT", ix->tc_recomputed, ix->KW, passes);
 
     // Pack keys and sort all tables at once.
     const size_t LN = (size_t)L * N;
@@ -366,7 +492,9 @@ int build_device(culsh_index* ix, const float* dX, cudaStream_t st, FILE* dbg) {
     sb.status = ix->ws_status.p;
     sb.err = ix->err.p;
     bool alt = false;
+    CU_TRY(cudaEventRecord(ix->bev[2], st));
     CU_TRY(run_segmented_sort(sb, N, L, ix->KW, passes, &alt, st));
+    CU_TRY(cudaEventRecord(ix->bev[3], st));
     const uint32_t* skeys = ix->ws_keys[alt ? 1 : 0].p;
     if (alt) ix->ids.swap(ix->ws_vals);
 
@@ -394,9 +522,11 @@ int build_device(culsh_index* ix, const float* dX, cudaStream_t st, FILE* dbg) {
     CU_TRY(launch_rl_write(skeys, N, L, ix->KW, ix->ws_toff.p, ix->boff.p, ix->starts.p, ix->ukeys.p, st));
     CU_TRY(launch_bucket_sizes(ix->boff.p, ix->starts.p, N, L, maxB, ix->sizes.p, st));
     TRY(build_hash(ix, st));
+    CU_TRY(cudaEventRecord(ix->bev[4], st));
     TRY(read_err_flag(ix, st, "index"));
     ix->indexed = ix->dev_valid = true;
     ix->host_valid = false;
+    ix->built_once = true;
     if (dbg) {
         for (int l = 0; l < L; ++l)
             fprintf(dbg, "[HashTables::index]\ttable %d/%d -----> %u distinct buckets\n", l + 1, L, ix->buckets[l]);
@@ -898,6 +1028,23 @@ const unsigned* culsh_index_starting_indices(culsh_index* ix, int table) { HOST_
 const unsigned* culsh_index_sizes(culsh_index* ix, int table) { HOST_GETTER(sizes, h_sizes) }
 const float* culsh_index_codes(culsh_index* ix, int table) { HOST_GETTER(codes, h_codes) }
 #undef HOST_GETTER
+
+int culsh_index_profile_get(culsh_index* ix, culsh_index_profile* out) {
+    if (!ix || !out) return fail(CULSH_ERR_INVALID_ARGUMENT, "null argument");
+    *out = culsh_index_profile{};
+    if (!ix->built_once) return fail(CULSH_ERR_STATE, "no index has been built on the device");
+    CU_TRY(cudaEventSynchronize(ix->bev[4]));
+    CU_TRY(cudaEventElapsedTime(&out->project_ms, ix->bev[0], ix->bev[1]));
+    CU_TRY(cudaEventElapsedTime(&out->pack_ms, ix->bev[1], ix->bev[2]));
+    CU_TRY(cudaEventElapsedTime(&out->sort_ms, ix->bev[2], ix->bev[3]));
+    CU_TRY(cudaEventElapsedTime(&out->bucket_ms, ix->bev[3], ix->bev[4]));
+    CU_TRY(cudaEventElapsedTime(&out->total_ms, ix->bev[0], ix->bev[4]));
+    out->tensor_cores = ix->tc_recomputed >= 0;
+    out->recomputed = ix->tc_recomputed;
+    out->key_words = ix->KW;
+    out->sort_passes = ix->sort_passes;
+    return CULSH_OK;
+}
 
 int culsh_search_create(culsh_search** out) {
     if (!out) return fail(CULSH_ERR_INVALID_ARGUMENT, "null output pointer");

@@ -102,6 +102,28 @@ int project_grid_x(int64_t n_pts);
 cudaError_t launch_minmax_reduce(const int32_t* pmin, const int32_t* pmax, int nparts, int LM, int32_t* cmin,
                                  int32_t* cmax, cudaStream_t st);
 
+// Tensor-core (tcgen05) projection for index builds: plan, bf16 split of X,
+// the GEMM with the proven-code epilogue, and the canonical recomputation of
+// the codes its error bound could not prove.
+struct TcPlan {
+    bool ok;
+    int Dp, LMp, ntiles, grid, tmem_cols;
+    uint32_t b_bytes, x_bytes;
+    int stages[2];        // X-tile ring depth without / with the low bf16 part
+    size_t smem[2];
+};
+TcPlan tc_plan(int64_t N, int D, int LM, int num_sms, int max_smem);
+cudaError_t launch_split_rows(const float* X, int64_t N, int D, int Dp, void* xh, void* xl, float* xnorm, int* flags,
+                              cudaStream_t st);
+cudaError_t launch_project_tc(const TcPlan& p, int need_lo, int64_t N, int D, int LM, const void* xh, const void* xl,
+                              const void* ah, const void* al, const float* b, const float* anorm, const float* xnorm,
+                              float W, float kappa, int32_t* codes, int32_t* pmin, int32_t* pmax,
+                              unsigned long long* relist, unsigned long long relist_cap, unsigned int* relist_cnt,
+                              int* err, cudaStream_t st);
+cudaError_t launch_tc_recompute(const float* X, int64_t N, int D, int LM, const float* A, const float* b, float W,
+                                const unsigned long long* list, unsigned long long cap, const unsigned int* cnt,
+                                int regions, int32_t* codes, int32_t* cmin, int32_t* cmax, int* err, cudaStream_t st);
+
 // Key packing from int codes [LM][N] into SoA keys [KW][L*N] and identity values.
 cudaError_t launch_pack_keys(const int32_t* codes, int64_t N, int L, int M, int KW, const int32_t* cmin,
                              const uint8_t* fbits, const uint16_t* foff, uint32_t* keys, uint32_t* vals,

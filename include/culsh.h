@@ -98,6 +98,21 @@ const unsigned* culsh_index_starting_indices(culsh_index* ix, int table);
 const unsigned* culsh_index_sizes(culsh_index* ix, int table);
 const float* culsh_index_codes(culsh_index* ix, int table);
 
+/* Measurement aid with no counterpart in the reference: device time of each
+ * stage of the last device index build (CUDA events on its stream). */
+typedef struct culsh_index_profile {
+    float project_ms;      /* projection + codes (tensor-core or FP32 SIMT kernel) */
+    float pack_ms;         /* packing codes into sort keys                         */
+    float sort_ms;         /* radix sort of all tables                             */
+    float bucket_ms;       /* run-length bucketing + hash build                    */
+    float total_ms;
+    int tensor_cores;      /* 1 when the tcgen05 projection produced the codes     */
+    long long recomputed;  /* codes its error bound left to the FP32 recomputation */
+    int key_words;         /* 32-bit words of a packed bucket key                  */
+    int sort_passes;       /* 8-bit digit passes over the keys                     */
+} culsh_index_profile;
+int culsh_index_profile_get(culsh_index* ix, culsh_index_profile* out);
+
 /* ---- SearchTables -------------------------------------------------------- */
 int culsh_search_create(culsh_search** out);        /* SearchTables::SearchTables  cuLSH_SearchTables.cu:112-122 */
 void culsh_search_destroy(culsh_search* s);         /* SearchTables::~SearchTables cuLSH_SearchTables.cu:74 */

@@ -247,3 +247,12 @@ def test_search_general_probe_kernel(culsh, name, monkeypatch):
     st.reset(ht, int(c["K"]), int(c["T"]))
     st.search(c["queries"], dataset=c["X"])
     check_search(st, c)
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_index_simt_projection(culsh, name, monkeypatch):
+    """The SIMT projection kernel (the form every shape supports) builds the
+    same index as the tensor-core kernel most cases take."""
+    monkeypatch.setenv("CULSH_PROJECT_SIMT", "1")
+    c = load_case(name)
+    check_index(build_index(culsh, c), c)
