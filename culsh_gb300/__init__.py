@@ -53,7 +53,8 @@ class _Times(ctypes.Structure):
 
 class _Profile(ctypes.Structure):
     _fields_ = [("project_ms", ctypes.c_float), ("probe_ms", ctypes.c_float), ("candidates_ms", ctypes.c_float),
-                ("launches", ctypes.c_int), ("deferred_queries", ctypes.c_int), ("key_words", ctypes.c_int)]
+                ("launches", ctypes.c_int), ("deferred_queries", ctypes.c_int), ("key_words", ctypes.c_int),
+                ("candidates_mode", ctypes.c_int)]
 
 
 class _IndexProfile(ctypes.Structure):

@@ -188,6 +188,13 @@ struct culsh_search {
     DevBuf<unsigned long long> cnu, cu, stats;
     DevBuf<int> deferred;
     DevBuf<uint32_t> arena;
+    // work-stealing candidate stage
+    DevBuf<int> q_items, q_off, item_q, part_n;
+    DevBuf<unsigned int> q_done;
+    DevBuf<uint8_t> item_p;
+    DevBuf<float> part_d;
+    DevBuf<uint32_t> part_i;
+    int ws_grid = 0, ws_D = 0, ws_K = 0, ws_used = 0, ws_overflow = 0;
     PinBuf<int32_t> h_ids, h_qb;
     PinBuf<float> h_d;
     PinBuf<unsigned long long> h_stats;
@@ -658,6 +665,86 @@ size_t arena_cap_words() {
     return ~size_t(0);
 }
 
+// The candidate stage runs as the persistent work-stealing kernel unless
+// CULSH_CANDIDATES_PER_QUERY is set (one block per query; the tests run both).
+int use_work_stealing() { return getenv("CULSH_CANDIDATES_PER_QUERY") == nullptr; }
+
+constexpr int kWsPartitions = 64;              // most partitions of one query
+constexpr unsigned long long kWsChunk = 1024;  // non-unique candidates per partition
+constexpr size_t kWsPartialBytes = size_t(64) << 20;
+
+// Sizes the work-stealing buffers and fills the kernel arguments. stats[4]
+// holds the item counter (low word) and the overflow flag (high word),
+// stats[5] the number of items.
+// CULSH_WS_PARTITIONS (1..64) and CULSH_WS_ITEMS lower the partition count
+// and the item capacity; the tests use them to reach both overflow re-runs.
+int env_int(const char* name, int lo, int hi, int dflt) {
+    const char* e = getenv(name);
+    if (!e) return dflt;
+    const long long v = atoll(e);
+    return v < lo ? lo : (v > hi ? hi : (int)v);
+}
+
+int prepare_ws(culsh_search* s, const CandArgs& ca, WsArgs* w, cudaStream_t st) {
+    (void)st;
+    const int Q = ca.Q, K = ca.K;
+    const int pmax = env_int("CULSH_WS_PARTITIONS", 1, kWsPartitions, kWsPartitions);
+    const size_t per_item = (size_t)K * 8 + 4 + 4 + 1;
+    size_t cap = std::max<size_t>((size_t)Q * 2, kWsPartialBytes / per_item);
+    cap = std::min(cap, (size_t)Q * pmax);
+    cap = std::min<size_t>(cap, (size_t)env_int("CULSH_WS_ITEMS", 1, 0x7fffffff, 0x7fffffff));
+    CU_TRY(s->q_items.reserve(Q));
+    CU_TRY(s->q_off.reserve(Q));
+    CU_TRY(s->q_done.reserve(Q));
+    CU_TRY(s->item_q.reserve(cap));
+    CU_TRY(s->item_p.reserve(cap));
+    CU_TRY(s->part_n.reserve(cap));
+    CU_TRY(s->part_d.reserve(cap * K));
+    CU_TRY(s->part_i.reserve(cap * K));
+    if (!s->ws_grid || s->ws_D != ca.D || s->ws_K != K) {
+        int dev = 0, sms = 0;
+        CU_TRY(cudaGetDevice(&dev));
+        CU_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        s->ws_grid = sms * ws_blocks_per_sm(ca.D, K);
+        s->ws_D = ca.D;
+        s->ws_K = K;
+    }
+    WsArgs& a = *w;
+    a.X = ca.X;
+    a.N = ca.N;
+    a.D = ca.D;
+    a.L = ca.L;
+    a.T = ca.T;
+    a.Q = Q;
+    a.K = K;
+    a.queries = ca.queries;
+    a.qbuckets = ca.qbuckets;
+    a.boff = ca.boff;
+    a.starts = ca.starts;
+    a.sizes = ca.sizes;
+    a.ids = ca.ids;
+    a.cnu = ca.cnu;
+    a.out_ids = ca.out_ids;
+    a.out_d = ca.out_d;
+    a.cu = ca.cu;
+    a.totals = ca.totals;
+    a.pmax = pmax;
+    a.chunk = kWsChunk;
+    a.q_items = s->q_items.p;
+    a.q_off = s->q_off.p;
+    a.q_done = s->q_done.p;
+    a.item_q = s->item_q.p;
+    a.item_p = s->item_p.p;
+    a.part_n = s->part_n.p;
+    a.part_d = s->part_d.p;
+    a.part_i = s->part_i.p;
+    a.item_cap = (unsigned int)cap;
+    a.next_item = reinterpret_cast<unsigned int*>(s->stats.p + 4);
+    a.overflow = reinterpret_cast<unsigned int*>(s->stats.p + 4) + 1;
+    a.n_items = reinterpret_cast<unsigned int*>(s->stats.p + 5);
+    return CULSH_OK;
+}
+
 // The query path on device buffers (cuLSH_SearchTables.cu:197-463).
 int search_device(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* d_d, cudaStream_t st) {
     culsh_index* ix = s->ix;
@@ -670,9 +757,9 @@ int search_device(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float
     CU_TRY(s->qb.reserve((size_t)L * Q * T));
     CU_TRY(s->cnu.reserve(Q));
     CU_TRY(s->cu.reserve(Q));
-    CU_TRY(s->stats.reserve(4));
+    CU_TRY(s->stats.reserve(8));
     CU_TRY(s->deferred.reserve(2 * (size_t)Q));
-    CU_TRY(s->h_stats.reserve(4));
+    CU_TRY(s->h_stats.reserve(8));
     const size_t cap_words = arena_cap_words();
     const size_t init_words = std::min(kArenaInitialWords, cap_words);
     if (s->arena.n < init_words || s->arena.n > cap_words) {
@@ -680,7 +767,7 @@ int search_device(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float
         CU_TRY(s->arena.reserve(init_words));
     }
     CU_TRY(cudaMemsetAsync(s->cnu.p, 0, 8 * (size_t)Q, st));
-    CU_TRY(cudaMemsetAsync(s->stats.p, 0, 8 * 4, st));
+    CU_TRY(cudaMemsetAsync(s->stats.p, 0, 8 * 8, st));
     s->launches = 0;
     s->deferred_queries = 0;
     s->host_copy_timed = false;
@@ -724,11 +811,32 @@ int search_device(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float
     ca.n_deferred = reinterpret_cast<unsigned int*>(s->stats.p + 3);
     ca.qlist = nullptr;
     ca.nq = Q;
-    CU_TRY(launch_candidates(ca, st));
-    s->launches += 1;
+    s->ws_used = use_work_stealing();
+    s->ws_overflow = 0;
+    if (s->ws_used) {
+        WsArgs wa;
+        TRY(prepare_ws(s, ca, &wa, st));
+        CU_TRY(launch_plan_items(wa, st));
+        CU_TRY(launch_candidates_ws(wa, s->ws_grid, st));
+        s->launches += 2;
+    } else {
+        CU_TRY(launch_candidates(ca, st));
+        s->launches += 1;
+    }
     CU_TRY(cudaEventRecord(s->ev[3], st));
-    CU_TRY(cudaMemcpyAsync(s->h_stats.p, s->stats.p, 8 * 4, cudaMemcpyDeviceToHost, st));
+    CU_TRY(cudaMemcpyAsync(s->h_stats.p, s->stats.p, 8 * 8, cudaMemcpyDeviceToHost, st));
     CU_TRY(cudaStreamSynchronize(st));
+    if (s->ws_used && (s->h_stats.p[4] >> 32) != 0) {
+        // A partition overflowed the shared-memory set (or the plan outgrew the
+        // partial-list buffers): redo the stage with the per-query kernel,
+        // whose global arena takes any set size.
+        s->ws_overflow = 1;
+        CU_TRY(cudaMemsetAsync(s->stats.p, 0, 8 * 8, st));
+        CU_TRY(launch_candidates(ca, st));
+        s->launches += 1;
+        CU_TRY(cudaMemcpyAsync(s->h_stats.p, s->stats.p, 8 * 8, cudaMemcpyDeviceToHost, st));
+        CU_TRY(cudaStreamSynchronize(st));
+    }
     unsigned int ndef = (unsigned int)(s->h_stats.p[3] & 0xffffffffu);
     if (ndef) {
         // Queries whose candidate sets did not fit the arena: admit them in
@@ -1181,6 +1289,7 @@ int culsh_search_profile_get(culsh_search* s, culsh_search_profile* out) {
     out->launches = s->launches;
     out->deferred_queries = s->deferred_queries;
     out->key_words = s->ix ? s->ix->KW : 0;
+    out->candidates_mode = s->ws_used ? (s->ws_overflow ? 2 : 1) : 0;
     return CULSH_OK;
 }
 

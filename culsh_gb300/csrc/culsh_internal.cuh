@@ -204,6 +204,43 @@ struct CandArgs {
     const int* qlist;                  // optional subset of queries (nullptr = all)
     int nq;
 };
+// Work-stealing form of the candidate stage (candidates.cu): queries split
+// into id-partition items, claimed by a persistent grid.
+struct WsArgs {
+    const float* X;
+    int64_t N;
+    int D, L, T, Q, K;
+    const float* queries;              // [Q][D]
+    const int32_t* qbuckets;           // [L][Q*T]
+    const uint64_t* boff;
+    const uint32_t* starts;
+    const uint32_t* sizes;
+    const uint32_t* ids;               // [L][N]
+    const unsigned long long* cnu;     // [Q]
+    int32_t* out_ids;                  // [Q][K]
+    float* out_d;                      // [Q][K]
+    unsigned long long* cu;            // [Q] unique counts
+    unsigned long long* totals;        // [2]: sum unique, sum non-unique
+    int pmax;                          // partitions per query, at most 64
+    unsigned long long chunk;          // non-unique candidates per partition
+    int* q_items;                      // [Q] partitions of each query
+    int* q_off;                        // [Q] first item of each query
+    unsigned int* q_done;              // [Q] partitions finished
+    int* item_q;                       // [item_cap]
+    uint8_t* item_p;                   // [item_cap]
+    int* part_n;                       // [item_cap] partial list lengths
+    float* part_d;                     // [item_cap][K]
+    uint32_t* part_i;                  // [item_cap][K]
+    unsigned int item_cap;
+    unsigned int* n_items;
+    unsigned int* next_item;           // work-stealing counter, zero before the launch
+    unsigned int* overflow;            // nonzero: rerun with the per-query kernel
+};
+size_t ws_smem_bytes(int D, int K);
+int ws_blocks_per_sm(int D, int K);
+cudaError_t launch_plan_items(const WsArgs& a, cudaStream_t st);
+cudaError_t launch_candidates_ws(const WsArgs& a, int grid, cudaStream_t st);
+
 int cand_smem_capacity();              // candidates handled in shared memory per query
 cudaError_t launch_candidates(const CandArgs& a, cudaStream_t st);
 size_t cand_arena_words(unsigned long long nonunique);

@@ -20,6 +20,7 @@
 #include <cstdlib>
 
 #include "culsh_internal.cuh"
+#include "topk_common.cuh"
 
 namespace culsh {
 namespace {
@@ -28,7 +29,6 @@ constexpr int CT = 128;
 constexpr int CW = CT / 32;
 constexpr int SM_SLOTS = 4096;
 constexpr int SM_CAP = SM_SLOTS / 2;
-constexpr uint32_t kEmpty32 = 0xFFFFFFFFu;
 
 __device__ __forceinline__ int ceil_log2_dev(int n) {
     int l = 0;
@@ -489,65 +489,6 @@ cudaError_t launch_probe_fast(const ProbeArgs& a, cudaStream_t st) {
     return a.lv.M <= 16 ? launch_probe_fast_t<uint32_t>(a, st) : launch_probe_fast_t<uint64_t>(a, st);
 }
 
-__device__ __forceinline__ bool lessp(float a, uint32_t ai, float b, uint32_t bi) {
-    return a < b || (a == b && ai < bi);
-}
-
-// Inserts (d, id) into a warp's sorted list [0, n) of capacity K; all lanes
-// call it with the same arguments. Keeps ascending (distance, id) order.
-__device__ __forceinline__ void warp_insert(float* wd, uint32_t* wi, int& n, int K, float d, uint32_t id,
-                                            float& thr_d, uint32_t& thr_i) {
-    const int lane = threadIdx.x & 31;
-    int pos = 0;
-    for (int b = 0; b < n; b += 32) {
-        const int e = b + lane;
-        const bool lt = e < n && lessp(wd[e], wi[e], d, id);
-        pos += __popc(__ballot_sync(0xffffffffu, lt));
-    }
-    if (pos >= K) return;
-    const int newn = min(n + 1, K);
-    for (int hi = newn - 1; hi > pos; hi -= 32) {
-        const int e = hi - lane;
-        const bool act = e > pos;
-        float vd = 0.f;
-        uint32_t vi = 0;
-        if (act) {
-            vd = wd[e - 1];
-            vi = wi[e - 1];
-        }
-        __syncwarp();
-        if (act) {
-            wd[e] = vd;
-            wi[e] = vi;
-        }
-        __syncwarp();
-    }
-    if (lane == 0) {
-        wd[pos] = d;
-        wi[pos] = id;
-    }
-    __syncwarp();
-    n = newn;
-    if (n == K) {
-        thr_d = wd[K - 1];
-        thr_i = wi[K - 1];
-    }
-}
-
-__device__ __forceinline__ void set_insert(uint32_t* hset, uint32_t mask, uint32_t* ulist, uint32_t* ucount,
-                                           uint32_t id) {
-    uint32_t h = mix32(id) & mask;
-    for (uint32_t p = 0; p <= mask; ++p) {
-        const uint32_t prev = atomicCAS(&hset[h], kEmpty32, id);
-        if (prev == kEmpty32) {
-            ulist[atomicAdd(ucount, 1u)] = id;
-            return;
-        }
-        if (prev == id) return;
-        h = (h + 1) & mask;
-    }
-}
-
 __global__ void __launch_bounds__(CT) k_candidates(CandArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ uint32_t s_ucount;
@@ -605,6 +546,7 @@ __global__ void __launch_bounds__(CT) k_candidates(CandArgs a) {
     // reference's candidate lists are) and deduplicate them.
     const int LT = L * T;
     const uint32_t mask = cap - 1;
+    const uint32_t lcap = C > (unsigned long long)SM_CAP ? (uint32_t)C : (uint32_t)SM_CAP;
     for (int e = warp; e < LT; e += CW) {
         const int l = e / T, t = e - l * T;
         const int32_t j = a.qbuckets[(int64_t)l * a.Q * T + (int64_t)q * T + t];
@@ -612,7 +554,7 @@ __global__ void __launch_bounds__(CT) k_candidates(CandArgs a) {
         const uint64_t g = a.boff[l] + (uint32_t)j;
         const uint32_t st = a.starts[g], sz = a.sizes[g];
         const uint32_t* src = a.ids + (int64_t)l * a.N + st;
-        for (uint32_t k = lane; k < sz; k += 32) set_insert(hset, mask, ulist, &s_ucount, __ldg(src + k));
+        for (uint32_t k = lane; k < sz; k += 32) set_insert(hset, mask, ulist, lcap, &s_ucount, __ldg(src + k));
     }
     __syncthreads();
     const uint32_t U = s_ucount;

@@ -147,6 +147,9 @@ typedef struct culsh_search_profile {
     int launches;        /* kernels launched by libculsh in the last search    */
     int deferred_queries;/* queries re-run after growing the overflow arena    */
     int key_words;       /* 32-bit words of a packed bucket key (index layout) */
+    int candidates_mode; /* 0: one block per query; 1: persistent work-stealing
+                            grid over id partitions; 2: work-stealing, re-run
+                            per query after a partition overflowed            */
 } culsh_search_profile;
 int culsh_search_profile_get(culsh_search* s, culsh_search_profile* out);
 

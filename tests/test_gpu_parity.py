@@ -143,7 +143,10 @@ def test_overflow_arena_and_deferred_admission(culsh, monkeypatch):
     """Candidate sets larger than shared memory use the global arena; with a
     tiny arena the queries are deferred and admitted in chunks; with an arena
     smaller than one query's set the search fails like the reference's
-    admission check (cuLSH_SearchTables.cu:303-306)."""
+    admission check (cuLSH_SearchTables.cu:303-306). The arena belongs to
+    the per-query candidate kernel (the work-stealing kernel partitions
+    large sets instead and needs none), so the test selects that kernel."""
+    monkeypatch.setenv("CULSH_CANDIDATES_PER_QUERY", "1")
     c = load_case("heavy")
     assert int(c["nonunique"].max()) > 2048
     ht = build_index(culsh, c)
@@ -256,3 +259,72 @@ def test_index_simt_projection(culsh, name, monkeypatch):
     monkeypatch.setenv("CULSH_PROJECT_SIMT", "1")
     c = load_case(name)
     check_index(build_index(culsh, c), c)
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_search_per_query_candidates_kernel(culsh, name, monkeypatch):
+    """The per-query candidate kernel (one block per query) and the default
+    persistent work-stealing kernel give identical results."""
+    monkeypatch.setenv("CULSH_CANDIDATES_PER_QUERY", "1")
+    c = load_case(name)
+    ht = build_index(culsh, c)
+    st = culsh.SearchTables()
+    st.reset(ht, int(c["K"]), int(c["T"]))
+    st.search(c["queries"], dataset=c["X"])
+    check_search(st, c)
+    np.testing.assert_array_equal(st.getKnnDistances(), c["knn_dists"])
+    assert st.profile()["candidates_mode"] == 0
+
+
+def test_work_stealing_partitions_and_overflow_reruns(culsh, monkeypatch):
+    """'heavy' splits its larger queries into several id partitions whose
+    partial top-K lists are merged; a partition that overflows the shared
+    set, or a plan larger than the item buffers, re-runs per query."""
+    c = load_case("heavy")
+    ht = build_index(culsh, c)
+    st = culsh.SearchTables()
+    st.reset(ht, int(c["K"]), int(c["T"]))
+    st.search(c["queries"], dataset=c["X"])
+    check_search(st, c)
+    assert st.profile()["candidates_mode"] == 1
+    monkeypatch.setenv("CULSH_WS_PARTITIONS", "1")
+    st.search(c["queries"], dataset=c["X"])
+    check_search(st, c)
+    assert st.profile()["candidates_mode"] == 2
+    monkeypatch.delenv("CULSH_WS_PARTITIONS")
+    monkeypatch.setenv("CULSH_WS_ITEMS", "5")
+    st.search(c["queries"], dataset=c["X"])
+    check_search(st, c)
+    assert st.profile()["candidates_mode"] == 2
+    monkeypatch.delenv("CULSH_WS_ITEMS")
+    st.search(c["queries"], dataset=c["X"])
+    check_search(st, c)
+    assert st.profile()["candidates_mode"] == 1
+
+
+def test_work_stealing_large_candidate_sets(culsh):
+    """Queries with about 90,000 distinct candidates each (64 partitions per
+    query) mixed with queries that have none, against the oracle."""
+    import oracle
+    rng = np.random.default_rng(77)
+    N, D, L, M, W = 90000, 8, 3, 2, 40.0
+    X = rng.normal(0, 1, (N, D)).astype(np.float32)
+    A = rng.normal(0, 1, (L, M, D)).astype(np.float32)
+    b = rng.uniform(0, W, (L, M)).astype(np.float32)
+    far = np.full((3, D), 500.0, np.float32)
+    queries = np.concatenate([X[:5] + 0.01, far, X[5:8]]).astype(np.float32)
+    K, T = 16, 3
+    ht = culsh.HashTables()
+    ht.reset(N, D, L, M, W, A=A, b=b)
+    ht.index(X)
+    st = culsh.SearchTables()
+    st.reset(ht, K, T)
+    st.search(queries, dataset=X)
+    assert st.profile()["candidates_mode"] == 1
+    idx = oracle.build_index(X, A, b, W)
+    ref = oracle.search(idx, X, queries, K, T)
+    np.testing.assert_array_equal(st.getKnnIds(), ref["knn_ids"])
+    np.testing.assert_array_equal(st.getKnnDistances(), ref["knn_dists"])
+    assert st.getTotalCandidates_unique() == int(ref["unique"].sum())
+    assert st.getTotalCandidates_nonUnique() == int(ref["nonunique"].sum())
+    assert int(ref["unique"][:5].min()) > 60000 and int(ref["nonunique"][5:8].max()) == 0
