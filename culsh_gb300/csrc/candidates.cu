@@ -32,6 +32,7 @@ constexpr int WW = WT / 32;
 constexpr int W_SLOTS = 4096;          // shared hash slots per item
 constexpr int W_CAP = W_SLOTS / 2;     // distinct ids per item
 constexpr uint32_t kPartSalt = 0x5bd1e995u;
+constexpr int GCH = 256;               // bucket slots scanned per gather chunk
 
 constexpr int PT_PLAN = 256;           // queries per planning block
 
@@ -100,6 +101,7 @@ __global__ void __launch_bounds__(WT) k_candidates_ws(WsArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ uint32_t s_ucount;
     __shared__ int s_item, s_last, s_wn[WW];
+    __shared__ GatherSmem<WT, GCH> s_gather;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int D = a.D, K = a.K, L = a.L, T = a.T;
     const int Dp = (D + 3) & ~3;
@@ -129,20 +131,11 @@ __global__ void __launch_bounds__(WT) k_candidates_ws(WsArgs a) {
         __syncthreads();
 
         // Gather this item's id partition from every matched bucket.
-        const int LT = L * T;
-        for (int e = warp; e < LT; e += WW) {
-            const int l = e / T, t = e - l * T;
-            const int32_t j = a.qbuckets[(int64_t)l * a.Q * T + (int64_t)q * T + t];
-            if (j < 0) continue;
-            const uint64_t g = a.boff[l] + (uint32_t)j;
-            const uint32_t st = a.starts[g], sz = a.sizes[g];
-            const uint32_t* src = a.ids + (int64_t)l * a.N + st;
-            for (uint32_t k = lane; k < sz; k += 32) {
-                const uint32_t id = __ldg(src + k);
-                if (P > 1 && mix32(id ^ kPartSalt) % P != p) continue;
-                set_insert(hset, W_SLOTS - 1, ulist, W_CAP, &s_ucount, id);
-            }
-        }
+        const BucketView bv{a.qbuckets, a.boff, a.starts, a.sizes, a.ids, a.N, L, T, a.Q};
+        gather_bucket_ids<WT, GCH>(bv, q, s_gather, [&](uint32_t id) {
+            if (P > 1 && mix32(id ^ kPartSalt) % P != p) return;
+            set_insert(hset, W_SLOTS - 1, ulist, W_CAP, &s_ucount, id);
+        });
         __syncthreads();
         uint32_t U = s_ucount;
         if (U > W_CAP) {   // the set overflowed: flag it, finish the protocol with no candidates

@@ -29,6 +29,7 @@ constexpr int CT = 128;
 constexpr int CW = CT / 32;
 constexpr int SM_SLOTS = 4096;
 constexpr int SM_CAP = SM_SLOTS / 2;
+constexpr int GCH = 256;   // bucket slots scanned per gather chunk
 
 __device__ __forceinline__ int ceil_log2_dev(int n) {
     int l = 0;
@@ -495,6 +496,7 @@ __global__ void __launch_bounds__(CT) k_candidates(CandArgs a) {
     __shared__ int s_ok;
     __shared__ unsigned long long s_off;
     __shared__ int s_wn[CW];
+    __shared__ GatherSmem<CT, GCH> s_gather;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int q = a.qlist ? a.qlist[blockIdx.x] : (int)blockIdx.x;
@@ -544,18 +546,11 @@ __global__ void __launch_bounds__(CT) k_candidates(CandArgs a) {
 
     // Gather every matched bucket's ids (duplicate probes included, as the
     // reference's candidate lists are) and deduplicate them.
-    const int LT = L * T;
     const uint32_t mask = cap - 1;
     const uint32_t lcap = C > (unsigned long long)SM_CAP ? (uint32_t)C : (uint32_t)SM_CAP;
-    for (int e = warp; e < LT; e += CW) {
-        const int l = e / T, t = e - l * T;
-        const int32_t j = a.qbuckets[(int64_t)l * a.Q * T + (int64_t)q * T + t];
-        if (j < 0) continue;
-        const uint64_t g = a.boff[l] + (uint32_t)j;
-        const uint32_t st = a.starts[g], sz = a.sizes[g];
-        const uint32_t* src = a.ids + (int64_t)l * a.N + st;
-        for (uint32_t k = lane; k < sz; k += 32) set_insert(hset, mask, ulist, lcap, &s_ucount, __ldg(src + k));
-    }
+    const BucketView bv{a.qbuckets, a.boff, a.starts, a.sizes, a.ids, a.N, L, T, a.Q};
+    gather_bucket_ids<CT, GCH>(bv, q, s_gather,
+                               [&](uint32_t id) { set_insert(hset, mask, ulist, lcap, &s_ucount, id); });
     __syncthreads();
     const uint32_t U = s_ucount;
 

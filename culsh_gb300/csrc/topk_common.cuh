@@ -73,4 +73,83 @@ __device__ __forceinline__ void set_insert(uint32_t* hset, uint32_t mask, uint32
     }
 }
 
+// Visits every candidate id of query q: the ids of every matched bucket over
+// all L tables and T probes, duplicates included (the reference's candidate
+// lists, cuLSH_SearchTables.cu:321-343). The L*T bucket slots are read in
+// chunks of CH by all NT threads at once (coalesced along t), the matched
+// buckets compacted in shared memory with their sizes, and the ids of the
+// chunk visited as one flattened range so that small and large buckets both
+// keep every thread busy. f(id) is called once per (bucket, id) occurrence by
+// some thread of the block; every thread must call this function.
+struct BucketView {
+    const int32_t* qbuckets;   // [L][Q*T]
+    const uint64_t* boff;      // [L+1]
+    const uint32_t* starts;
+    const uint32_t* sizes;
+    const uint32_t* ids;       // [L][N]
+    int64_t N;
+    int L, T, Q;
+};
+
+template <int NT, int CH>
+struct GatherSmem {
+    uint64_t base[CH];         // ids offset of each matched bucket
+    unsigned long long pre[CH];  // inclusive prefix of the bucket sizes
+    uint32_t n;
+};
+
+template <int NT, int CH, class F>
+__device__ __forceinline__ void gather_bucket_ids(const BucketView& v, int q, GatherSmem<NT, CH>& g, F f) {
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int T = v.T, LT = v.L * v.T;
+    for (int c0 = 0; c0 < LT; c0 += CH) {
+        if (tid == 0) g.n = 0;
+        __syncthreads();
+        const int c1 = min(LT, c0 + CH);
+        for (int e = c0 + tid; e < c1; e += NT) {
+            const int l = e / T, t = e - l * T;
+            const int32_t j = __ldg(v.qbuckets + (int64_t)l * v.Q * T + (int64_t)q * T + t);
+            if (j >= 0) {
+                const uint64_t gi = __ldg(v.boff + l) + (uint32_t)j;
+                const uint32_t st = __ldg(v.starts + gi), sz = __ldg(v.sizes + gi);
+                if (sz) {
+                    const uint32_t k = atomicAdd(&g.n, 1u);
+                    g.base[k] = (uint64_t)l * (uint64_t)v.N + st;
+                    g.pre[k] = sz;
+                }
+            }
+        }
+        __syncthreads();
+        const uint32_t n = g.n;
+        if (n == 0) continue;   // uniform: every thread read the same n
+        if (tid < 32) {
+            unsigned long long carry = 0;
+            for (uint32_t b = 0; b < n; b += 32) {
+                const uint32_t k = b + lane;
+                unsigned long long x = k < n ? g.pre[k] : 0ull;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+                    if (lane >= o) x += y;
+                }
+                if (k < n) g.pre[k] = x + carry;
+                carry += __shfl_sync(0xffffffffu, x, 31);
+            }
+        }
+        __syncthreads();
+        const unsigned long long total = g.pre[n - 1];
+        for (unsigned long long i = tid; i < total; i += NT) {
+            uint32_t lo = 0, hi = n - 1;   // first bucket whose inclusive prefix exceeds i
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (g.pre[mid] > i) hi = mid;
+                else lo = mid + 1;
+            }
+            const uint64_t off = i - (lo ? g.pre[lo - 1] : 0ull);
+            f(__ldg(v.ids + g.base[lo] + off));
+        }
+        __syncthreads();
+    }
+}
+
 }  // namespace culsh
