@@ -311,7 +311,8 @@ int upload_layout(culsh_index* ix, cudaStream_t st) {
     return CULSH_OK;
 }
 
-// Hash tables over the unique keys, load factor between 1/4 and 1/2.
+// Hash tables over the unique keys, load factor between 1/4 and 1/2, in
+// groups of kGroupSlots slots.
 int build_hash(culsh_index* ix, cudaStream_t st) {
     const int L = ix->L;
     ix->h_hoff.assign(L + 1, 0);
@@ -319,9 +320,9 @@ int build_hash(culsh_index* ix, cudaStream_t st) {
     int64_t maxB = 0;
     for (int l = 0; l < L; ++l) {
         const uint64_t B = ix->h_boff[l + 1] - ix->h_boff[l];
-        const uint64_t cap = next_pow2(std::max<uint64_t>(2 * B, 2));
-        ix->h_hmask[l] = (uint32_t)(cap - 1);
-        ix->h_hoff[l + 1] = ix->h_hoff[l] + cap;
+        const uint64_t groups = next_pow2(std::max<uint64_t>(2 * B, kGroupSlots)) / kGroupSlots;
+        ix->h_hmask[l] = (uint32_t)(groups - 1);
+        ix->h_hoff[l + 1] = ix->h_hoff[l] + groups * kGroupWords;
         maxB = std::max<int64_t>(maxB, (int64_t)B);
     }
     CU_TRY(ix->hoff.reserve(L + 1));

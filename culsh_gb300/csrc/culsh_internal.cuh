@@ -10,8 +10,13 @@
 //   boff     [L+1]   u64    bucket offsets: buckets of table l are [boff[l], boff[l+1])
 //   starts/sizes [sum B]    bucket start (within the table's ids) and size
 //   ukeys    [sum B][KW]    packed key of each bucket (column 0 in the most significant bits)
-//   hslots   [sum H]  u64   open-addressing hash (bucket index | fingerprint << 32)
-//   hoff     [L+1]   u64    slot offsets;  hmask[L] u32 power-of-two capacity - 1
+//   hslots   [sum H]  u64   bucketized open-addressing hash in 32-byte groups (one
+//                           DRAM sector, kGroupWords u64): word 0 holds four 16-bit
+//                           fingerprints (0xFFFF = empty), words 1-2 the four 32-bit
+//                           bucket indices; probing visits a group's slots in order,
+//                           then the next group
+//   hoff     [L+1]   u64    word offsets of each table's groups
+//   hmask    [L]     u32    power-of-two group count - 1
 #pragma once
 
 #include <cstdint>
@@ -24,6 +29,15 @@ constexpr int kMaxKW = 8;     // packed key words (256 bits)
 constexpr int kMaxT = 256;    // probes per table
 constexpr int kMaxK = 2048;   // neighbours per query
 constexpr unsigned long long kEmptySlot = ~0ull;
+constexpr int kGroupSlots = 4;   // hash slots per 32-byte group
+constexpr int kGroupWords = 4;   // u64 words per group
+constexpr uint32_t kEmptyFp = 0xFFFFu;
+
+// 16-bit slot fingerprint from the top bits of a key hash (never the empty mark).
+__host__ __device__ __forceinline__ uint32_t slot_fp(uint64_t hh) {
+    const uint32_t f = (uint32_t)(hh >> 48);
+    return f == kEmptyFp ? kEmptyFp - 1 : f;
+}
 
 // Device error flags (bit values OR-ed into an int in device memory).
 enum DevErr : int {

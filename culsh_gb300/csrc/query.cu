@@ -77,21 +77,25 @@ __device__ int32_t lookup_row(const LookupView& lv, int l, const float* row) {
         const int bits = __ldg(lv.fbits + c);
         if (bits) key_put(key, __ldg(lv.foff + c), bits, (uint32_t)(ci - lo));
     }
-    const uint32_t mask = __ldg(lv.hmask + l);
+    const uint32_t gmask = __ldg(lv.hmask + l);
     const uint64_t hh = key_hash64(key, KW);
     const uint32_t h = (uint32_t)hh;
-    const uint32_t fp = (uint32_t)(hh >> 32);
+    const uint32_t fp = slot_fp(hh);
     const unsigned long long* slots = lv.hslots + __ldg(lv.hoff + l);
     const uint64_t bo = __ldg(lv.boff + l);
-    for (uint32_t p = 0; p <= mask; ++p) {
-        const unsigned long long s = __ldg(slots + ((h + p) & mask));
-        if (s == kEmptySlot) return -1;
-        if ((uint32_t)(s >> 32) == fp) {
-            const uint32_t j = (uint32_t)s;
-            const uint32_t* uk = lv.ukeys + (bo + j) * KW;
-            bool eq = true;
-            for (int w = 0; w < KW; ++w) eq &= __ldg(uk + w) == key[w];
-            if (eq) return (int32_t)j;
+    for (uint32_t p = 0; p <= gmask; ++p) {
+        const unsigned long long* grp = slots + (uint64_t)((h + p) & gmask) * kGroupWords;
+        const unsigned long long fps = __ldg(grp);
+        for (int g = 0; g < kGroupSlots; ++g) {
+            const uint32_t f = (uint32_t)(fps >> (16 * g)) & 0xFFFFu;
+            if (f == kEmptyFp) return -1;
+            if (f == fp) {
+                const uint32_t j = __ldg(reinterpret_cast<const uint32_t*>(grp + 1) + g);
+                const uint32_t* uk = lv.ukeys + (bo + j) * KW;
+                bool eq = true;
+                for (int w = 0; w < KW; ++w) eq &= __ldg(uk + w) == key[w];
+                if (eq) return (int32_t)j;
+            }
         }
     }
     return -1;
@@ -199,17 +203,23 @@ __global__ void __launch_bounds__(128) k_probe(ProbeArgs a) {
 // procedure instead. The shift/expand enumeration then runs exactly as in
 // k_probe. A probe's key is the home key plus or minus one unit of each
 // perturbed column's field (packing is linear) in 128-bit modular arithmetic,
-// and column range validity is three bit masks. Slot loads are issued eight
+// and column range validity is three bit masks. Group loads are issued four
 // at a time before any is consumed. Per-thread state lives in a strided
 // slice of shared memory. Results equal k_probe's exactly.
 constexpr int PF = 128;
+constexpr int PCH = 2;   // probes whose group loads are in flight together
 typedef unsigned __int128 u128;
 
 __device__ __forceinline__ u128 field_term(int64_t f, int off) { return ((u128)(__int128)f) << off; }
 
+__device__ __forceinline__ int lowest_bit(uint32_t b) { return __ffs((int)b) - 1; }
+__device__ __forceinline__ int lowest_bit(uint64_t b) { return __ffsll((long long)b) - 1; }
+__device__ __forceinline__ int highest_bit(uint32_t b) { return 31 - __clz((int)b); }
+__device__ __forceinline__ int highest_bit(uint64_t b) { return 63 - __clzll((long long)b); }
+
 struct FastProbeCtx {
     u128 hkey;
-    uint64_t ok0, okUp, okDn, allM;
+    uint32_t ok0, okUp, okDn, allM;     // per-column range validity (M <= 32)
     const uint8_t* enc;                 // sorted delta i -> column | (up << 7); strided slice
     const unsigned long long* funit;    // this table's field units 2^foff (low, high)
 };
@@ -218,19 +228,21 @@ __device__ __forceinline__ u128 unit_of(const unsigned long long* funit, int m) 
     return ((u128)__ldg(funit + 2 * m + 1) << 64) | (u128)__ldg(funit + 2 * m);
 }
 
-// Key of a probe mask; returns false when a column leaves [cmin, cmax].
-__device__ __forceinline__ bool probe_key(const FastProbeCtx& c, uint64_t mask, u128& key) {
-    uint64_t up = 0, dn = 0;
-    for (uint64_t b = mask; b; b &= b - 1) {
-        const int e = c.enc[(__ffsll((long long)b) - 1) * PF];
-        if (e & 0x80) up |= 1ull << (e & 0x3f);
-        else dn |= 1ull << (e & 0x3f);
+// Key of a probe mask; returns false when a column leaves [cmin, cmax]. A
+// column perturbed both up and down keeps its home code.
+template <typename MaskT>
+__device__ __forceinline__ bool probe_key(const FastProbeCtx& c, MaskT mask, u128& key) {
+    uint32_t up = 0, dn = 0;
+    for (MaskT b = mask; b; b &= b - 1) {
+        const int e = c.enc[lowest_bit(b) * PF];
+        if (e & 0x80) up |= 1u << (e & 0x3f);
+        else dn |= 1u << (e & 0x3f);
     }
-    const uint64_t nu = up & ~dn, nd = dn & ~up;
+    const uint32_t nu = up & ~dn, nd = dn & ~up;
     if ((~(nu | nd) & c.allM & ~c.ok0) | (nu & ~c.okUp) | (nd & ~c.okDn)) return false;
     u128 k = c.hkey;
-    for (uint64_t b = nu; b; b &= b - 1) k += unit_of(c.funit, __ffsll((long long)b) - 1);
-    for (uint64_t b = nd; b; b &= b - 1) k -= unit_of(c.funit, __ffsll((long long)b) - 1);
+    for (uint32_t b = nu; b; b &= b - 1) k += unit_of(c.funit, lowest_bit(b));
+    for (uint32_t b = nd; b; b &= b - 1) k -= unit_of(c.funit, lowest_bit(b));
     key = k;
     return true;
 }
@@ -250,8 +262,10 @@ __device__ __forceinline__ bool key_matches(const uint32_t* uk, u128 k, int KW) 
 }
 
 // The reference's heap selection + heap sort over a strided slice (used
-// only when deltas tie or are NaN). perm[] receives delta indices.
-__device__ void heap_order_strided(const float* dl, int8_t* perm, int M2, int maxT) {
+// only when deltas tie or are NaN). val(i) is delta i; perm[] receives the
+// delta indices in ascending order.
+template <class V>
+__device__ void heap_order_strided(V val, int8_t* perm, int M2, int maxT) {
     const int levels = ceil_log2_dev(M2 + 1);
     auto sift = [&](int total) {
         int parent = 0;
@@ -264,12 +278,12 @@ __device__ void heap_order_strided(const float* dl, int8_t* perm, int M2, int ma
             } else if (right < total && pr == -1) {
                 mx = right;
             } else {
-                float best = dl[perm[parent * PF] * PF];
-                if (left < total && dl[pl * PF] > best) {
+                float best = val(perm[parent * PF]);
+                if (left < total && val(pl) > best) {
                     mx = left;
-                    best = dl[pl * PF];
+                    best = val(pl);
                 }
-                if (right < total && dl[pr * PF] > best) mx = right;
+                if (right < total && val(pr) > best) mx = right;
             }
             if (mx == parent) break;
             const int8_t t = perm[parent * PF];
@@ -281,7 +295,7 @@ __device__ void heap_order_strided(const float* dl, int8_t* perm, int M2, int ma
     for (int i = 0; i < maxT; ++i) perm[i * PF] = -1;
     for (int i = 0; i < M2; ++i) {
         const int p0 = perm[0];
-        if (p0 == -1 || dl[i * PF] < dl[p0 * PF]) {
+        if (p0 == -1 || val(i) < val(p0)) {
             perm[0] = (int8_t)i;
             sift(maxT);
         }
@@ -294,6 +308,12 @@ __device__ void heap_order_strided(const float* dl, int8_t* perm, int M2, int ma
     }
 }
 
+// Per-thread shared-memory slice of the fast kernel, in bytes per thread.
+template <typename MaskT>
+__host__ __device__ constexpr size_t probe_fast_bytes_per_thread(int M, int T) {
+    return sizeof(MaskT) * (size_t)T + sizeof(float) * (size_t)(M + T) + (size_t)(2 * M + M);
+}
+
 template <typename MaskT>
 __global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
     extern __shared__ __align__(16) unsigned char psm[];
@@ -301,18 +321,29 @@ __global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
     const int Q = a.Q, T = a.T, L = lv.L, M = lv.M, KW = lv.KW;
     const int tid = threadIdx.x;
     const int M2 = 2 * M;
-    // Strided per-thread slices: dl[2M] f32, cd[T] f32, comb[T] MaskT,
-    // enc[2M] u8 (sorted delta -> column | up << 7), ord[M] u8 (down order).
-    float* dl = reinterpret_cast<float*>(psm) + tid;
-    float* cd = dl + M2 * PF;
-    MaskT* comb = reinterpret_cast<MaskT*>(reinterpret_cast<float*>(psm) + (M2 + T) * PF) + tid;
-    uint8_t* enc = reinterpret_cast<uint8_t*>(reinterpret_cast<MaskT*>(
-                       reinterpret_cast<float*>(psm) + (M2 + T) * PF) + T * PF) + tid;
-    uint8_t* ord = enc + M2 * PF;
-    // sorted delta i (value of the column/direction it encodes)
+    // Strided per-thread slices (element i of a thread at [i * PF + tid]):
+    // comb[T] (MaskT), dn[M], cd[T] (f32), enc[2M] (sorted delta -> column |
+    // up << 7), ord[M] (u8). Each slice is placed from the block's base; the
+    // thread offset is added last, in units of the slice's own element type.
+    size_t off = 0;
+    MaskT* comb = reinterpret_cast<MaskT*>(psm + off) + tid;
+    off += sizeof(MaskT) * (size_t)T * PF;
+    float* dn = reinterpret_cast<float*>(psm + off) + tid;
+    float* cd = reinterpret_cast<float*>(psm + off) + M * PF + tid;
+    off += sizeof(float) * (size_t)(M + T) * PF;
+    uint8_t* enc = psm + off + tid;
+    uint8_t* ord = psm + off + M2 * PF + tid;
+    // value of delta i (i < M: down of column i; else up of column i - M,
+    // 1 - down as the reference computes it)
+    auto dv = [&](int i) {
+        const float d = dn[(i < M ? i : i - M) * PF];
+        return i < M ? d : __fsub_rn(1.0f, d);
+    };
+    // value of sorted delta i
     auto sv = [&](int i) {
         const int e = enc[i * PF];
-        return dl[((e & 0x3f) + ((e & 0x80) ? M : 0)) * PF];
+        const float d = dn[(e & 0x3f) * PF];
+        return (e & 0x80) ? __fsub_rn(1.0f, d) : d;
     };
     const int64_t idx = (int64_t)blockIdx.x * PF + tid;
     if (idx >= (int64_t)L * Q) return;   // no block-level synchronisation below
@@ -321,7 +352,7 @@ __global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
     FastProbeCtx c;
     c.hkey = 0;
     c.ok0 = c.okUp = c.okDn = 0;
-    c.allM = M >= 64 ? ~0ull : ((1ull << M) - 1);
+    c.allM = M >= 32 ? ~0u : ((1u << M) - 1);
     c.enc = enc;
     c.funit = lv.funit + 2 * l * M;
     bool distinct = true;
@@ -331,24 +362,23 @@ __global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
         const float f = floorf(v);
         const float down = __fsub_rn(v, f);
         const float up = __fsub_rn(1.0f, down);
-        dl[m * PF] = down;
-        dl[(m + M) * PF] = up;
+        dn[m * PF] = down;
         distinct &= (down == down) && (up == up);
         const int64_t lo = __ldg(lv.cmin + col), hi = __ldg(lv.cmax + col);
         const int64_t h = (f >= -1.0e15f && f <= 1.0e15f) ? (int64_t)f : (int64_t)1 << 50;
-        c.ok0 |= (uint64_t)(h >= lo && h <= hi) << m;
-        c.okUp |= (uint64_t)(h + 1 >= lo && h + 1 <= hi) << m;
-        c.okDn |= (uint64_t)(h - 1 >= lo && h - 1 <= hi) << m;
+        c.ok0 |= (uint32_t)(h >= lo && h <= hi) << m;
+        c.okUp |= (uint32_t)(h + 1 >= lo && h + 1 <= hi) << m;
+        c.okDn |= (uint32_t)(h - 1 >= lo && h - 1 <= hi) << m;
         c.hkey += field_term(h - lo, __ldg(lv.foff + col));
     }
 
     if (T > 1) {
         // Rank the downs (ties or NaN fall back to the heap procedure).
         for (int i = 0; i < M && distinct; ++i) {
-            const float di = dl[i * PF];
+            const float di = dn[i * PF];
             int r = 0;
             for (int j = 0; j < M; ++j) {
-                const float dj = dl[j * PF];
+                const float dj = dn[j * PF];
                 r += dj < di;
                 distinct &= (j == i) | (dj != di);
             }
@@ -357,13 +387,13 @@ __global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
         // Ups in reverse down order must be strictly increasing, then merge.
         if (distinct) {
             for (int k = 1; k < M && distinct; ++k)
-                distinct &= dl[(ord[(M - k) * PF] + M) * PF] < dl[(ord[(M - 1 - k) * PF] + M) * PF];
+                distinct &= dv(ord[(M - k) * PF] + M) < dv(ord[(M - 1 - k) * PF] + M);
         }
         if (distinct) {
             int id = 0, iu = M - 1;
             for (int o = 0; o < M2; ++o) {
-                const float vd = id < M ? dl[ord[id * PF] * PF] : FLT_MAX;
-                const float vu = iu >= 0 ? dl[(ord[iu * PF] + M) * PF] : FLT_MAX;
+                const float vd = id < M ? dn[ord[id * PF] * PF] : FLT_MAX;
+                const float vu = iu >= 0 ? dv(ord[iu * PF] + M) : FLT_MAX;
                 const bool take_down = iu < 0 || (id < M && vd < vu);
                 if (id < M && iu >= 0 && vd == vu) {
                     distinct = false;
@@ -377,7 +407,7 @@ __global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
         }
         if (!distinct) {
             int8_t* perm = reinterpret_cast<int8_t*>(enc);
-            heap_order_strided(dl, perm, M2, M2);
+            heap_order_strided(dv, perm, M2, M2);
             for (int i = 0; i < M2; ++i) {
                 const int pm = perm[i * PF];
                 enc[i * PF] = (uint8_t)((pm % M) | (pm >= M ? 0x80 : 0));
@@ -387,24 +417,25 @@ __global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
         cd[0] = sv(0);
     }
 
-    // Probes: enumerate (cuLSH_Kernels.cu:216-255) in groups of eight, issue
-    // the group's slot loads, then resolve them.
-    const uint32_t hmask = __ldg(lv.hmask + l);
+    // Probes: enumerate (cuLSH_Kernels.cu:216-255) PCH at a time, issue the
+    // group loads of the batch together, then resolve each probe: walk its
+    // group's fingerprints (registers) until an empty slot, verifying the
+    // stored key on a fingerprint match.
+    const uint32_t gmask = __ldg(lv.hmask + l);
     const unsigned long long* slots = lv.hslots + __ldg(lv.hoff + l);
     const uint64_t bo = __ldg(lv.boff + l);
     int32_t* qb = a.qbuckets + (int64_t)l * Q * T + (int64_t)q * T;
     unsigned long long cnu = 0;
     int size = 1;
-    constexpr int CH = 8;
-    for (int t0 = 0; t0 < T; t0 += CH) {
-        MaskT pm[CH];
-        unsigned long long slv[CH];
-        uint32_t hsv[CH], fpv[CH], valid = 0;
+    for (int t0 = 0; t0 < T; t0 += PCH) {
+        MaskT pm[PCH];
+        unsigned long long fw[PCH];   // fingerprint word of each probe's group
+        uint32_t hsv[PCH], fpv[PCH], valid = 0;
 #pragma unroll
-        for (int j = 0; j < CH; ++j) {
+        for (int j = 0; j < PCH; ++j) {
             const int t = t0 + j;
             pm[j] = 0;
-            slv[j] = kEmptySlot;
+            fw[j] = ~0ull;
             hsv[j] = fpv[j] = 0;
             if (t < T) {
                 MaskT probe = 0;
@@ -419,7 +450,7 @@ __global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
                         }
                     }
                     probe = comb[mi * PF];
-                    const int top = 63 - __clzll((long long)(uint64_t)probe);
+                    const int top = highest_bit(probe);
                     if (top < M2 - 1) {
                         const MaskT p1 = probe | ((MaskT)1 << (top + 1));
                         const float m1 = __fadd_rn(mn, sv(top + 1));
@@ -434,32 +465,41 @@ __global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
                 u128 k;
                 if (probe_key(c, probe, k)) {
                     const uint64_t hh = key_hash128(k, KW);
-                    hsv[j] = (uint32_t)hh & hmask;
-                    fpv[j] = (uint32_t)(hh >> 32);
-                    slv[j] = __ldg(slots + hsv[j]);
+                    hsv[j] = (uint32_t)hh & gmask;
+                    fpv[j] = slot_fp(hh);
+                    fw[j] = __ldg(slots + (uint64_t)hsv[j] * kGroupWords);
                     valid |= 1u << j;
                 }
             }
         }
 #pragma unroll
-        for (int j = 0; j < CH; ++j) {
+        for (int j = 0; j < PCH; ++j) {
             const int t = t0 + j;
             if (t >= T) break;
             int32_t res = -1;
             if (valid & (1u << j)) {
-                unsigned long long sl = slv[j];
+                unsigned long long w = fw[j];
                 uint32_t h = hsv[j];
-                for (uint32_t p = 0; p <= hmask && sl != kEmptySlot; ++p) {
-                    if ((uint32_t)(sl >> 32) == fpv[j]) {
-                        u128 k;
-                        probe_key(c, pm[j], k);
-                        if (key_matches(lv.ukeys + (bo + (uint32_t)sl) * KW, k, KW)) {
-                            res = (int32_t)(uint32_t)sl;
-                            break;
+                bool done = false;
+                for (uint32_t p = 0; p <= gmask && !done; ++p) {
+                    const unsigned long long* grp = slots + (uint64_t)h * kGroupWords;
+#pragma unroll
+                    for (int e = 0; e < kGroupSlots && !done; ++e) {
+                        const uint32_t f = (uint32_t)(w >> (16 * e)) & 0xFFFFu;
+                        if (f == kEmptyFp) {
+                            done = true;
+                        } else if (f == fpv[j]) {
+                            const uint32_t bj = __ldg(reinterpret_cast<const uint32_t*>(grp + 1) + e);
+                            u128 k;
+                            probe_key(c, pm[j], k);
+                            if (key_matches(lv.ukeys + (bo + bj) * KW, k, KW)) {
+                                res = (int32_t)bj;
+                                done = true;
+                            }
                         }
                     }
-                    h = (h + 1) & hmask;
-                    sl = __ldg(slots + h);
+                    h = (h + 1) & gmask;
+                    if (!done) w = __ldg(slots + (uint64_t)h * kGroupWords);
                 }
             }
             qb[t] = res;
@@ -471,8 +511,7 @@ __global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
 
 template <typename MaskT>
 cudaError_t launch_probe_fast_t(const ProbeArgs& a, cudaStream_t st) {
-    const int M2 = 2 * a.lv.M, T = a.T;
-    const size_t smem = (size_t)PF * ((M2 + T) * sizeof(float) + T * sizeof(MaskT) + M2 + a.lv.M);
+    const size_t smem = (size_t)PF * probe_fast_bytes_per_thread<MaskT>(a.lv.M, a.T);
     static size_t configured = 0;
     if (smem > 48 * 1024 && smem > configured) {
         cudaError_t e =

@@ -320,13 +320,32 @@ __global__ void k_hash_build(const uint64_t* __restrict__ boff, const uint32_t* 
     const uint32_t* key = ukeys + (boff[l] + j) * KW;
     uint32_t k[kMaxKW];
     for (int w = 0; w < KW; ++w) k[w] = key[w];
-    const uint32_t mask = hmask[l];
+    const uint32_t gmask = hmask[l];
     const uint64_t hh = key_hash64(k, KW);
     const uint32_t h = (uint32_t)hh;
-    const unsigned long long val = (hh & 0xffffffff00000000ull) | (uint32_t)j;
+    const uint32_t fp = slot_fp(hh);
     unsigned long long* slots = hslots + hoff[l];
-    for (uint32_t p = 0; p <= mask; ++p) {
-        if (atomicCAS(&slots[(h + p) & mask], kEmptySlot, val) == kEmptySlot) return;
+    // Claim the first empty slot in probe order (a group's slots in order,
+    // then the next group), then store the bucket index beside it. Lookups
+    // stop at the first empty slot they meet, which can only lie past every
+    // key inserted along the same path.
+    for (uint32_t p = 0; p <= gmask; ++p) {
+        unsigned long long* grp = slots + (uint64_t)((h + p) & gmask) * kGroupWords;
+        unsigned long long cur = *reinterpret_cast<volatile unsigned long long*>(grp);
+        // One 64-bit CAS per attempt on the group's fingerprint word; each
+        // failure means another insert took a slot, so at most four tries.
+        for (int tries = 0; tries <= kGroupSlots; ++tries) {
+            int e = 0;
+            while (e < kGroupSlots && ((cur >> (16 * e)) & 0xFFFFu) != kEmptyFp) ++e;
+            if (e == kGroupSlots) break;   // group full: next group
+            const unsigned long long nw = (cur & ~(0xFFFFull << (16 * e))) | ((unsigned long long)fp << (16 * e));
+            const unsigned long long old = atomicCAS(grp, cur, nw);
+            if (old == cur) {
+                reinterpret_cast<uint32_t*>(grp + 1)[e] = (uint32_t)j;
+                return;
+            }
+            cur = old;
+        }
     }
     atomicOr(err, kErrHashFull);
 }
