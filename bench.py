@@ -55,6 +55,7 @@ def parse_args(argv=None):
     p.add_argument("--recall-sample", type=int, default=200)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-autotune", action="store_true", help="search with the default tuning")
     return p.parse_args(argv)
 
 
@@ -270,11 +271,14 @@ def run_culsh(args):
 
     X, Qm, A, b, d, name = workload(args)
     N, D, L, M, Q, K, T = d["N"], d["D"], d["L"], d["M"], d["Q"], d["K"], d["T"]
-    stream = torch.cuda.current_stream(dev)
+    # A dedicated stream: the search replays its captured CUDA graph there
+    # (graphs are not used on the legacy default stream).
+    stream = torch.cuda.Stream(dev)
     sp = stream.cuda_stream
 
     # Index build (device-resident dataset, borrowed by the index).
     Xt = torch.from_numpy(X).to(dev)
+    torch.cuda.synchronize()   # the library works on its own stream
     ht = culsh.HashTables()
     ht.reset(N, D, L, M, d["W"], A=A, b=b)
     ht.index_device(Xt.data_ptr(), sp)
@@ -290,11 +294,15 @@ def run_culsh(args):
     build_profile = ht.profile()
 
     qt = torch.from_numpy(Qm).to(dev)
+    torch.cuda.synchronize()
     ids = torch.empty((Q, K), dtype=torch.int32, device=dev)
     dists = torch.empty((Q, K), dtype=torch.float32, device=dev)
     st = culsh.SearchTables()
     st.reset(ht, K, T)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    tuning = None
+    if not args.no_autotune:   # untimed: picks tiles, probe batch depth, candidate kernel shape
+        tuning = st.autotune(qt.data_ptr(), Q, ids.data_ptr(), dists.data_ptr(), sp)
 
     for _ in range(args.warmup):
         st.search_device(qt.data_ptr(), Q, ids.data_ptr(), dists.data_ptr(), sp)
@@ -315,7 +323,8 @@ def run_culsh(args):
         dist.barrier()
     torch.cuda.synchronize()
     for i in range(args.steps):
-        flush.fill_(i & 0xFF)
+        with torch.cuda.stream(stream):
+            flush.fill_(i & 0xFF)
         e0, e1 = events[i]
         e0.record(stream)
         st.search_device(qt.data_ptr(), Q, ids.data_ptr(), dists.data_ptr(), sp)
@@ -388,7 +397,9 @@ def run_culsh(args):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded generator of the workload's distribution)",
                 "config": {"workload": name, **d, "form": "fp32 (canonical order, bit-exact)",
-                           "l2": "flushed by a 256 MB write between timed steps", "parallelism": "replicas"},
+                           "l2": "flushed by a 256 MB write between timed steps", "parallelism": "replicas",
+                           "search": "captured CUDA graph, persistent work-stealing candidate kernel",
+                           "tuning": tuning},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
                 "clocks": clk, "index_build_ms": round(statistics.median(build_ms), 3),
                 "index_build_stages_ms": {k: (round(v, 4) if isinstance(v, float) else v)

@@ -54,7 +54,13 @@ class _Times(ctypes.Structure):
 class _Profile(ctypes.Structure):
     _fields_ = [("project_ms", ctypes.c_float), ("probe_ms", ctypes.c_float), ("candidates_ms", ctypes.c_float),
                 ("launches", ctypes.c_int), ("deferred_queries", ctypes.c_int), ("key_words", ctypes.c_int),
-                ("candidates_mode", ctypes.c_int)]
+                ("candidates_mode", ctypes.c_int), ("graph_mode", ctypes.c_int)]
+
+
+class _Tuning(ctypes.Structure):
+    _fields_ = [("proj_tile", ctypes.c_int), ("probe_batch", ctypes.c_int), ("candidates_mode", ctypes.c_int),
+                ("ws_threads", ctypes.c_int), ("ws_blocks_per_sm", ctypes.c_int), ("ws_chunk", ctypes.c_int),
+                ("search_ms", ctypes.c_float), ("configs_tried", ctypes.c_int)]
 
 
 class _IndexProfile(ctypes.Structure):
@@ -107,6 +113,10 @@ ABI = {
     "culsh_search_times": (None, [_P, ctypes.POINTER(_Times)]),
     "culsh_search_profile_get": (_I, [_P, ctypes.POINTER(_Profile)]),
     "culsh_search_run_device_noalloc": (_I, [_P, _P, _I, _P, _P, _P]),
+    "culsh_search_autotune": (_I, [_P, _P, _I, _P, _P, _P, ctypes.POINTER(_Tuning)]),
+    "culsh_search_get_tuning": (_I, [_P, ctypes.POINTER(_Tuning)]),
+    "culsh_search_set_tuning": (_I, [_P, ctypes.POINTER(_Tuning)]),
+    "culsh_search_set_graphs": (_I, [_P, _I]),
 }
 
 _lib = None
@@ -281,6 +291,34 @@ class SearchTables:
         _check(lib().culsh_search_run_device(self._h, ctypes.c_void_p(d_queries), int(Q), ctypes.c_void_p(d_ids),
                                              ctypes.c_void_p(d_dists), ctypes.c_void_p(stream or None)))
         self.Q = int(Q)
+
+    def autotune(self, d_queries: int, Q: int, d_ids: int, d_dists: int, stream: int = 0):
+        """Times the search over its tuning space on these device queries and
+        keeps the fastest configuration; returns it as a dict."""
+        t = _Tuning()
+        _check(lib().culsh_search_autotune(self._h, ctypes.c_void_p(d_queries), int(Q), ctypes.c_void_p(d_ids),
+                                           ctypes.c_void_p(d_dists), ctypes.c_void_p(stream or None), ctypes.byref(t)))
+        self.Q = int(Q)
+        return {n: getattr(t, n) for n, _ in _Tuning._fields_}
+
+    def get_tuning(self):
+        t = _Tuning()
+        _check(lib().culsh_search_get_tuning(self._h, ctypes.byref(t)))
+        return {n: getattr(t, n) for n, _ in _Tuning._fields_}
+
+    def set_tuning(self, **kw):
+        """Sets tuning fields (proj_tile, probe_batch, candidates_mode,
+        ws_threads, ws_blocks_per_sm, ws_chunk); others keep their value."""
+        t = _Tuning()
+        _check(lib().culsh_search_get_tuning(self._h, ctypes.byref(t)))
+        for k, v in kw.items():
+            if k not in dict(_Tuning._fields_):
+                raise KeyError(k)
+            setattr(t, k, v)
+        _check(lib().culsh_search_set_tuning(self._h, ctypes.byref(t)))
+
+    def set_graphs(self, enabled: bool):
+        _check(lib().culsh_search_set_graphs(self._h, 1 if enabled else 0))
 
     def getKnnIds(self):
         a = _copy_out(lib().culsh_search_knn_ids(self._h), self.Q * self.K, np.int32)

@@ -27,8 +27,6 @@
 namespace culsh {
 namespace {
 
-constexpr int WT = 128;                // threads per CTA
-constexpr int WW = WT / 32;
 constexpr int W_SLOTS = 4096;          // shared hash slots per item
 constexpr int W_CAP = W_SLOTS / 2;     // distinct ids per item
 constexpr uint32_t kPartSalt = 0x5bd1e995u;
@@ -97,7 +95,11 @@ __global__ void __launch_bounds__(PT_PLAN) k_plan_items(WsArgs a) {
     }
 }
 
+// WT threads per item: WT / 32 warps each keep a sorted top-K list over a
+// strided share of the item's candidates (tuned: 64, 128 or 256).
+template <int WT>
 __global__ void __launch_bounds__(WT) k_candidates_ws(WsArgs a) {
+    constexpr int WW = WT / 32;
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ uint32_t s_ucount;
     __shared__ int s_item, s_last, s_wn[WW];
@@ -278,9 +280,9 @@ __global__ void __launch_bounds__(WT) k_candidates_ws(WsArgs a) {
 
 }  // namespace
 
-size_t ws_smem_bytes(int D, int K) {
+size_t ws_smem_bytes(int D, int K, int wt) {
     return sizeof(float) * (size_t)((D + 3) & ~3) + sizeof(uint32_t) * (W_SLOTS + W_CAP) +
-           (size_t)WW * K * (sizeof(float) + sizeof(uint32_t));
+           (size_t)(wt / 32) * K * (sizeof(float) + sizeof(uint32_t));
 }
 
 cudaError_t launch_plan_items(const WsArgs& a, cudaStream_t st) {
@@ -289,24 +291,44 @@ cudaError_t launch_plan_items(const WsArgs& a, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_candidates_ws(const WsArgs& a, int grid, cudaStream_t st) {
-    const size_t smem = ws_smem_bytes(a.D, a.K);
+namespace {
+template <int WT>
+cudaError_t launch_ws_v(const WsArgs& a, int grid, cudaStream_t st) {
+    const size_t smem = ws_smem_bytes(a.D, a.K, WT);
     static size_t configured = 0;
     if (smem > 48 * 1024 && smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_candidates_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(k_candidates_ws<WT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         configured = smem;
     }
-    k_candidates_ws<<<grid, WT, smem, st>>>(a);
+    k_candidates_ws<WT><<<grid, WT, smem, st>>>(a);
     return cudaGetLastError();
 }
 
-int ws_blocks_per_sm(int D, int K) {
+template <int WT>
+int ws_bps_v(int D, int K) {
     int n = 0;
-    const size_t smem = ws_smem_bytes(D, K);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_candidates_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_candidates_ws, WT, smem) != cudaSuccess) n = 1;
+    const size_t smem = ws_smem_bytes(D, K, WT);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_candidates_ws<WT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_candidates_ws<WT>, WT, smem) != cudaSuccess) n = 1;
     return n > 0 ? n : 1;
+}
+}  // namespace
+
+cudaError_t launch_candidates_ws(const WsArgs& a, int grid, cudaStream_t st) {
+    switch (a.wt) {
+        case 64: return launch_ws_v<64>(a, grid, st);
+        case 256: return launch_ws_v<256>(a, grid, st);
+        default: return launch_ws_v<128>(a, grid, st);
+    }
+}
+
+int ws_blocks_per_sm(int D, int K, int wt) {
+    switch (wt) {
+        case 64: return ws_bps_v<64>(D, K);
+        case 256: return ws_bps_v<256>(D, K);
+        default: return ws_bps_v<128>(D, K);
+    }
 }
 
 }  // namespace culsh

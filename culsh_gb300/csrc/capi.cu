@@ -173,6 +173,17 @@ struct culsh_index {
     const float* dev_x() const { return x_borrow ? x_borrow : (X.p ? X.p : nullptr); }
 };
 
+// Tuning knobs of the search path (culsh_search_autotune picks them).
+struct SearchTune {
+    int proj_tile = 0;     // query projection tiling (launch_project_fp32)
+    int probe_pch = 2;     // probes whose hash-group loads overlap (1, 2, 4)
+    int cand_ws = 1;       // 1: work-stealing candidate kernel, 0: one block per query
+    int ws_wt = 128;       // threads per work item (64, 128, 256)
+    int ws_bps = 0;        // resident work-stealing CTAs per SM (0: occupancy limit)
+    int ws_chunk = 1024;   // non-unique candidates per id partition
+};
+constexpr size_t kPlanBytes = 1024;   // room for the graph key (checked below)
+
 struct culsh_search {
     culsh_index* ix = nullptr;
     int K = 0, T = 1, Q = 0, L = 0;
@@ -194,13 +205,19 @@ struct culsh_search {
     DevBuf<uint8_t> item_p;
     DevBuf<float> part_d;
     DevBuf<uint32_t> part_i;
-    int ws_grid = 0, ws_D = 0, ws_K = 0, ws_used = 0, ws_overflow = 0;
+    int sms = 0, ws_used = 0, ws_overflow = 0;
+    SearchTune tune;
+    bool use_graphs = true;
+    cudaGraphExec_t gexec = nullptr;     // cached search graph and the plan it was captured from
+    unsigned char gplan[kPlanBytes] = {};
+    int glaunches = 0, graph_mode = 0;
     PinBuf<int32_t> h_ids, h_qb;
     PinBuf<float> h_d;
     PinBuf<unsigned long long> h_stats;
     bool qb_host_valid = false;
 
     ~culsh_search() {
+        if (gexec) cudaGraphExecDestroy(gexec);
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
         if (stream) cudaStreamDestroy(stream);
@@ -666,17 +683,13 @@ size_t arena_cap_words() {
     return ~size_t(0);
 }
 
-// The candidate stage runs as the persistent work-stealing kernel unless
-// CULSH_CANDIDATES_PER_QUERY is set (one block per query; the tests run both).
-int use_work_stealing() { return getenv("CULSH_CANDIDATES_PER_QUERY") == nullptr; }
+// CULSH_CANDIDATES_PER_QUERY forces the per-query candidate kernel (one
+// block per query; the tests run both forms).
+int forced_per_query() { return getenv("CULSH_CANDIDATES_PER_QUERY") != nullptr; }
 
 constexpr int kWsPartitions = 64;              // most partitions of one query
-constexpr unsigned long long kWsChunk = 1024;  // non-unique candidates per partition
 constexpr size_t kWsPartialBytes = size_t(64) << 20;
 
-// Sizes the work-stealing buffers and fills the kernel arguments. stats[4]
-// holds the item counter (low word) and the overflow flag (high word),
-// stats[5] the number of items.
 // CULSH_WS_PARTITIONS (1..64) and CULSH_WS_ITEMS lower the partition count
 // and the item capacity; the tests use them to reach both overflow re-runs.
 int env_int(const char* name, int lo, int hi, int dflt) {
@@ -686,68 +699,32 @@ int env_int(const char* name, int lo, int hi, int dflt) {
     return v < lo ? lo : (v > hi ? hi : (int)v);
 }
 
-int prepare_ws(culsh_search* s, const CandArgs& ca, WsArgs* w, cudaStream_t st) {
-    (void)st;
-    const int Q = ca.Q, K = ca.K;
-    const int pmax = env_int("CULSH_WS_PARTITIONS", 1, kWsPartitions, kWsPartitions);
-    const size_t per_item = (size_t)K * 8 + 4 + 4 + 1;
-    size_t cap = std::max<size_t>((size_t)Q * 2, kWsPartialBytes / per_item);
-    cap = std::min(cap, (size_t)Q * pmax);
-    cap = std::min<size_t>(cap, (size_t)env_int("CULSH_WS_ITEMS", 1, 0x7fffffff, 0x7fffffff));
-    CU_TRY(s->q_items.reserve(Q));
-    CU_TRY(s->q_off.reserve(Q));
-    CU_TRY(s->q_done.reserve(Q));
-    CU_TRY(s->item_q.reserve(cap));
-    CU_TRY(s->item_p.reserve(cap));
-    CU_TRY(s->part_n.reserve(cap));
-    CU_TRY(s->part_d.reserve(cap * K));
-    CU_TRY(s->part_i.reserve(cap * K));
-    if (!s->ws_grid || s->ws_D != ca.D || s->ws_K != K) {
-        int dev = 0, sms = 0;
-        CU_TRY(cudaGetDevice(&dev));
-        CU_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        s->ws_grid = sms * ws_blocks_per_sm(ca.D, K);
-        s->ws_D = ca.D;
-        s->ws_K = K;
-    }
-    WsArgs& a = *w;
-    a.X = ca.X;
-    a.N = ca.N;
-    a.D = ca.D;
-    a.L = ca.L;
-    a.T = ca.T;
-    a.Q = Q;
-    a.K = K;
-    a.queries = ca.queries;
-    a.qbuckets = ca.qbuckets;
-    a.boff = ca.boff;
-    a.starts = ca.starts;
-    a.sizes = ca.sizes;
-    a.ids = ca.ids;
-    a.cnu = ca.cnu;
-    a.out_ids = ca.out_ids;
-    a.out_d = ca.out_d;
-    a.cu = ca.cu;
-    a.totals = ca.totals;
-    a.pmax = pmax;
-    a.chunk = kWsChunk;
-    a.q_items = s->q_items.p;
-    a.q_off = s->q_off.p;
-    a.q_done = s->q_done.p;
-    a.item_q = s->item_q.p;
-    a.item_p = s->item_p.p;
-    a.part_n = s->part_n.p;
-    a.part_d = s->part_d.p;
-    a.part_i = s->part_i.p;
-    a.item_cap = (unsigned int)cap;
-    a.next_item = reinterpret_cast<unsigned int*>(s->stats.p + 4);
-    a.overflow = reinterpret_cast<unsigned int*>(s->stats.p + 4) + 1;
-    a.n_items = reinterpret_cast<unsigned int*>(s->stats.p + 5);
-    return CULSH_OK;
-}
+// Everything the enqueued search work depends on: kernel arguments, launch
+// shapes, buffers, events. Built zero-filled and compared bytewise, it is
+// the key of the cached CUDA graph.
+struct SearchPlan {
+    const float* dQ;
+    int Q, D, LM, proj_tile;
+    float W;
+    const float* A;
+    const float* b;
+    float* vals;
+    ProbeArgs pa;
+    int probe_generic;
+    int use_ws, ws_grid;
+    CandArgs ca;
+    WsArgs wa;
+    unsigned long long* stats;
+    unsigned long long* h_stats;
+    unsigned long long* cnu;
+    cudaEvent_t ev[4];
+};
 
-// The query path on device buffers (cuLSH_SearchTables.cu:197-463).
-int search_device(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* d_d, cudaStream_t st) {
+static_assert(sizeof(SearchPlan) <= kPlanBytes, "graph key buffer too small");
+
+// Sizes every buffer of a search of Q queries and fills the plan. Allocates
+// (when buffers grow) but launches nothing.
+int plan_search(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* d_d, SearchPlan* out) {
     culsh_index* ix = s->ix;
     const int L = ix->L, M = ix->M, D = ix->D, K = s->K, T = s->T, LM = L * M;
     const float* dX = ix->dev_x();
@@ -767,26 +744,28 @@ int search_device(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float
         s->arena.release();
         CU_TRY(s->arena.reserve(init_words));
     }
-    CU_TRY(cudaMemsetAsync(s->cnu.p, 0, 8 * (size_t)Q, st));
-    CU_TRY(cudaMemsetAsync(s->stats.p, 0, 8 * 8, st));
-    s->launches = 0;
-    s->deferred_queries = 0;
-    s->host_copy_timed = false;
-    CU_TRY(cudaEventRecord(s->ev[0], st));
-    CU_TRY(launch_project_fp32(dQ, Q, D, ix->dA.p, ix->db.p, LM, ix->W, nullptr, s->vals.p, nullptr, nullptr, nullptr, st));
-    CU_TRY(cudaEventRecord(s->ev[1], st));
-    ProbeArgs pa;
-    pa.vals = s->vals.p;
-    pa.Q = Q;
-    pa.T = T;
-    pa.lv = lookup_view(ix);
-    pa.qbuckets = s->qb.p;
-    pa.cnu = s->cnu.p;
-    pa.small_codes = small_codes(ix);
-    CU_TRY(launch_probe(pa, st));
-    CU_TRY(cudaEventRecord(s->ev[2], st));
-    s->launches += 2;
-    CandArgs ca;
+    const SearchTune& tu = s->tune;
+    SearchPlan& P = *out;
+    std::memset(&P, 0, sizeof(P));
+    P.dQ = dQ;
+    P.Q = Q;
+    P.D = D;
+    P.LM = LM;
+    P.proj_tile = tu.proj_tile;
+    P.W = ix->W;
+    P.A = ix->dA.p;
+    P.b = ix->db.p;
+    P.vals = s->vals.p;
+    P.pa.vals = s->vals.p;
+    P.pa.Q = Q;
+    P.pa.T = T;
+    P.pa.lv = lookup_view(ix);
+    P.pa.qbuckets = s->qb.p;
+    P.pa.cnu = s->cnu.p;
+    P.pa.small_codes = small_codes(ix);
+    P.pa.pch = tu.probe_pch;
+    P.probe_generic = getenv("CULSH_PROBE_GENERIC") != nullptr;
+    CandArgs& ca = P.ca;
     ca.X = dX;
     ca.N = ix->N;
     ca.D = D;
@@ -812,22 +791,161 @@ int search_device(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float
     ca.n_deferred = reinterpret_cast<unsigned int*>(s->stats.p + 3);
     ca.qlist = nullptr;
     ca.nq = Q;
-    s->ws_used = use_work_stealing();
-    s->ws_overflow = 0;
-    if (s->ws_used) {
-        WsArgs wa;
-        TRY(prepare_ws(s, ca, &wa, st));
-        CU_TRY(launch_plan_items(wa, st));
-        CU_TRY(launch_candidates_ws(wa, s->ws_grid, st));
-        s->launches += 2;
-    } else {
-        CU_TRY(launch_candidates(ca, st));
-        s->launches += 1;
+    P.use_ws = tu.cand_ws && !forced_per_query();
+    if (P.use_ws) {
+        // Work-stealing buffers. stats[4] holds the item counter (low word)
+        // and the overflow flag (high word), stats[5] the number of items.
+        const int pmax = env_int("CULSH_WS_PARTITIONS", 1, kWsPartitions, kWsPartitions);
+        const size_t per_item = (size_t)K * 8 + 4 + 4 + 1;
+        size_t cap = std::max<size_t>((size_t)Q * 2, kWsPartialBytes / per_item);
+        cap = std::min(cap, (size_t)Q * pmax);
+        cap = std::min<size_t>(cap, (size_t)env_int("CULSH_WS_ITEMS", 1, 0x7fffffff, 0x7fffffff));
+        CU_TRY(s->q_items.reserve(Q));
+        CU_TRY(s->q_off.reserve(Q));
+        CU_TRY(s->q_done.reserve(Q));
+        CU_TRY(s->item_q.reserve(cap));
+        CU_TRY(s->item_p.reserve(cap));
+        CU_TRY(s->part_n.reserve(cap));
+        CU_TRY(s->part_d.reserve(cap * K));
+        CU_TRY(s->part_i.reserve(cap * K));
+        if (s->sms == 0) {
+            int dev = 0;
+            CU_TRY(cudaGetDevice(&dev));
+            CU_TRY(cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, dev));
+        }
+        const int occ = ws_blocks_per_sm(D, K, tu.ws_wt);
+        const int bps = tu.ws_bps > 0 ? std::min(tu.ws_bps, occ) : occ;
+        P.ws_grid = s->sms * bps;
+        WsArgs& a = P.wa;
+        a.X = ca.X;
+        a.N = ca.N;
+        a.D = D;
+        a.L = L;
+        a.T = T;
+        a.Q = Q;
+        a.K = K;
+        a.queries = dQ;
+        a.qbuckets = ca.qbuckets;
+        a.boff = ca.boff;
+        a.starts = ca.starts;
+        a.sizes = ca.sizes;
+        a.ids = ca.ids;
+        a.cnu = ca.cnu;
+        a.out_ids = d_ids;
+        a.out_d = d_d;
+        a.cu = ca.cu;
+        a.totals = ca.totals;
+        a.pmax = pmax;
+        a.chunk = (unsigned long long)tu.ws_chunk;
+        a.q_items = s->q_items.p;
+        a.q_off = s->q_off.p;
+        a.q_done = s->q_done.p;
+        a.item_q = s->item_q.p;
+        a.item_p = s->item_p.p;
+        a.part_n = s->part_n.p;
+        a.part_d = s->part_d.p;
+        a.part_i = s->part_i.p;
+        a.item_cap = (unsigned int)cap;
+        a.next_item = reinterpret_cast<unsigned int*>(s->stats.p + 4);
+        a.overflow = reinterpret_cast<unsigned int*>(s->stats.p + 4) + 1;
+        a.n_items = reinterpret_cast<unsigned int*>(s->stats.p + 5);
+        a.wt = tu.ws_wt;
     }
-    CU_TRY(cudaEventRecord(s->ev[3], st));
-    CU_TRY(cudaMemcpyAsync(s->h_stats.p, s->stats.p, 8 * 8, cudaMemcpyDeviceToHost, st));
+    P.stats = s->stats.p;
+    P.h_stats = s->h_stats.p;
+    P.cnu = s->cnu.p;
+    for (int i = 0; i < 4; ++i) P.ev[i] = s->ev[i];
+    return CULSH_OK;
+}
+
+// Enqueues one search: no allocation, no host synchronisation, so that it
+// can be captured into a CUDA graph. Returns the number of kernels launched.
+// Inside a capture the stage events become event-record nodes (external
+// events); outside one they are ordinary records.
+int enqueue_search(const SearchPlan& P, cudaStream_t st, bool capturing, int* launches) {
+    const unsigned int evf = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+    CU_TRY(cudaMemsetAsync(P.cnu, 0, 8 * (size_t)P.Q, st));
+    CU_TRY(cudaMemsetAsync(P.stats, 0, 8 * 8, st));
+    CU_TRY(cudaEventRecordWithFlags(P.ev[0], st, evf));
+    CU_TRY(launch_project_fp32(P.dQ, P.Q, P.D, P.A, P.b, P.LM, P.W, nullptr, P.vals, nullptr, nullptr, nullptr, st,
+                               P.proj_tile));
+    CU_TRY(cudaEventRecordWithFlags(P.ev[1], st, evf));
+    CU_TRY(launch_probe(P.pa, st));
+    CU_TRY(cudaEventRecordWithFlags(P.ev[2], st, evf));
+    if (P.use_ws) {
+        CU_TRY(launch_plan_items(P.wa, st));
+        CU_TRY(launch_candidates_ws(P.wa, P.ws_grid, st));
+    } else {
+        CU_TRY(launch_candidates(P.ca, st));
+    }
+    CU_TRY(cudaEventRecordWithFlags(P.ev[3], st, evf));
+    CU_TRY(cudaMemcpyAsync(P.h_stats, P.stats, 8 * 8, cudaMemcpyDeviceToHost, st));
+    *launches = P.use_ws ? 4 : 3;
+    return CULSH_OK;
+}
+
+// CULSH_NO_GRAPH (or culsh_search_set_graphs(s, 0)) runs the launches
+// directly instead of through the cached graph.
+bool graphs_enabled(const culsh_search* s, cudaStream_t st) {
+    if (!s->use_graphs || st == nullptr || getenv("CULSH_NO_GRAPH")) return false;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return false;
+    return true;
+}
+
+// Runs the plan: replays the cached graph when the plan is unchanged,
+// re-captures it otherwise, or launches directly when graphs are off.
+int run_plan(culsh_search* s, const SearchPlan& P, cudaStream_t st) {
+    if (!graphs_enabled(s, st)) {
+        s->graph_mode = 0;
+        return enqueue_search(P, st, false, &s->launches);
+    }
+    if (s->gexec && std::memcmp(&P, &s->gplan, sizeof(P)) == 0) {
+        CU_TRY(cudaGraphLaunch(s->gexec, st));
+        s->launches = s->glaunches;
+        s->graph_mode = 2;
+        return CULSH_OK;
+    }
+    if (s->gexec) {
+        cudaGraphExecDestroy(s->gexec);
+        s->gexec = nullptr;
+    }
+    CU_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+    int launches = 0;
+    const int rc = enqueue_search(P, st, true, &launches);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(st, &g);
+    if (rc != CULSH_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (ec != cudaSuccess) return fail(CULSH_ERR_DEVICE, "search graph capture: %s", cudaGetErrorString(ec));
+    const cudaError_t ei = cudaGraphInstantiate(&s->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+        s->gexec = nullptr;
+        return fail(CULSH_ERR_DEVICE, "search graph instantiation: %s", cudaGetErrorString(ei));
+    }
+    std::memcpy(&s->gplan, &P, sizeof(P));
+    s->glaunches = launches;
+    CU_TRY(cudaGraphLaunch(s->gexec, st));
+    s->launches = launches;
+    s->graph_mode = 1;
+    return CULSH_OK;
+}
+
+// After the plan ran: waits for its statistics, re-runs the candidate stage
+// per query when a work-stealing partition overflowed, and admits the
+// queries whose candidate sets did not fit the arena in chunks
+// (cuLSH_SearchTables.cu:282-306).
+int finish_search(culsh_search* s, const SearchPlan& P, cudaStream_t st) {
+    const int Q = P.Q;
+    const CandArgs& ca = P.ca;
     CU_TRY(cudaStreamSynchronize(st));
-    if (s->ws_used && (s->h_stats.p[4] >> 32) != 0) {
+    s->ws_used = P.use_ws;
+    s->ws_overflow = 0;
+    s->deferred_queries = 0;
+    if (P.use_ws && (s->h_stats.p[4] >> 32) != 0) {
         // A partition overflowed the shared-memory set (or the plan outgrew the
         // partial-list buffers): redo the stage with the per-query kernel,
         // whose global arena takes any set size.
@@ -840,8 +958,7 @@ int search_device(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float
     }
     unsigned int ndef = (unsigned int)(s->h_stats.p[3] & 0xffffffffu);
     if (ndef) {
-        // Queries whose candidate sets did not fit the arena: admit them in
-        // chunks that fit free device memory (cuLSH_SearchTables.cu:282-306).
+        const size_t cap_words = arena_cap_words();
         std::vector<int> dl(ndef);
         std::vector<unsigned long long> cnu(Q);
         CU_TRY(cudaMemcpyAsync(dl.data(), s->deferred.p, 4 * (size_t)ndef, cudaMemcpyDeviceToHost, st));
@@ -892,6 +1009,15 @@ int search_device(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float
     s->tot_unique = s->h_stats.p[0];
     s->tot_nonunique = s->h_stats.p[1];
     return CULSH_OK;
+}
+
+// The query path on device buffers (cuLSH_SearchTables.cu:197-463).
+int search_device(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* d_d, cudaStream_t st) {
+    SearchPlan P;
+    TRY(plan_search(s, dQ, Q, d_ids, d_d, &P));
+    s->host_copy_timed = false;
+    TRY(run_plan(s, P, st));
+    return finish_search(s, P, st);
 }
 
 }  // namespace
@@ -1247,6 +1373,184 @@ int culsh_search_run_device(culsh_search* s, const float* d_queries, int Q, int*
     return CULSH_OK;
 }
 
+static void tune_to_c(const SearchTune& t, culsh_tuning* o) {
+    o->proj_tile = t.proj_tile;
+    o->probe_batch = t.probe_pch;
+    o->candidates_mode = t.cand_ws;
+    o->ws_threads = t.ws_wt;
+    o->ws_blocks_per_sm = t.ws_bps;
+    o->ws_chunk = t.ws_chunk;
+}
+
+int culsh_search_get_tuning(culsh_search* s, culsh_tuning* out) {
+    if (!s || !out) return fail(CULSH_ERR_INVALID_ARGUMENT, "null argument");
+    *out = culsh_tuning{};
+    tune_to_c(s->tune, out);
+    return CULSH_OK;
+}
+
+int culsh_search_set_tuning(culsh_search* s, const culsh_tuning* in) {
+    if (!s || !in) return fail(CULSH_ERR_INVALID_ARGUMENT, "null argument");
+    const bool ok = in->proj_tile >= 0 && in->proj_tile <= 2 &&
+                    (in->probe_batch == 1 || in->probe_batch == 2 || in->probe_batch == 4) &&
+                    (in->candidates_mode == 0 || in->candidates_mode == 1) &&
+                    (in->ws_threads == 64 || in->ws_threads == 128 || in->ws_threads == 256) &&
+                    in->ws_blocks_per_sm >= 0 && in->ws_blocks_per_sm <= 64 && in->ws_chunk >= 64 &&
+                    in->ws_chunk <= 65536;
+    if (!ok) return fail(CULSH_ERR_INVALID_ARGUMENT, "tuning value out of range");
+    s->tune.proj_tile = in->proj_tile;
+    s->tune.probe_pch = in->probe_batch;
+    s->tune.cand_ws = in->candidates_mode;
+    s->tune.ws_wt = in->ws_threads;
+    s->tune.ws_bps = in->ws_blocks_per_sm;
+    s->tune.ws_chunk = in->ws_chunk;
+    return CULSH_OK;
+}
+
+int culsh_search_set_graphs(culsh_search* s, int enabled) {
+    if (!s) return fail(CULSH_ERR_INVALID_ARGUMENT, "null search");
+    s->use_graphs = enabled != 0;
+    return CULSH_OK;
+}
+
+// Coordinate search: the projection tiling by its stage time, the probe batch
+// depth by its stage time, then the candidate stage over its kernel form,
+// item width, partition size and residency. Each configuration is searched
+// once untimed and three times timed (median of each stage, device events).
+int culsh_search_autotune(culsh_search* s, const float* d_queries, int Q, int* d_ids, float* d_dists, void* stream,
+                          culsh_tuning* out) {
+    TRY(precheck_search(s, Q));
+    if (!d_queries || !d_ids || !d_dists) return fail(CULSH_ERR_INVALID_ARGUMENT, "null device buffer");
+    TRY(ensure_stream(&s->stream));
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
+    s->searched = false;
+    s->qb_host_valid = false;
+    TRY(ensure_device(s->ix, st));
+    const size_t nout = (size_t)Q * s->K;
+    std::vector<int> ref_ids(nout), got_ids(nout);
+    std::vector<float> ref_d(nout), got_d(nout);
+    unsigned long long ref_u = 0, ref_nu = 0;
+    bool have_ref = false;
+    int tried = 0;
+    auto median3 = [](float a, float b, float c) { return std::max(std::min(a, b), std::min(std::max(a, b), c)); };
+    // stage[0..2]: project, probe, candidates; stage[3]: whole search
+    auto measure = [&](float stage[4]) -> int {
+        float v[4][3];
+        for (int r = -1; r < 3; ++r) {
+            TRY(search_device(s, d_queries, Q, d_ids, d_dists, st));
+            if (r < 0) continue;
+            CU_TRY(cudaEventElapsedTime(&v[0][r], s->ev[0], s->ev[1]));
+            CU_TRY(cudaEventElapsedTime(&v[1][r], s->ev[1], s->ev[2]));
+            CU_TRY(cudaEventElapsedTime(&v[2][r], s->ev[2], s->ev[3]));
+            CU_TRY(cudaEventElapsedTime(&v[3][r], s->ev[0], s->ev[3]));
+        }
+        for (int k = 0; k < 4; ++k) stage[k] = median3(v[k][0], v[k][1], v[k][2]);
+        CU_TRY(cudaMemcpy(got_ids.data(), d_ids, 4 * nout, cudaMemcpyDeviceToHost));
+        CU_TRY(cudaMemcpy(got_d.data(), d_dists, 4 * nout, cudaMemcpyDeviceToHost));
+        if (!have_ref) {
+            ref_ids = got_ids;
+            ref_d = got_d;
+            ref_u = s->tot_unique;
+            ref_nu = s->tot_nonunique;
+            have_ref = true;
+        } else if (got_ids != ref_ids || std::memcmp(got_d.data(), ref_d.data(), 4 * nout) != 0 ||
+                   s->tot_unique != ref_u || s->tot_nonunique != ref_nu) {
+            return fail(CULSH_ERR_DEVICE, "autotune: configurations returned different results");
+        }
+        ++tried;
+        return CULSH_OK;
+    };
+    const SearchTune start = s->tune;
+    SearchTune best = start;
+    float stage[4];
+    float best_t = 0;
+    // projection tiling
+    for (int tile = 0; tile <= 2; ++tile) {
+        s->tune = best;
+        s->tune.proj_tile = tile;
+        const int rc = measure(stage);
+        if (rc != CULSH_OK) {
+            s->tune = start;
+            return rc;
+        }
+        if (tile == 0 || stage[0] < best_t) {
+            best_t = stage[0];
+            best.proj_tile = tile;
+        }
+    }
+    // probe batch depth
+    const int pchs[3] = {1, 2, 4};
+    for (int i = 0; i < 3; ++i) {
+        s->tune = best;
+        s->tune.probe_pch = pchs[i];
+        const int rc = measure(stage);
+        if (rc != CULSH_OK) {
+            s->tune = start;
+            return rc;
+        }
+        if (i == 0 || stage[1] < best_t) {
+            best_t = stage[1];
+            best.probe_pch = pchs[i];
+        }
+    }
+    // candidate stage
+    std::vector<SearchTune> cands;
+    {
+        SearchTune t = best;
+        t.cand_ws = 0;
+        cands.push_back(t);
+        const int wts[3] = {64, 128, 256}, chunks[3] = {512, 1024, 2048};
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) {
+                SearchTune u = best;
+                u.cand_ws = 1;
+                u.ws_wt = wts[a];
+                u.ws_chunk = chunks[b];
+                u.ws_bps = 0;
+                cands.push_back(u);
+            }
+    }
+    bool first = true;
+    for (const SearchTune& t : cands) {
+        s->tune = t;
+        const int rc = measure(stage);
+        if (rc != CULSH_OK) {
+            s->tune = start;
+            return rc;
+        }
+        if (first || stage[2] < best_t) {
+            best_t = stage[2];
+            best = t;
+            first = false;
+        }
+    }
+    if (best.cand_ws) {   // residency: half the occupancy limit as well
+        const int occ = ws_blocks_per_sm(s->ix->D, s->K, best.ws_wt);
+        if (occ > 1) {
+            SearchTune t = best;
+            t.ws_bps = occ / 2;
+            s->tune = t;
+            const int rc = measure(stage);
+            if (rc != CULSH_OK) {
+                s->tune = start;
+                return rc;
+            }
+            if (stage[2] < best_t) best = t;
+        }
+    }
+    s->tune = best;
+    const int rc = measure(stage);
+    if (rc != CULSH_OK) return rc;
+    s->Q = Q;
+    if (out) {
+        *out = culsh_tuning{};
+        tune_to_c(best, out);
+        out->search_ms = stage[3];
+        out->configs_tried = tried;
+    }
+    return CULSH_OK;
+}
+
 const int* culsh_search_knn_ids(culsh_search* s) { return (s && s->searched) ? s->h_ids.p : nullptr; }
 const float* culsh_search_knn_distances(culsh_search* s) { return (s && s->searched) ? s->h_d.p : nullptr; }
 
@@ -1291,6 +1595,7 @@ int culsh_search_profile_get(culsh_search* s, culsh_search_profile* out) {
     out->deferred_queries = s->deferred_queries;
     out->key_words = s->ix ? s->ix->KW : 0;
     out->candidates_mode = s->ws_used ? (s->ws_overflow ? 2 : 1) : 0;
+    out->graph_mode = s->graph_mode;
     return CULSH_OK;
 }
 
@@ -1400,6 +1705,7 @@ extern "C" int culsh_search_run_device_noalloc(culsh_search* s, const float* d_q
     pa.qbuckets = qb;
     pa.cnu = cnu;
     pa.small_codes = small_codes(ix);
+    pa.pch = 2;
     CU_TRY(launch_probe(pa, st));
     CandArgs ca;
     ca.X = ix->dev_x();

@@ -109,9 +109,10 @@ struct LookupView {
 // Canonical FP32 projection of n_pts points onto the LM stacked columns.
 // codes != nullptr: floored codes [LM][n_pts] + per-block min/max partials
 // [grid_x][LM]; vals != nullptr: unfloored values [LM][n_pts].
+// tile picks the query-value tiling (0: 64x128, 1: 32x128, 2: 128x64 points x columns).
 cudaError_t launch_project_fp32(const float* X, int64_t n_pts, int D, const float* A, const float* b, int LM,
                                 float W, int32_t* codes, float* vals, int32_t* pmin, int32_t* pmax, int* err,
-                                cudaStream_t st);
+                                cudaStream_t st, int tile = 0);
 int project_grid_x(int64_t n_pts);
 cudaError_t launch_minmax_reduce(const int32_t* pmin, const int32_t* pmax, int nparts, int LM, int32_t* cmin,
                                  int32_t* cmax, cudaStream_t st);
@@ -192,6 +193,7 @@ struct ProbeArgs {
     int32_t* qbuckets;         // [L][Q*T]
     unsigned long long* cnu;   // [Q] non-unique candidate counts (accumulated)
     int small_codes;           // every |cmin|, |cmax| < 2^24 - 2 (set by the host)
+    int pch;                   // fast kernel: probes whose group loads overlap (1, 2, 4)
 };
 cudaError_t launch_probe(const ProbeArgs& a, cudaStream_t st);
 
@@ -249,9 +251,10 @@ struct WsArgs {
     unsigned int* n_items;
     unsigned int* next_item;           // work-stealing counter, zero before the launch
     unsigned int* overflow;            // nonzero: rerun with the per-query kernel
+    int wt;                            // threads per item CTA: 64, 128 or 256
 };
-size_t ws_smem_bytes(int D, int K);
-int ws_blocks_per_sm(int D, int K);
+size_t ws_smem_bytes(int D, int K, int wt);
+int ws_blocks_per_sm(int D, int K, int wt);
 cudaError_t launch_plan_items(const WsArgs& a, cudaStream_t st);
 cudaError_t launch_candidates_ws(const WsArgs& a, int grid, cudaStream_t st);
 

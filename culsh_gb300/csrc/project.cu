@@ -23,8 +23,9 @@ constexpr int NT = 256;   // threads: 16 (points) x 16 (columns), each PT x CT o
 
 // Block tile BN = 16*PT points x BC = 16*CT columns, BK dimensions per
 // shared-memory stage. Index builds use PT = 8, CT = 4, BK = 16; query batches
-// use PT = 4, CT = 8, BK = 64 (fewer barriers and shared-memory loads per FMA,
-// enough blocks for ten thousand queries).
+// use PT = 4, CT = 8, BK = 64 by default (fewer barriers and shared-memory
+// loads per FMA, enough blocks for ten thousand queries), PT = 2 for small
+// batches or PT = 8, CT = 4, BK = 32 for large ones, as the search tuner picks.
 template <bool kCodes, int PT, int CT, int BK>
 __global__ void __launch_bounds__(NT) k_project(const float* __restrict__ X, int64_t n_pts, int D,
                                                 const float* __restrict__ A, const float* __restrict__ b, int LM,
@@ -213,11 +214,17 @@ int project_grid_x(int64_t n_pts) { return (int)((n_pts + 127) / 128); }
 
 cudaError_t launch_project_fp32(const float* X, int64_t n_pts, int D, const float* A, const float* b, int LM,
                                 float W, int32_t* codes, float* vals, int32_t* pmin, int32_t* pmax, int* err,
-                                cudaStream_t st) {
+                                cudaStream_t st, int tile) {
     if (n_pts <= 0) return cudaSuccess;
     if (codes) {
         k_project<true, 8, 4, 16><<<dim3(project_grid_x(n_pts), (LM + 63) / 64), NT, 0, st>>>(
             X, n_pts, D, A, b, LM, W, codes, nullptr, pmin, pmax, err);
+    } else if (tile == 1) {
+        k_project<false, 2, 8, 64><<<dim3((unsigned)((n_pts + 31) / 32), (LM + 127) / 128), NT, 0, st>>>(
+            X, n_pts, D, A, b, LM, W, nullptr, vals, nullptr, nullptr, err);
+    } else if (tile == 2) {
+        k_project<false, 8, 4, 32><<<dim3((unsigned)((n_pts + 127) / 128), (LM + 63) / 64), NT, 0, st>>>(
+            X, n_pts, D, A, b, LM, W, nullptr, vals, nullptr, nullptr, err);
     } else {
         k_project<false, 4, 8, 64><<<dim3((unsigned)((n_pts + 63) / 64), (LM + 127) / 128), NT, 0, st>>>(
             X, n_pts, D, A, b, LM, W, nullptr, vals, nullptr, nullptr, err);

@@ -207,7 +207,6 @@ __global__ void __launch_bounds__(128) k_probe(ProbeArgs a) {
 // at a time before any is consumed. Per-thread state lives in a strided
 // slice of shared memory. Results equal k_probe's exactly.
 constexpr int PF = 128;
-constexpr int PCH = 2;   // probes whose group loads are in flight together
 typedef unsigned __int128 u128;
 
 __device__ __forceinline__ u128 field_term(int64_t f, int off) { return ((u128)(__int128)f) << off; }
@@ -314,7 +313,8 @@ __host__ __device__ constexpr size_t probe_fast_bytes_per_thread(int M, int T) {
     return sizeof(MaskT) * (size_t)T + sizeof(float) * (size_t)(M + T) + (size_t)(2 * M + M);
 }
 
-template <typename MaskT>
+// PCH: probes whose group loads are in flight together (tuned: 1, 2 or 4).
+template <typename MaskT, int PCH>
 __global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
     extern __shared__ __align__(16) unsigned char psm[];
     const LookupView& lv = a.lv;
@@ -509,19 +509,28 @@ __global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
     if (cnu) atomicAdd(a.cnu + q, cnu);
 }
 
-template <typename MaskT>
-cudaError_t launch_probe_fast_t(const ProbeArgs& a, cudaStream_t st) {
+template <typename MaskT, int PCH>
+cudaError_t launch_probe_fast_v(const ProbeArgs& a, cudaStream_t st) {
     const size_t smem = (size_t)PF * probe_fast_bytes_per_thread<MaskT>(a.lv.M, a.T);
     static size_t configured = 0;
     if (smem > 48 * 1024 && smem > configured) {
         cudaError_t e =
-            cudaFuncSetAttribute(k_probe_fast<MaskT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cudaFuncSetAttribute(k_probe_fast<MaskT, PCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         configured = smem;
     }
     const int64_t n = (int64_t)a.lv.L * a.Q;
-    k_probe_fast<MaskT><<<(unsigned)((n + PF - 1) / PF), PF, smem, st>>>(a);
+    k_probe_fast<MaskT, PCH><<<(unsigned)((n + PF - 1) / PF), PF, smem, st>>>(a);
     return cudaGetLastError();
+}
+
+template <typename MaskT>
+cudaError_t launch_probe_fast_t(const ProbeArgs& a, cudaStream_t st) {
+    switch (a.pch) {
+        case 1: return launch_probe_fast_v<MaskT, 1>(a, st);
+        case 4: return launch_probe_fast_v<MaskT, 4>(a, st);
+        default: return launch_probe_fast_v<MaskT, 2>(a, st);
+    }
 }
 
 // 32-bit masks when the 2M sorted deltas fit (M <= 16).

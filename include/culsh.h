@@ -127,6 +127,32 @@ int culsh_search_run(culsh_search* s, const float* queries, int Q, const float* 
 int culsh_search_run_device(culsh_search* s, const float* d_queries, int Q, int* d_ids, float* d_dists,
                             void* stream);
 
+/* Search-path tuning (no counterpart in the reference). The search runs as a
+ * CUDA graph captured on first use and replayed while the query pointer,
+ * count, outputs, index buffers and tuning stay the same (captured again
+ * otherwise); graphs are used on any stream but the legacy default stream
+ * and never inside a caller's own capture. */
+typedef struct culsh_tuning {
+    int proj_tile;        /* query projection tiling: 0 (64x128), 1 (32x128), 2 (128x64) */
+    int probe_batch;      /* multiprobe hash-group loads in flight per thread: 1, 2, 4   */
+    int candidates_mode;  /* 0: one block per query; 1: persistent work-stealing grid   */
+    int ws_threads;       /* work-stealing threads per item: 64, 128, 256               */
+    int ws_blocks_per_sm; /* resident work-stealing CTAs per SM, 0 = occupancy limit     */
+    int ws_chunk;         /* non-unique candidates per id partition (64 .. 65536)        */
+    float search_ms;      /* culsh_search_autotune: median device ms of the choice       */
+    int configs_tried;    /* culsh_search_autotune: configurations timed                 */
+} culsh_tuning;
+
+/* Times the search over the tuning space on the caller's queries (device
+ * buffers, as culsh_search_run_device) and keeps the fastest configuration
+ * for later searches of this object. Every configuration must return the
+ * same ids, distances and counts, else CULSH_ERR_DEVICE. */
+int culsh_search_autotune(culsh_search* s, const float* d_queries, int Q, int* d_ids, float* d_dists,
+                          void* stream, culsh_tuning* out);
+int culsh_search_get_tuning(culsh_search* s, culsh_tuning* out);
+int culsh_search_set_tuning(culsh_search* s, const culsh_tuning* in);   /* CULSH_ERR_INVALID_ARGUMENT when out of range */
+int culsh_search_set_graphs(culsh_search* s, int enabled);               /* default 1 */
+
 /* Getters cuLSH_SearchTables.cu:83-105. */
 const int* culsh_search_knn_ids(culsh_search* s);
 const float* culsh_search_knn_distances(culsh_search* s);
@@ -150,6 +176,7 @@ typedef struct culsh_search_profile {
     int candidates_mode; /* 0: one block per query; 1: persistent work-stealing
                             grid over id partitions; 2: work-stealing, re-run
                             per query after a partition overflowed            */
+    int graph_mode;      /* 0: direct launches; 1: graph captured; 2: replayed */
 } culsh_search_profile;
 int culsh_search_profile_get(culsh_search* s, culsh_search_profile* out);
 

@@ -1,0 +1,126 @@
+"""The batched search form: CUDA-graph capture and replay of the whole query
+path, every tuning configuration, and the autotuner. Each configuration must
+return exactly the oracle's results (ids, distances, query buckets, counts)."""
+
+import itertools
+
+import numpy as np
+import pytest
+
+from conftest import load_case
+from test_gpu_parity import build_index, check_search
+
+pytestmark = pytest.mark.gpu
+
+
+def search_host(culsh, ht, c, st=None):
+    st = st or culsh.SearchTables()
+    st.reset(ht, int(c["K"]), int(c["T"]))
+    st.search(c["queries"], dataset=c["X"])
+    return st
+
+
+def test_graph_captured_then_replayed(culsh):
+    c = load_case("mix_d16_t8")
+    ht = build_index(culsh, c)
+    st = culsh.SearchTables()
+    st.reset(ht, int(c["K"]), int(c["T"]))
+    modes = []
+    for _ in range(3):
+        st.search(c["queries"], dataset=c["X"])
+        check_search(st, c)
+        modes.append(st.profile()["graph_mode"])
+    assert modes == [1, 2, 2]
+    # fewer queries: a different plan, captured again, then replayed
+    st.search(c["queries"][:7], dataset=c["X"])
+    assert st.profile()["graph_mode"] == 1
+    np.testing.assert_array_equal(st.getKnnIds(), c["knn_ids"][:7])
+    st.search(c["queries"][:7], dataset=c["X"])
+    assert st.profile()["graph_mode"] == 2
+    np.testing.assert_array_equal(st.getKnnIds(), c["knn_ids"][:7])
+
+
+def test_graph_off_matches(culsh, monkeypatch):
+    c = load_case("heavy")
+    ht = build_index(culsh, c)
+    st = culsh.SearchTables()
+    st.set_graphs(False)
+    search_host(culsh, ht, c, st)
+    check_search(st, c)
+    assert st.profile()["graph_mode"] == 0
+    st.set_graphs(True)
+    monkeypatch.setenv("CULSH_NO_GRAPH", "1")
+    search_host(culsh, ht, c, st)
+    assert st.profile()["graph_mode"] == 0
+    monkeypatch.delenv("CULSH_NO_GRAPH")
+    search_host(culsh, ht, c, st)
+    check_search(st, c)
+    assert st.profile()["graph_mode"] == 1
+
+
+def test_graph_follows_index_rebuild(culsh):
+    """A rebuilt index (other data, other sizes) re-captures the graph."""
+    a, b = load_case("odd_d13"), load_case("int_dups")
+    st = culsh.SearchTables()
+    for c in (a, b, a):
+        ht = build_index(culsh, c)
+        for _ in range(2):
+            search_host(culsh, ht, c, st)
+            check_search(st, c)
+
+
+@pytest.mark.parametrize("name", ["heavy", "m20_t40", "odd_d13"])
+def test_every_tuning_configuration(culsh, name):
+    c = load_case(name)
+    ht = build_index(culsh, c)
+    st = culsh.SearchTables()
+    st.reset(ht, int(c["K"]), int(c["T"]))
+    for tile, pch in itertools.product((0, 1, 2), (1, 2, 4)):
+        st.set_tuning(proj_tile=tile, probe_batch=pch)
+        st.search(c["queries"], dataset=c["X"])
+        check_search(st, c)
+    st.set_tuning(proj_tile=0, probe_batch=2, candidates_mode=0)
+    st.search(c["queries"], dataset=c["X"])
+    check_search(st, c)
+    assert st.profile()["candidates_mode"] == 0
+    for wt, chunk, bps in itertools.product((64, 128, 256), (64, 1024, 4096), (0, 1)):
+        st.set_tuning(candidates_mode=1, ws_threads=wt, ws_chunk=chunk, ws_blocks_per_sm=bps)
+        st.search(c["queries"], dataset=c["X"])
+        check_search(st, c)
+        np.testing.assert_array_equal(st.getKnnDistances(), c["knn_dists"])
+
+
+def test_tuning_rejects_out_of_range(culsh):
+    st = culsh.SearchTables()
+    for bad in ({"probe_batch": 3}, {"proj_tile": 5}, {"ws_threads": 96}, {"ws_chunk": 8}, {"candidates_mode": 2}):
+        with pytest.raises(culsh.CulshError) as ei:
+            st.set_tuning(**bad)
+        assert ei.value.code == culsh.ERR_INVALID_ARGUMENT
+    t = st.get_tuning()
+    assert (t["probe_batch"], t["candidates_mode"], t["ws_threads"]) == (2, 1, 128)
+
+
+def test_autotune_keeps_results(culsh):
+    torch = pytest.importorskip("torch")
+    c = load_case("heavy")
+    ht = build_index(culsh, c)
+    K, T = int(c["K"]), int(c["T"])
+    q = torch.from_numpy(c["queries"]).cuda()
+    ids = torch.empty((q.shape[0], K), dtype=torch.int32, device="cuda")
+    d = torch.empty((q.shape[0], K), dtype=torch.float32, device="cuda")
+    st = culsh.SearchTables()
+    st.reset(ht, K, T)
+    side = torch.cuda.Stream()
+    tune = st.autotune(q.data_ptr(), q.shape[0], ids.data_ptr(), d.data_ptr(), side.cuda_stream)
+    assert tune["configs_tried"] >= 16 and tune["search_ms"] > 0
+    assert tune["probe_batch"] in (1, 2, 4) and tune["ws_threads"] in (64, 128, 256)
+    assert st.get_tuning()["probe_batch"] == tune["probe_batch"]
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(ids.cpu().numpy(), c["knn_ids"])
+    np.testing.assert_array_equal(d.cpu().numpy(), c["knn_dists"])
+    # the tuned object keeps serving identical results through the graph
+    for _ in range(2):
+        st.search_device(q.data_ptr(), q.shape[0], ids.data_ptr(), d.data_ptr(), side.cuda_stream)
+        side.synchronize()
+        np.testing.assert_array_equal(ids.cpu().numpy(), c["knn_ids"])
+    assert st.profile()["graph_mode"] == 2
