@@ -35,6 +35,7 @@ ERR_NUMERIC = 6
 ERR_CAPACITY = 7
 ERR_DEVICE = 8
 ERR_FORMAT = 9
+PENDING = 10
 
 MAX_M = 64
 MAX_T = 256
@@ -67,6 +68,18 @@ class _IndexProfile(ctypes.Structure):
     _fields_ = [("project_ms", ctypes.c_float), ("pack_ms", ctypes.c_float), ("sort_ms", ctypes.c_float),
                 ("bucket_ms", ctypes.c_float), ("total_ms", ctypes.c_float), ("tensor_cores", ctypes.c_int),
                 ("recomputed", ctypes.c_longlong), ("key_words", ctypes.c_int), ("sort_passes", ctypes.c_int)]
+
+
+class _ServerConfig(ctypes.Structure):
+    _fields_ = [("slots", ctypes.c_int), ("max_batch_queries", ctypes.c_int), ("memory_budget", ctypes.c_longlong)]
+
+
+class _ServerStats(ctypes.Structure):
+    _fields_ = [("requests", ctypes.c_longlong), ("queries", ctypes.c_longlong), ("batches", ctypes.c_longlong),
+                ("failed", ctypes.c_longlong), ("wall_s", ctypes.c_double), ("qps", ctypes.c_double),
+                ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double), ("mean_ms", ctypes.c_double),
+                ("max_ms", ctypes.c_double), ("max_in_flight", ctypes.c_int), ("slots", ctypes.c_int),
+                ("peak_device_bytes", ctypes.c_longlong), ("budget_bytes", ctypes.c_longlong)]
 
 
 _P = ctypes.c_void_p
@@ -117,6 +130,15 @@ ABI = {
     "culsh_search_get_tuning": (_I, [_P, ctypes.POINTER(_Tuning)]),
     "culsh_search_set_tuning": (_I, [_P, ctypes.POINTER(_Tuning)]),
     "culsh_search_set_graphs": (_I, [_P, _I]),
+    "culsh_search_device_bytes": (ctypes.c_longlong, [_P]),
+    "culsh_search_estimate_bytes": (ctypes.c_longlong, [_P, _I, _I, _I]),
+    "culsh_search_release": (_I, [_P]),
+    "culsh_server_create": (_I, [ctypes.POINTER(_P), _P, ctypes.POINTER(_ServerConfig)]),
+    "culsh_server_submit": (_I, [_P, _P, _I, _I, _I, _P, _P, ctypes.POINTER(ctypes.c_ulonglong)]),
+    "culsh_server_wait": (_I, [_P, ctypes.c_ulonglong, ctypes.c_double]),
+    "culsh_server_stats_get": (_I, [_P, ctypes.POINTER(_ServerStats)]),
+    "culsh_server_stats_reset": (_I, [_P]),
+    "culsh_server_destroy": (None, [_P]),
 }
 
 _lib = None
@@ -354,3 +376,60 @@ class SearchTables:
         p = _Profile()
         _check(lib().culsh_search_profile_get(self._h, ctypes.byref(p)))
         return {n: getattr(p, n) for n, _ in _Profile._fields_}
+
+
+class Server:
+    """Serving loop over one device-resident index (culsh_server_*): requests
+    of any Q, K, T are batched as slots and device memory free up, and run
+    concurrently on the device; each returns what a lone search returns."""
+
+    def __init__(self, hashtables: HashTables, slots: int = 4, max_batch_queries: int = 8192,
+                 memory_budget: int = 0):
+        self._ht = hashtables
+        self._h = ctypes.c_void_p()
+        cfg = _ServerConfig(int(slots), int(max_batch_queries), int(memory_budget))
+        _check(lib().culsh_server_create(ctypes.byref(self._h), hashtables._h, ctypes.byref(cfg)))
+        self._keep = {}
+
+    def submit(self, queries, K: int, T: int = 1) -> int:
+        """Queues queries [Q, D]; returns a ticket for wait()."""
+        q = _f32(queries).reshape(-1, self._ht.getD())
+        Q = q.shape[0]
+        ids = np.empty((Q, int(K)), np.int32)
+        d = np.empty((Q, int(K)), np.float32)
+        t = ctypes.c_ulonglong()
+        _check(lib().culsh_server_submit(self._h, _ptr(q), Q, int(K), int(T), ids.ctypes.data_as(_P),
+                                         d.ctypes.data_as(_P), ctypes.byref(t)))
+        self._keep[t.value] = (q, ids, d)
+        return t.value
+
+    def wait(self, ticket: int, timeout: float = -1.0):
+        """(ids [Q, K], dists [Q, K]) of a request; raises CulshError on its error."""
+        rc = lib().culsh_server_wait(self._h, ctypes.c_ulonglong(ticket), float(timeout))
+        if rc == PENDING:
+            raise TimeoutError(f"request {ticket} still running")
+        _, ids, d = self._keep.pop(ticket)
+        _check(rc)
+        return ids, d
+
+    def stats(self):
+        st = _ServerStats()
+        _check(lib().culsh_server_stats_get(self._h, ctypes.byref(st)))
+        return {n: getattr(st, n) for n, _ in _ServerStats._fields_}
+
+    def reset_stats(self):
+        _check(lib().culsh_server_stats_reset(self._h))
+
+    def close(self):
+        if self._h and self._h.value and _lib is not None:
+            _lib.culsh_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -19,6 +19,7 @@
 //    count instead of spilling; the host then re-runs the search through the
 //    arena-based kernel (rare: more than ~65k non-unique candidates for one
 //    query).
+#include <atomic>
 #include <cfloat>
 
 #include "culsh_internal.cuh"
@@ -295,7 +296,7 @@ namespace {
 template <int WT>
 cudaError_t launch_ws_v(const WsArgs& a, int grid, cudaStream_t st) {
     const size_t smem = ws_smem_bytes(a.D, a.K, WT);
-    static size_t configured = 0;
+    static std::atomic<size_t> configured{0};   // largest dynamic shared memory opted into
     if (smem > 48 * 1024 && smem > configured) {
         cudaError_t e = cudaFuncSetAttribute(k_candidates_ws<WT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;

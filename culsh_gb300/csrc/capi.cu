@@ -683,6 +683,17 @@ size_t arena_cap_words() {
     return ~size_t(0);
 }
 
+}  // namespace
+
+std::mutex& culsh::alloc_capture_mutex() {
+    static std::mutex mu;
+    return mu;
+}
+
+int culsh::set_last_error(int code, const char* msg) { return fail(code, "%s", msg); }
+
+namespace {
+
 // CULSH_CANDIDATES_PER_QUERY forces the per-query candidate kernel (one
 // block per query; the tests run both forms).
 int forced_per_query() { return getenv("CULSH_CANDIDATES_PER_QUERY") != nullptr; }
@@ -983,6 +994,7 @@ int finish_search(culsh_search* s, const SearchPlan& P, cudaStream_t st) {
         }
         const size_t want = std::min(need_all, avail_words);
         if (want > s->arena.n) {
+            std::lock_guard<std::mutex> lk(alloc_capture_mutex());
             s->arena.release();
             CU_TRY(s->arena.reserve(want));
         }
@@ -1011,12 +1023,18 @@ int finish_search(culsh_search* s, const SearchPlan& P, cudaStream_t st) {
     return CULSH_OK;
 }
 
-// The query path on device buffers (cuLSH_SearchTables.cu:197-463).
+// The query path on device buffers (cuLSH_SearchTables.cu:197-463). Planning
+// (which may grow buffers) and graph capture hold the process-wide lock, so
+// that searches on other threads (the serving loop's slots) never free device
+// memory during a capture; launches and the wait for results do not.
 int search_device(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* d_d, cudaStream_t st) {
     SearchPlan P;
-    TRY(plan_search(s, dQ, Q, d_ids, d_d, &P));
-    s->host_copy_timed = false;
-    TRY(run_plan(s, P, st));
+    {
+        std::lock_guard<std::mutex> lk(alloc_capture_mutex());
+        TRY(plan_search(s, dQ, Q, d_ids, d_d, &P));
+        s->host_copy_timed = false;
+        TRY(run_plan(s, P, st));
+    }
     return finish_search(s, P, st);
 }
 
@@ -1230,6 +1248,23 @@ int culsh_index_load(culsh_index* ix, const char* path, FILE* dbg) {
     return CULSH_OK;
 }
 
+}  // extern "C"
+
+// Makes the index and its dataset device-resident (serving loop start-up), so
+// that concurrent searches only read it.
+int culsh::index_make_resident(culsh_index* ix) {
+    if (!ix) return fail(CULSH_ERR_INVALID_ARGUMENT, "null index");
+    if (!ix->indexed && !ix->host_valid) return fail(CULSH_ERR_STATE, "No index: have you performed indexing or loaded a file???");
+    if (!ix->dev_x())
+        return fail(CULSH_ERR_STATE, "the dataset is not on the device (index it, or search once with it after a load)");
+    TRY(ensure_stream(&ix->stream));
+    TRY(ensure_device(ix, ix->stream));
+    CU_TRY(cudaStreamSynchronize(ix->stream));
+    return CULSH_OK;
+}
+
+extern "C" {
+
 void culsh_index_params(const culsh_index* ix, int* N, int* D, int* L, int* M, float* W) {
     if (N) *N = ix ? ix->N : 0;
     if (D) *D = ix ? ix->D : 0;
@@ -1370,6 +1405,73 @@ int culsh_search_run_device(culsh_search* s, const float* d_queries, int Q, int*
     TRY(search_device(s, d_queries, Q, d_ids, d_dists, st));
     s->Q = Q;
     s->searched = false;   // results live in the caller's device buffers
+    return CULSH_OK;
+}
+
+long long culsh_search_device_bytes(culsh_search* s) {
+    if (!s) return 0;
+    size_t b = 0;
+    auto add = [&](const auto& buf) { b += buf.n * sizeof(*buf.p); };
+    add(s->dq);
+    add(s->vals);
+    add(s->od);
+    add(s->qb);
+    add(s->oids);
+    add(s->cnu);
+    add(s->cu);
+    add(s->stats);
+    add(s->deferred);
+    add(s->arena);
+    add(s->q_items);
+    add(s->q_off);
+    add(s->item_q);
+    add(s->part_n);
+    add(s->q_done);
+    add(s->item_p);
+    add(s->part_d);
+    add(s->part_i);
+    return (long long)b;
+}
+
+long long culsh_search_estimate_bytes(const culsh_index* ix, int Q, int K, int T) {
+    if (!ix || Q <= 0 || K <= 0 || T <= 0) return 0;
+    const size_t L = ix->L, M = ix->M, q = (size_t)Q, k = (size_t)K;
+    size_t b = 4 * L * M * q + 4 * L * q * (size_t)T + 8 * q + 8 * q + 64 + 8 * q + 4 * kArenaInitialWords;
+    const size_t per_item = k * 8 + 4 + 4 + 1;
+    size_t cap = std::max<size_t>(2 * q, kWsPartialBytes / per_item);
+    cap = std::min(cap, q * kWsPartitions);
+    b += 12 * q + cap * per_item;
+    return (long long)b;
+}
+
+int culsh_search_release(culsh_search* s) {
+    if (!s) return fail(CULSH_ERR_INVALID_ARGUMENT, "null search");
+    std::lock_guard<std::mutex> lk(alloc_capture_mutex());
+    if (s->gexec) {
+        cudaGraphExecDestroy(s->gexec);
+        s->gexec = nullptr;
+    }
+    s->dq.release();
+    s->vals.release();
+    s->od.release();
+    s->qb.release();
+    s->oids.release();
+    s->cnu.release();
+    s->cu.release();
+    s->stats.release();
+    s->deferred.release();
+    s->arena.release();
+    s->q_items.release();
+    s->q_off.release();
+    s->item_q.release();
+    s->part_n.release();
+    s->q_done.release();
+    s->item_p.release();
+    s->part_d.release();
+    s->part_i.release();
+    s->Q = 0;
+    s->searched = false;
+    s->qb_host_valid = false;
     return CULSH_OK;
 }
 

@@ -20,9 +20,15 @@
 #pragma once
 
 #include <cstdint>
+#include <mutex>
 #include <cuda_runtime.h>
 
+struct culsh_index;
+
 namespace culsh {
+
+// Makes an index and its dataset device-resident (capi.cu).
+int index_make_resident(culsh_index* ix);
 
 constexpr int kMaxM = 64;     // projection columns per table
 constexpr int kMaxKW = 8;     // packed key words (256 bits)
@@ -257,6 +263,12 @@ size_t ws_smem_bytes(int D, int K, int wt);
 int ws_blocks_per_sm(int D, int K, int wt);
 cudaError_t launch_plan_items(const WsArgs& a, cudaStream_t st);
 cudaError_t launch_candidates_ws(const WsArgs& a, int grid, cudaStream_t st);
+
+// Process-wide lock held while a search plans (and grows) its buffers and
+// captures its graph: no thread frees device memory while another captures.
+std::mutex& alloc_capture_mutex();
+// Sets the calling thread's culsh_last_error() message; returns code.
+int set_last_error(int code, const char* msg);
 
 int cand_smem_capacity();              // candidates handled in shared memory per query
 cudaError_t launch_candidates(const CandArgs& a, cudaStream_t st);

@@ -16,6 +16,7 @@
 // sorted id arrays, deduplicated in a shared-memory hash set (global arena for
 // large sets), squared L2 distances are computed in the reference's lane order
 // from 16-byte loads, and each warp keeps a sorted top-K that the block merges.
+#include <atomic>
 #include <cfloat>
 #include <cstdlib>
 
@@ -512,7 +513,7 @@ __global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
 template <typename MaskT, int PCH>
 cudaError_t launch_probe_fast_v(const ProbeArgs& a, cudaStream_t st) {
     const size_t smem = (size_t)PF * probe_fast_bytes_per_thread<MaskT>(a.lv.M, a.T);
-    static size_t configured = 0;
+    static std::atomic<size_t> configured{0};   // largest dynamic shared memory opted into
     if (smem > 48 * 1024 && smem > configured) {
         cudaError_t e =
             cudaFuncSetAttribute(k_probe_fast<MaskT, PCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -716,7 +717,7 @@ cudaError_t launch_candidates(const CandArgs& a, cudaStream_t st) {
     if (nblk <= 0) return cudaSuccess;
     const size_t smem = sizeof(float) * (size_t)((a.D + 3) & ~3) + sizeof(uint32_t) * (SM_SLOTS + SM_CAP) +
                         (size_t)CW * a.K * (sizeof(float) + sizeof(uint32_t));
-    static size_t configured = 0;
+    static std::atomic<size_t> configured{0};   // largest dynamic shared memory opted into
     if (smem > 48 * 1024 && smem > configured) {
         cudaError_t e = cudaFuncSetAttribute(k_candidates, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;

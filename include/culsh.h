@@ -39,6 +39,7 @@ extern "C" {
 #define CULSH_ERR_CAPACITY 7         /* size beyond a documented limit of this library   */
 #define CULSH_ERR_DEVICE 8           /* a device-side bounded wait or insert gave up     */
 #define CULSH_ERR_FORMAT 9           /* index file truncated or inconsistent             */
+#define CULSH_PENDING 10             /* serving: the request has not completed (no error) */
 
 /* Limits of this implementation (the reference has the memory limits only). */
 #define CULSH_MAX_M 64      /* projection columns per table               */
@@ -153,6 +154,15 @@ int culsh_search_get_tuning(culsh_search* s, culsh_tuning* out);
 int culsh_search_set_tuning(culsh_search* s, const culsh_tuning* in);   /* CULSH_ERR_INVALID_ARGUMENT when out of range */
 int culsh_search_set_graphs(culsh_search* s, int enabled);               /* default 1 */
 
+/* Device memory of a search object (no counterpart in the reference; the
+ * serving loop's admission uses them). device_bytes: bytes its buffers hold
+ * now (they grow to the largest search and are kept for reuse);
+ * estimate_bytes: an upper bound on what one device search of Q queries with
+ * K, T makes them hold; release: frees them (and the cached graph). */
+long long culsh_search_device_bytes(culsh_search* s);
+long long culsh_search_estimate_bytes(const culsh_index* ix, int Q, int K, int T);
+int culsh_search_release(culsh_search* s);
+
 /* Getters cuLSH_SearchTables.cu:83-105. */
 const int* culsh_search_knn_ids(culsh_search* s);
 const float* culsh_search_knn_distances(culsh_search* s);
@@ -198,6 +208,55 @@ int culsh_search_profile_get(culsh_search* s, culsh_search_profile* out);
  *    are not updated (results go only to d_ids / d_dists). */
 int culsh_search_run_device_noalloc(culsh_search* s, const float* d_queries, int Q, int* d_ids, float* d_dists,
                                     void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Serving loop (no counterpart in the reference, whose search is one blocking
+ * call per query set, cuLSH_SearchTables.cu:197-463). A server keeps one index
+ * resident and runs kNN requests of any Q, K, T as they arrive: a scheduler
+ * merges pending requests with the same (K, T) into batches (continuous
+ * batching) and hands each batch to a free slot (a search object with its own
+ * stream and worker thread), so batches overlap on the device. A batch is
+ * admitted when the device bytes of all slots stay within the memory budget;
+ * a request that alone exceeds it fails with CULSH_ERR_OUT_OF_MEMORY. Every
+ * request gets exactly the ids and distances it gets when searched alone.
+ * The index must not be rebuilt, reset or destroyed while a server uses it;
+ * its dataset must be on the device (after index(), or after one search with
+ * the dataset following a load()). */
+typedef struct culsh_server culsh_server;
+typedef struct culsh_server_config {
+    int slots;                /* batches on the device at once, 1..64 (0: 4)          */
+    int max_batch_queries;    /* queries merged into one batch (0: 8192)              */
+    long long memory_budget;  /* device bytes for all slots (0: 80% of free memory)   */
+} culsh_server_config;
+typedef struct culsh_server_stats {
+    long long requests;       /* completed requests (including failed ones)           */
+    long long queries;        /* queries of the requests that succeeded               */
+    long long batches;        /* device batches run                                   */
+    long long failed;         /* requests that ended with an error                    */
+    double wall_s;            /* first submission to last completion                  */
+    double qps;               /* queries / wall_s                                     */
+    double p50_ms, p99_ms;    /* request latency (submission to completion)           */
+    double mean_ms, max_ms;
+    int max_in_flight;        /* most batches on the device at once                   */
+    int slots;
+    long long peak_device_bytes;  /* most device bytes held by the slots              */
+    long long budget_bytes;
+} culsh_server_stats;
+
+int culsh_server_create(culsh_server** out, culsh_index* ix, const culsh_server_config* cfg);
+/* Queues Q queries (D x Q column-major host floats, as search()); results go
+ * to out_ids / out_dists (K x Q each, as getKnnIds / getKnnDistances). All
+ * three buffers must stay valid until culsh_server_wait reports completion. */
+int culsh_server_submit(culsh_server* srv, const float* queries, int Q, int K, int T, int* out_ids,
+                        float* out_dists, unsigned long long* ticket);
+/* Waits up to timeout_s seconds (< 0: no limit). Returns the request's status
+ * (its error message in culsh_last_error), or CULSH_PENDING on time-out; a
+ * completed ticket is forgotten after it is reported. */
+int culsh_server_wait(culsh_server* srv, unsigned long long ticket, double timeout_s);
+int culsh_server_stats_get(culsh_server* srv, culsh_server_stats* out);
+int culsh_server_stats_reset(culsh_server* srv);
+/* Completes every submitted request, then frees the server. */
+void culsh_server_destroy(culsh_server* srv);
 
 #ifdef __cplusplus
 }
