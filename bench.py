@@ -56,6 +56,9 @@ def parse_args(argv=None):
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-autotune", action="store_true", help="search with the default tuning")
+    p.add_argument("--serve-rates", default="1000,4000,16000",
+                   help="Poisson request rates (requests/s) for the serving measurement; empty to skip")
+    p.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per serving rate")
     return p.parse_args(argv)
 
 
@@ -260,6 +263,59 @@ def run_reference(args):
     return 0
 
 
+def serve_run(culsh, ht, pool, rate, seconds, Ks, Ts, seed, slots=4):
+    """Serving measurement: requests arrive as a Poisson process of the given
+    rate for `seconds`; each holds a log-uniform 1..4096 queries drawn from
+    `pool` with K and T uniform over Ks, Ts. One thread submits at the arrival
+    times, one collects results; latency is submission to completion."""
+    import threading
+    rng = np.random.default_rng(seed)
+    n = max(1, int(rng.poisson(rate * seconds)))
+    gaps = rng.exponential(1.0 / rate, n)
+    sizes = np.minimum(4096, np.floor(np.exp(rng.uniform(0.0, np.log(4097.0), n)))).astype(int)
+    starts = rng.integers(0, pool.shape[0] - 4096, n)
+    Kc = rng.choice(Ks, n)
+    Tc = rng.choice(Ts, n)
+    tickets = []
+    lock = threading.Condition()
+    errors = []
+    with culsh.Server(ht, slots=slots, max_batch_queries=8192) as srv:
+        def collector():
+            got = 0
+            while got < n:
+                with lock:
+                    while len(tickets) <= got:
+                        lock.wait()
+                    t = tickets[got]
+                try:
+                    srv.wait(t)
+                except Exception as e:  # noqa: BLE001 - reported in the JSON line
+                    errors.append(str(e))
+                got += 1
+        th = threading.Thread(target=collector)
+        th.start()
+        t0 = time.perf_counter()
+        due = t0
+        for i in range(n):
+            due += gaps[i]
+            while True:
+                now = time.perf_counter()
+                if now >= due:
+                    break
+                time.sleep(min(due - now, 0.0005))
+            q = pool[starts[i]: starts[i] + sizes[i]]
+            t = srv.submit(q, int(Kc[i]), int(Tc[i]))
+            with lock:
+                tickets.append(t)
+                lock.notify()
+        th.join()
+        st = srv.stats()
+    return {"rate_rps": rate, "requests": n, "queries": int(st["queries"]), "qps": round(st["qps"], 1),
+            "p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3), "mean_ms": round(st["mean_ms"], 3),
+            "batches": int(st["batches"]), "max_in_flight": int(st["max_in_flight"]),
+            "peak_device_mb": round(st["peak_device_bytes"] / 2**20, 1), "failed": int(st["failed"]) + len(errors)}
+
+
 def run_culsh(args):
     import torch
     rank, world, local_rank = dist_env()
@@ -383,6 +439,18 @@ def run_culsh(args):
                "path": "culsh_search_run (C ABI, pageable host buffers)"}
         del st_h, ht_h
 
+    serving = None
+    rates = [float(r) for r in args.serve_rates.split(",") if r.strip()]
+    if rates and rank == 0:
+        from culsh_gb300 import synth
+        pool = synth.dataset(args.config, n=16, q=max(65536, Q))[1]
+        Ks = sorted({K, 10, 100})
+        Ts = sorted({1, T})
+        serving = {"arrivals": "Poisson", "request_queries": "log-uniform 1..4096", "K": Ks, "T": Ts,
+                   "slots": 4, "index": "the resident index above",
+                   "runs": [serve_run(culsh, ht, pool, r, args.serve_seconds, Ks, Ts, seed=17 + i)
+                            for i, r in enumerate(rates)]}
+
     found = ids.cpu().numpy()
     ns = min(args.recall_sample, Q)
     rec = recall_at_k(found[:ns], X, Qm[:ns], K) if ns > 0 else None
@@ -404,7 +472,7 @@ def run_culsh(args):
                 "clocks": clk, "index_build_ms": round(statistics.median(build_ms), 3),
                 "index_build_stages_ms": {k: (round(v, 4) if isinstance(v, float) else v)
                                           for k, v in build_profile.items()},
-                "recall_at_k": rec, "recall_sample": ns,
+                "recall_at_k": rec, "recall_sample": ns, "serving": serving,
                 "selectivity": st.getSelectivity(), "candidates_unique_per_query": uniq / Q,
                 "candidates_nonunique_per_query": nonuniq / Q}
         print(json.dumps(line), flush=True)
