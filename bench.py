@@ -59,6 +59,8 @@ def parse_args(argv=None):
     p.add_argument("--serve-rates", default="1000,4000,16000",
                    help="Poisson request rates (requests/s) for the serving measurement; empty to skip")
     p.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per serving rate")
+    p.add_argument("--no-recall-point", action="store_true",
+                   help="skip the recall@10 >= 0.90 operating point (clustered 1M x 128, W chosen for recall)")
     return p.parse_args(argv)
 
 
@@ -316,6 +318,65 @@ def serve_run(culsh, ht, pool, rate, seconds, Ks, Ts, seed, slots=4):
             "peak_device_mb": round(st["peak_device_bytes"] / 2**20, 1), "failed": int(st["failed"]) + len(errors)}
 
 
+def recall_point(culsh, torch, dev, steps, warmup):
+    """Search throughput where LSH reaches recall@10 >= 0.90: the Gaussian-
+    mixture generator (100 centres ~N(0,10^2), unit noise) at 1M x 128, L=8,
+    M=8, T=16, K=10, with W=32 (the named W=4 leaves every held-out query
+    without candidates). FP32 and BF16 distance forms return identical
+    results; both are timed (device events, inputs resident, L2 flushed)."""
+    from culsh_gb300 import synth
+    X, Qm, _, _, cfg = synth.dataset(1, n=1_000_000, q=10_000)
+    N, D = X.shape
+    L, M, W, T, K, Q = 8, 8, 32.0, 16, 10, Qm.shape[0]
+    A, b = synth.projection(L, M, D, W, 3001)
+    Xt = torch.from_numpy(X).to(dev)
+    qt = torch.from_numpy(Qm).to(dev)
+    torch.cuda.synchronize()
+    stream = torch.cuda.Stream(dev)
+    sp = stream.cuda_stream
+    ht = culsh.HashTables()
+    ht.reset(N, D, L, M, W, A=A, b=b)
+    ht.index_device(Xt.data_ptr(), sp)
+    ids = torch.empty((Q, K), dtype=torch.int32, device=dev)
+    dists = torch.empty((Q, K), dtype=torch.float32, device=dev)
+    st = culsh.SearchTables()
+    st.reset(ht, K, T)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    forms = {}
+    ref = None
+    for name, bf in (("fp32", 0), ("bf16_rerank", 1)):
+        st.set_tuning(candidates_mode=1, distance_bf16=bf)
+        for _ in range(warmup):
+            st.search_device(qt.data_ptr(), Q, ids.data_ptr(), dists.data_ptr(), sp)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        cand = []
+        for i in range(steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(i & 0xFF)
+            ev[i][0].record(stream)
+            st.search_device(qt.data_ptr(), Q, ids.data_ptr(), dists.data_ptr(), sp)
+            ev[i][1].record(stream)
+            cand.append(st.profile()["candidates_ms"])
+        torch.cuda.synchronize()
+        ms = statistics.median(e0.elapsed_time(e1) for e0, e1 in ev)
+        out = ids.cpu().numpy()
+        if ref is None:
+            ref = out
+        pr = st.profile()
+        forms[name] = {"qps": round(Q / (ms / 1e3), 1), "ms_per_step": round(ms, 3),
+                       "candidates_ms": round(statistics.median(cand), 3), "rechecked_fp32": int(pr["rechecked"]),
+                       "identical_to_fp32": bool(np.array_equal(out, ref))}
+    uniq = st.getTotalCandidates_unique() / Q
+    # algorithmic gather bytes of the candidate stage: rows of the unique candidates
+    for name, f in forms.items():
+        row = 2 * D if name == "bf16_rerank" else 4 * D
+        f["candidate_gather_gbs"] = round(uniq * Q * row / (f["candidates_ms"] / 1e3) / 1e9, 1)
+    rec = recall_at_k(ref[:200], X, Qm[:200], K)
+    return {"workload": f"gauss-mixture-1m-d128 N={N} L={L} M={M} W={W} T={T} K={K} Q={Q}",
+            "recall_at_k": rec, "recall_sample": 200, "candidates_unique_per_query": round(uniq, 1),
+            "forms": forms}
+
+
 def run_culsh(args):
     import torch
     rank, world, local_rank = dist_env()
@@ -439,6 +500,10 @@ def run_culsh(args):
                "path": "culsh_search_run (C ABI, pageable host buffers)"}
         del st_h, ht_h
 
+    rpoint = None
+    if not args.no_recall_point and rank == 0:
+        rpoint = recall_point(culsh, torch, dev, max(3, min(args.steps, 10)), max(args.warmup, 3))
+
     serving = None
     rates = [float(r) for r in args.serve_rates.split(",") if r.strip()]
     if rates and rank == 0:
@@ -472,7 +537,7 @@ def run_culsh(args):
                 "clocks": clk, "index_build_ms": round(statistics.median(build_ms), 3),
                 "index_build_stages_ms": {k: (round(v, 4) if isinstance(v, float) else v)
                                           for k, v in build_profile.items()},
-                "recall_at_k": rec, "recall_sample": ns, "serving": serving,
+                "recall_at_k": rec, "recall_sample": ns, "recall_point": rpoint, "serving": serving,
                 "selectivity": st.getSelectivity(), "candidates_unique_per_query": uniq / Q,
                 "candidates_nonunique_per_query": nonuniq / Q}
         print(json.dumps(line), flush=True)

@@ -22,6 +22,10 @@
 #include <atomic>
 #include <cfloat>
 
+#include <cuda_bf16.h>
+
+#include <algorithm>
+
 #include "culsh_internal.cuh"
 #include "topk_common.cuh"
 
@@ -98,7 +102,7 @@ __global__ void __launch_bounds__(PT_PLAN) k_plan_items(WsArgs a) {
 
 // WT threads per item: WT / 32 warps each keep a sorted top-K list over a
 // strided share of the item's candidates (tuned: 64, 128 or 256).
-template <int WT>
+template <int WT, bool kBF16>
 __global__ void __launch_bounds__(WT) k_candidates_ws(WsArgs a) {
     constexpr int WW = WT / 32;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -115,7 +119,18 @@ __global__ void __launch_bounds__(WT) k_candidates_ws(WsArgs a) {
     uint32_t* wi_all = reinterpret_cast<uint32_t*>(wd_all + WW * K);
     float* wd = wd_all + warp * K;
     uint32_t* wi = wi_all + warp * K;
-    if (*(volatile unsigned int*)a.overflow) return;   // the plan did not fit
+    // BF16 form: approximate distance and error bound of each candidate.
+    float* dA = reinterpret_cast<float*>(wi_all + WW * K);
+    float* eA = dA + W_CAP;
+    __shared__ float s_tau;
+    __shared__ uint32_t s_scount, s_recheck, s_skip;
+    // Bit 0 of the overflow word: the plan did not fit (set by k_plan_items,
+    // which has finished). Read once and broadcast, so that the whole block
+    // returns or none of it does; bit 1 (a set overflow) may be raised by
+    // other blocks meanwhile and is left to the host.
+    if (tid == 0) s_skip = *(volatile unsigned int*)a.overflow & 1u;
+    __syncthreads();
+    if (s_skip) return;
     const unsigned int n_items = *a.n_items;
     const bool vec = (D & 3) == 0;
 
@@ -142,69 +157,223 @@ __global__ void __launch_bounds__(WT) k_candidates_ws(WsArgs a) {
         __syncthreads();
         uint32_t U = s_ucount;
         if (U > W_CAP) {   // the set overflowed: flag it, finish the protocol with no candidates
-            if (tid == 0) atomicAdd(a.overflow, 1u);
+            if (tid == 0) atomicOr(a.overflow, 2u);
             U = 0;
         }
 
-        // Distances in the reference lane order, per-warp sorted top-K.
+        // Exact FP32 distances in the reference lane order over list entries
+        // [0, cnt) (entry j is ulist[idx_of(j)]), into per-warp sorted top-K
+        // lists; an entry whose distance is already exact (pre) is not loaded.
         int n = 0;
         float thr_d = FLT_MAX;
         uint32_t thr_i = 0;
-        const int per = vec ? 16 : 4;
-        for (uint32_t base = warp * per; base < U; base += WW * per) {
-            float dist = 0.f;
-            uint32_t id = 0;
-            bool own;
-            if (vec) {
-                const uint32_t ci = base + (lane >> 1);
-                const int h = lane & 1;
-                const bool valid = ci < U;
-                id = valid ? ulist[ci] : 0u;
-                const float* rowp = a.X + (int64_t)id * D;
-                float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
-                if (valid) {
-                    for (int c = 4 * h; c < D; c += 8) {
-                        const float4 x = __ldg(reinterpret_cast<const float4*>(rowp + c));
-                        const float4 qv = *reinterpret_cast<const float4*>(qs + c);
-                        const float d0 = __fsub_rn(qv.x, x.x), d1 = __fsub_rn(qv.y, x.y);
-                        const float d2 = __fsub_rn(qv.z, x.z), d3 = __fsub_rn(qv.w, x.w);
-                        s0 = __fmaf_rn(d0, d0, s0);
-                        s1 = __fmaf_rn(d1, d1, s1);
-                        s2 = __fmaf_rn(d2, d2, s2);
-                        s3 = __fmaf_rn(d3, d3, s3);
+        auto fp32_pass = [&](uint32_t cnt, auto idx_of, auto pre) {
+            const int per = vec ? 16 : 4;
+            for (uint32_t base = warp * per; base < cnt; base += WW * per) {
+                float dist = 0.f;
+                uint32_t id = 0;
+                bool own;
+                if (vec) {
+                    const uint32_t j = base + (lane >> 1);
+                    const int h = lane & 1;
+                    bool valid = j < cnt;
+                    const uint32_t ci = valid ? idx_of(j) : 0u;
+                    id = valid ? ulist[ci] : 0u;
+                    float pd = 0.f;
+                    const bool have = valid && pre(ci, pd);
+                    const float* rowp = a.X + (int64_t)id * D;
+                    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+                    if (valid && !have) {
+                        for (int c = 4 * h; c < D; c += 8) {
+                            const float4 x = __ldg(reinterpret_cast<const float4*>(rowp + c));
+                            const float4 qv = *reinterpret_cast<const float4*>(qs + c);
+                            const float d0 = __fsub_rn(qv.x, x.x), d1 = __fsub_rn(qv.y, x.y);
+                            const float d2 = __fsub_rn(qv.z, x.z), d3 = __fsub_rn(qv.w, x.w);
+                            s0 = __fmaf_rn(d0, d0, s0);
+                            s1 = __fmaf_rn(d1, d1, s1);
+                            s2 = __fmaf_rn(d2, d2, s2);
+                            s3 = __fmaf_rn(d3, d3, s3);
+                        }
+                    }
+                    const float o0 = __shfl_xor_sync(0xffffffffu, s0, 1), o1 = __shfl_xor_sync(0xffffffffu, s1, 1);
+                    const float o2 = __shfl_xor_sync(0xffffffffu, s2, 1), o3 = __shfl_xor_sync(0xffffffffu, s3, 1);
+                    const float t0 = __fadd_rn(s0, o0), t1 = __fadd_rn(s1, o1), t2 = __fadd_rn(s2, o2),
+                                t3 = __fadd_rn(s3, o3);
+                    dist = have ? pd : __fadd_rn(__fadd_rn(t0, t2), __fadd_rn(t1, t3));
+                    own = valid && h == 0;
+                } else {
+                    const uint32_t j = base + (lane >> 3);
+                    const int r = lane & 7;
+                    const bool valid = j < cnt;
+                    const uint32_t ci = valid ? idx_of(j) : 0u;
+                    id = valid ? ulist[ci] : 0u;
+                    float pd = 0.f;
+                    const bool have = valid && pre(ci, pd);
+                    const float* rowp = a.X + (int64_t)id * D;
+                    float sacc = 0.f;
+                    if (valid && !have)
+                        for (int c = r; c < D; c += 8) {
+                            const float df = __fsub_rn(qs[c], __ldg(rowp + c));
+                            sacc = __fmaf_rn(df, df, sacc);
+                        }
+                    // every lane takes part in all three shuffles, whatever `have` is
+                    const float t = __fadd_rn(sacc, __shfl_xor_sync(0xffffffffu, sacc, 4));
+                    const float u = __fadd_rn(t, __shfl_xor_sync(0xffffffffu, t, 2));
+                    const float v = __fadd_rn(u, __shfl_xor_sync(0xffffffffu, u, 1));
+                    dist = have ? pd : v;
+                    own = valid && r == 0;
+                }
+                uint32_t want = __ballot_sync(0xffffffffu, own && lessp(dist, id, thr_d, thr_i));
+                while (want) {
+                    const int src = __ffs(want) - 1;
+                    want &= want - 1;
+                    const float cdv = __shfl_sync(0xffffffffu, dist, src);
+                    const uint32_t cid = __shfl_sync(0xffffffffu, id, src);
+                    if (lessp(cdv, cid, thr_d, thr_i)) warp_insert(wd, wi, n, K, cdv, cid, thr_d, thr_i);
+                }
+            }
+        };
+        if constexpr (!kBF16) {
+            fp32_pass(U, [](uint32_t j) { return j; }, [](uint32_t, float&) { return false; });
+        } else {
+            // Pass 1: BF16 rows. d~ is computed in the reference lane order
+            // from the bf16 copy; E bounds |d~ - d| where d is the FP32
+            // distance (exact rows: E = 0, since d~ is then d itself; rows
+            // with extreme magnitudes: E = inf). Each warp keeps the K
+            // smallest upper ends d~ + E; tau, the K-th smallest over the
+            // item, caps the distance of its K nearest, so only candidates
+            // with d~ - E <= tau can be among them.
+            const int per = vec ? 16 : 4;
+            for (uint32_t base = warp * per; base < U; base += WW * per) {
+                float dt = 0.f, b1 = 0.f, b2 = 0.f;
+                uint32_t ci, id;
+                bool own;
+                if (vec) {
+                    ci = base + (lane >> 1);
+                    const int h = lane & 1;
+                    const bool valid = ci < U;
+                    id = valid ? ulist[ci] : 0u;
+                    const uint16_t* rowp = a.xb + (int64_t)id * D;
+                    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+                    if (valid) {
+                        for (int c = 4 * h; c < D; c += 8) {
+                            const uint2 raw = __ldg(reinterpret_cast<const uint2*>(rowp + c));
+                            const float x0 = __uint_as_float(raw.x << 16), x1 = __uint_as_float(raw.x & 0xFFFF0000u);
+                            const float x2 = __uint_as_float(raw.y << 16), x3 = __uint_as_float(raw.y & 0xFFFF0000u);
+                            const float4 qv = *reinterpret_cast<const float4*>(qs + c);
+                            const float d0 = __fsub_rn(qv.x, x0), d1 = __fsub_rn(qv.y, x1);
+                            const float d2 = __fsub_rn(qv.z, x2), d3 = __fsub_rn(qv.w, x3);
+                            s0 = __fmaf_rn(d0, d0, s0);
+                            s1 = __fmaf_rn(d1, d1, s1);
+                            s2 = __fmaf_rn(d2, d2, s2);
+                            s3 = __fmaf_rn(d3, d3, s3);
+                            b1 = __fmaf_rn(fabsf(x0), fabsf(d0), b1);
+                            b1 = __fmaf_rn(fabsf(x1), fabsf(d1), b1);
+                            b1 = __fmaf_rn(fabsf(x2), fabsf(d2), b1);
+                            b1 = __fmaf_rn(fabsf(x3), fabsf(d3), b1);
+                            b2 = __fmaf_rn(x0, x0, b2);
+                            b2 = __fmaf_rn(x1, x1, b2);
+                            b2 = __fmaf_rn(x2, x2, b2);
+                            b2 = __fmaf_rn(x3, x3, b2);
+                        }
+                    }
+                    const float o0 = __shfl_xor_sync(0xffffffffu, s0, 1), o1 = __shfl_xor_sync(0xffffffffu, s1, 1);
+                    const float o2 = __shfl_xor_sync(0xffffffffu, s2, 1), o3 = __shfl_xor_sync(0xffffffffu, s3, 1);
+                    const float t0 = __fadd_rn(s0, o0), t1 = __fadd_rn(s1, o1), t2 = __fadd_rn(s2, o2),
+                                t3 = __fadd_rn(s3, o3);
+                    dt = __fadd_rn(__fadd_rn(t0, t2), __fadd_rn(t1, t3));
+                    b1 = __fadd_rn(b1, __shfl_xor_sync(0xffffffffu, b1, 1));
+                    b2 = __fadd_rn(b2, __shfl_xor_sync(0xffffffffu, b2, 1));
+                    own = valid && h == 0;
+                } else {
+                    ci = base + (lane >> 3);
+                    const int r = lane & 7;
+                    const bool valid = ci < U;
+                    id = valid ? ulist[ci] : 0u;
+                    const uint16_t* rowp = a.xb + (int64_t)id * D;
+                    float sacc = 0.f;
+                    if (valid)
+                        for (int c = r; c < D; c += 8) {
+                            const float x = __uint_as_float((uint32_t)__ldg(rowp + c) << 16);
+                            const float df = __fsub_rn(qs[c], x);
+                            sacc = __fmaf_rn(df, df, sacc);
+                            b1 = __fmaf_rn(fabsf(x), fabsf(df), b1);
+                            b2 = __fmaf_rn(x, x, b2);
+                        }
+                    const float t = __fadd_rn(sacc, __shfl_xor_sync(0xffffffffu, sacc, 4));
+                    const float u = __fadd_rn(t, __shfl_xor_sync(0xffffffffu, t, 2));
+                    dt = __fadd_rn(u, __shfl_xor_sync(0xffffffffu, u, 1));
+#pragma unroll
+                    for (int o = 4; o > 0; o >>= 1) {
+                        b1 = __fadd_rn(b1, __shfl_xor_sync(0xffffffffu, b1, o));
+                        b2 = __fadd_rn(b2, __shfl_xor_sync(0xffffffffu, b2, o));
+                    }
+                    own = valid && r == 0;
+                }
+                float e = 0.f, up = 0.f;
+                if (own) {
+                    const uint8_t fl = __ldg(a.xflag + id);
+                    if (fl == 1) {
+                        e = 0.f;
+                    } else if (fl == 2 || !(dt <= FLT_MAX)) {
+                        e = __int_as_float(0x7f800000);
+                    } else {
+                        // E = c1 * d~ + c2 * (2 rho b1 + rho^2 b2), upward roundings
+                        const float rho = 0.00393676758f;   // 2^-8 (1 + 2^-7), bf16 rounding relative to |x~|
+                        const float delta = __fmaf_ru(rho * rho, b2, __fmul_ru(2.0f * rho, b1));
+                        e = __fmaf_ru(a.e_c1, dt, __fmul_ru(a.e_c2, delta));
+                    }
+                    dA[ci] = dt;
+                    eA[ci] = e;
+                    up = __fadd_ru(dt, e);
+                }
+                uint32_t want = __ballot_sync(0xffffffffu, own && lessp(up, ci, thr_d, thr_i));
+                while (want) {
+                    const int src = __ffs(want) - 1;
+                    want &= want - 1;
+                    const float cdv = __shfl_sync(0xffffffffu, up, src);
+                    const uint32_t cid = __shfl_sync(0xffffffffu, ci, src);
+                    if (lessp(cdv, cid, thr_d, thr_i)) warp_insert(wd, wi, n, K, cdv, cid, thr_d, thr_i);
+                }
+            }
+            if (lane == 0) s_wn[warp] = n;
+            if (tid == 0) s_scount = s_recheck = 0;
+            __syncthreads();
+            if (warp == 0) {
+                for (int w = 1; w < WW; ++w) {
+                    const int nw = s_wn[w];
+                    for (int e = 0; e < nw; ++e) {
+                        const float d = wd_all[w * K + e];
+                        const uint32_t id = wi_all[w * K + e];
+                        if (!lessp(d, id, thr_d, thr_i)) break;
+                        warp_insert(wd, wi, n, K, d, id, thr_d, thr_i);
                     }
                 }
-                const float o0 = __shfl_xor_sync(0xffffffffu, s0, 1), o1 = __shfl_xor_sync(0xffffffffu, s1, 1);
-                const float o2 = __shfl_xor_sync(0xffffffffu, s2, 1), o3 = __shfl_xor_sync(0xffffffffu, s3, 1);
-                const float t0 = __fadd_rn(s0, o0), t1 = __fadd_rn(s1, o1), t2 = __fadd_rn(s2, o2),
-                            t3 = __fadd_rn(s3, o3);
-                dist = __fadd_rn(__fadd_rn(t0, t2), __fadd_rn(t1, t3));
-                own = valid && h == 0;
-            } else {
-                const uint32_t ci = base + (lane >> 3);
-                const int r = lane & 7;
-                const bool valid = ci < U;
-                id = valid ? ulist[ci] : 0u;
-                const float* rowp = a.X + (int64_t)id * D;
-                float s = 0.f;
-                if (valid)
-                    for (int c = r; c < D; c += 8) {
-                        const float df = __fsub_rn(qs[c], __ldg(rowp + c));
-                        s = __fmaf_rn(df, df, s);
-                    }
-                const float t = __fadd_rn(s, __shfl_xor_sync(0xffffffffu, s, 4));
-                const float u = __fadd_rn(t, __shfl_xor_sync(0xffffffffu, t, 2));
-                dist = __fadd_rn(u, __shfl_xor_sync(0xffffffffu, u, 1));
-                own = valid && r == 0;
+                if (lane == 0) s_tau = n == K ? wd[K - 1] : __int_as_float(0x7f800000);
             }
-            uint32_t want = __ballot_sync(0xffffffffu, own && lessp(dist, id, thr_d, thr_i));
-            while (want) {
-                const int src = __ffs(want) - 1;
-                want &= want - 1;
-                const float cdv = __shfl_sync(0xffffffffu, dist, src);
-                const uint32_t cid = __shfl_sync(0xffffffffu, id, src);
-                if (lessp(cdv, cid, thr_d, thr_i)) warp_insert(wd, wi, n, K, cdv, cid, thr_d, thr_i);
-            }
+            __syncthreads();
+            // Shortlist (into the free hash-set memory): d~ - E <= tau.
+            const float tau = s_tau;
+            uint32_t* slist = hset;
+            uint32_t rc = 0;
+            for (uint32_t ci = tid; ci < U; ci += WT)
+                if (__fsub_rd(dA[ci], eA[ci]) <= tau) {
+                    slist[atomicAdd(&s_scount, 1u)] = ci;
+                    rc += eA[ci] != 0.f;
+                }
+            if (rc) atomicAdd(&s_recheck, rc);
+            __syncthreads();
+            if (tid == 0 && s_recheck) atomicAdd(a.rechecked, (unsigned long long)s_recheck);
+            // Pass 2: exact distances of the shortlist (re-read in FP32 only
+            // for rows whose bf16 copy is inexact).
+            n = 0;
+            thr_d = FLT_MAX;
+            thr_i = 0;
+            fp32_pass(s_scount, [&](uint32_t j) { return slist[j]; }, [&](uint32_t ci, float& d) {
+                if (eA[ci] != 0.f) return false;
+                d = dA[ci];
+                return true;
+            });
         }
         if (lane == 0) s_wn[warp] = n;
         __syncthreads();
@@ -281,9 +450,9 @@ __global__ void __launch_bounds__(WT) k_candidates_ws(WsArgs a) {
 
 }  // namespace
 
-size_t ws_smem_bytes(int D, int K, int wt) {
+size_t ws_smem_bytes(int D, int K, int wt, int bf16) {
     return sizeof(float) * (size_t)((D + 3) & ~3) + sizeof(uint32_t) * (W_SLOTS + W_CAP) +
-           (size_t)(wt / 32) * K * (sizeof(float) + sizeof(uint32_t));
+           (size_t)(wt / 32) * K * (sizeof(float) + sizeof(uint32_t)) + (bf16 ? 2 * sizeof(float) * W_CAP : 0);
 }
 
 cudaError_t launch_plan_items(const WsArgs& a, cudaStream_t st) {
@@ -293,43 +462,87 @@ cudaError_t launch_plan_items(const WsArgs& a, cudaStream_t st) {
 }
 
 namespace {
-template <int WT>
+template <int WT, bool kBF16>
 cudaError_t launch_ws_v(const WsArgs& a, int grid, cudaStream_t st) {
-    const size_t smem = ws_smem_bytes(a.D, a.K, WT);
+    const size_t smem = ws_smem_bytes(a.D, a.K, WT, kBF16);
     static std::atomic<size_t> configured{0};   // largest dynamic shared memory opted into
     if (smem > 48 * 1024 && smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_candidates_ws<WT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e =
+            cudaFuncSetAttribute(k_candidates_ws<WT, kBF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         configured = smem;
     }
-    k_candidates_ws<WT><<<grid, WT, smem, st>>>(a);
+    k_candidates_ws<WT, kBF16><<<grid, WT, smem, st>>>(a);
     return cudaGetLastError();
 }
 
-template <int WT>
+template <int WT, bool kBF16>
 int ws_bps_v(int D, int K) {
     int n = 0;
-    const size_t smem = ws_smem_bytes(D, K, WT);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_candidates_ws<WT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_candidates_ws<WT>, WT, smem) != cudaSuccess) n = 1;
+    const size_t smem = ws_smem_bytes(D, K, WT, kBF16);
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(k_candidates_ws<WT, kBF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_candidates_ws<WT, kBF16>, WT, smem) != cudaSuccess) n = 1;
     return n > 0 ? n : 1;
+}
+
+template <bool kBF16>
+cudaError_t launch_ws_w(const WsArgs& a, int grid, cudaStream_t st) {
+    switch (a.wt) {
+        case 64: return launch_ws_v<64, kBF16>(a, grid, st);
+        case 256: return launch_ws_v<256, kBF16>(a, grid, st);
+        default: return launch_ws_v<128, kBF16>(a, grid, st);
+    }
+}
+
+template <bool kBF16>
+int ws_bps_w(int D, int K, int wt) {
+    switch (wt) {
+        case 64: return ws_bps_v<64, kBF16>(D, K);
+        case 256: return ws_bps_v<256, kBF16>(D, K);
+        default: return ws_bps_v<128, kBF16>(D, K);
+    }
+}
+
+// BF16 copy of the dataset (round to nearest even) and a per-row flag:
+// 1 when every element is exact in bf16, 2 when a nonzero element has a
+// magnitude outside [2^-100, 2^100] (the search then always re-checks the
+// row in FP32), 0 otherwise. One warp per row.
+__global__ void k_bf16_rows(const float* __restrict__ X, int64_t N, int D, uint16_t* __restrict__ xb,
+                            uint8_t* __restrict__ flag) {
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = w0; r < N; r += nw) {
+        bool exact = true, special = false;
+        for (int d = lane; d < D; d += 32) {
+            const float x = __ldg(X + r * D + d);
+            const uint16_t h = __bfloat16_as_ushort(__float2bfloat16_rn(x));
+            xb[r * D + d] = h;
+            exact &= __uint_as_float((uint32_t)h << 16) == x;
+            const float ax = fabsf(x);
+            special |= x != 0.0f && !(ax >= 7.88860905e-31f && ax <= 1.26765060e30f);
+        }
+        exact = __all_sync(0xffffffffu, exact);
+        special = __any_sync(0xffffffffu, special);
+        if (lane == 0) flag[r] = special ? 2 : (exact ? 1 : 0);
+    }
 }
 }  // namespace
 
 cudaError_t launch_candidates_ws(const WsArgs& a, int grid, cudaStream_t st) {
-    switch (a.wt) {
-        case 64: return launch_ws_v<64>(a, grid, st);
-        case 256: return launch_ws_v<256>(a, grid, st);
-        default: return launch_ws_v<128>(a, grid, st);
-    }
+    return a.bf16 ? launch_ws_w<true>(a, grid, st) : launch_ws_w<false>(a, grid, st);
 }
 
-int ws_blocks_per_sm(int D, int K, int wt) {
-    switch (wt) {
-        case 64: return ws_bps_v<64>(D, K);
-        case 256: return ws_bps_v<256>(D, K);
-        default: return ws_bps_v<128>(D, K);
-    }
+int ws_blocks_per_sm(int D, int K, int wt, int bf16) {
+    return bf16 ? ws_bps_w<true>(D, K, wt) : ws_bps_w<false>(D, K, wt);
+}
+
+cudaError_t launch_bf16_rows(const float* X, int64_t N, int D, uint16_t* xb, uint8_t* flag, cudaStream_t st) {
+    if (N <= 0) return cudaSuccess;
+    const int64_t warps = std::min<int64_t>(N, 152 * 64);
+    k_bf16_rows<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(X, N, D, xb, flag);
+    return cudaGetLastError();
 }
 
 }  // namespace culsh

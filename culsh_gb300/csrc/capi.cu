@@ -134,6 +134,9 @@ struct culsh_index {
     const float* x_borrow = nullptr;
     DevBuf<float> dA, db;
     bool proj_on_dev = false;
+    DevBuf<uint16_t> xb;    // bf16 copy of the device dataset (search precision form), built on first use
+    DevBuf<uint8_t> xflag;  // per row: 1 exact in bf16, 2 always re-check in FP32, 0 bound applies
+    bool xb_valid = false;
     int KW = 1;
     std::vector<int32_t> h_cmin, h_cmax;
     std::vector<uint8_t> h_fbits;
@@ -181,6 +184,7 @@ struct SearchTune {
     int ws_wt = 128;       // threads per work item (64, 128, 256)
     int ws_bps = 0;        // resident work-stealing CTAs per SM (0: occupancy limit)
     int ws_chunk = 1024;   // non-unique candidates per id partition
+    int dist_bf16 = 0;     // 1: BF16 candidate distances + certified FP32 rerank (work-stealing form)
 };
 constexpr size_t kPlanBytes = 1024;   // room for the graph key (checked below)
 
@@ -206,6 +210,7 @@ struct culsh_search {
     DevBuf<float> part_d;
     DevBuf<uint32_t> part_i;
     int sms = 0, ws_used = 0, ws_overflow = 0;
+    long long rechecked = 0;   // BF16 form: candidates re-read in FP32 by the last search
     SearchTune tune;
     bool use_graphs = true;
     cudaGraphExec_t gexec = nullptr;     // cached search graph and the plan it was captured from
@@ -253,6 +258,7 @@ void clear_index_state(culsh_index* ix) {
     ix->x_src = nullptr;
     ix->x_borrow = nullptr;
     ix->proj_on_dev = false;
+    ix->xb_valid = false;
 }
 
 int upload_projection(culsh_index* ix, cudaStream_t st) {
@@ -735,7 +741,8 @@ static_assert(sizeof(SearchPlan) <= kPlanBytes, "graph key buffer too small");
 
 // Sizes every buffer of a search of Q queries and fills the plan. Allocates
 // (when buffers grow) but launches nothing.
-int plan_search(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* d_d, SearchPlan* out) {
+int plan_search(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* d_d, cudaStream_t st,
+                SearchPlan* out) {
     culsh_index* ix = s->ix;
     const int L = ix->L, M = ix->M, D = ix->D, K = s->K, T = s->T, LM = L * M;
     const float* dX = ix->dev_x();
@@ -824,7 +831,18 @@ int plan_search(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* 
             CU_TRY(cudaGetDevice(&dev));
             CU_TRY(cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, dev));
         }
-        const int occ = ws_blocks_per_sm(D, K, tu.ws_wt);
+        const int bf16 = tu.dist_bf16 ? 1 : 0;
+        if (bf16 && !ix->xb_valid) {
+            // The bf16 copy and row flags, made once per dataset. The stream
+            // is drained before the copy is published: searches on other
+            // streams read it as soon as they see it.
+            CU_TRY(ix->xb.reserve((size_t)ix->N * D));
+            CU_TRY(ix->xflag.reserve((size_t)ix->N));
+            CU_TRY(launch_bf16_rows(dX, ix->N, D, ix->xb.p, ix->xflag.p, st));
+            CU_TRY(cudaStreamSynchronize(st));
+            ix->xb_valid = true;
+        }
+        const int occ = ws_blocks_per_sm(D, K, tu.ws_wt, bf16);
         const int bps = tu.ws_bps > 0 ? std::min(tu.ws_bps, occ) : occ;
         P.ws_grid = s->sms * bps;
         WsArgs& a = P.wa;
@@ -861,6 +879,20 @@ int plan_search(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* 
         a.overflow = reinterpret_cast<unsigned int*>(s->stats.p + 4) + 1;
         a.n_items = reinterpret_cast<unsigned int*>(s->stats.p + 5);
         a.wt = tu.ws_wt;
+        a.bf16 = bf16;
+        if (bf16) {
+            // |d~ - d| <= c1 d~ + c2 (2 rho b1 + rho^2 b2) with gamma_n = n u / (1 - n u),
+            // n = ceil(D/8) + 6 roundings along any path, u = 2^-24:
+            // c1 = 2 gamma / (1 - gamma), c2 = (1 + gamma) / (1 - gamma), both
+            // rounded up with a 2^-20 margin for the bound's own evaluation.
+            const double u = std::ldexp(1.0, -24), nn = (double)((D + 7) / 8 + 6);
+            const double g = nn * u / (1.0 - nn * u), margin = 1.0 + std::ldexp(1.0, -20);
+            a.xb = ix->xb.p;
+            a.xflag = ix->xflag.p;
+            a.e_c1 = std::nextafter((float)(2.0 * g / (1.0 - g) * margin), INFINITY);
+            a.e_c2 = std::nextafter((float)((1.0 + g) / (1.0 - g) * margin), INFINITY);
+            a.rechecked = s->stats.p + 6;
+        }
     }
     P.stats = s->stats.p;
     P.h_stats = s->h_stats.p;
@@ -1020,6 +1052,7 @@ int finish_search(culsh_search* s, const SearchPlan& P, cudaStream_t st) {
     }
     s->tot_unique = s->h_stats.p[0];
     s->tot_nonunique = s->h_stats.p[1];
+    s->rechecked = P.use_ws && P.wa.bf16 && !s->ws_overflow ? (long long)s->h_stats.p[6] : 0;
     return CULSH_OK;
 }
 
@@ -1031,7 +1064,7 @@ int search_device(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float
     SearchPlan P;
     {
         std::lock_guard<std::mutex> lk(alloc_capture_mutex());
-        TRY(plan_search(s, dQ, Q, d_ids, d_d, &P));
+        TRY(plan_search(s, dQ, Q, d_ids, d_d, st, &P));
         s->host_copy_timed = false;
         TRY(run_plan(s, P, st));
     }
@@ -1242,6 +1275,7 @@ int culsh_index_load(culsh_index* ix, const char* path, FILE* dbg) {
     }
     ix->indexed = ix->host_valid = true;
     ix->dev_valid = false;
+    ix->xb_valid = false;
     if (dbg)
         fprintf(dbg, "[HashTables::load]\tIndexing structure loaded from file \"%s\", (N, D, L, M, W) = (%d, %d, %d, %d, %.2f)\n",
                 path, N, D, L, M, W);
@@ -1365,6 +1399,7 @@ int culsh_search_run(culsh_search* s, const float* queries, int Q, const float* 
         CU_TRY(ix->X.reserve((size_t)ix->N * ix->D));
         CU_TRY(cudaMemcpyAsync(ix->X.p, dataset, sizeof(float) * (size_t)ix->N * ix->D, cudaMemcpyHostToDevice, st));
         ix->x_src = dataset;
+        ix->xb_valid = false;
     }
     if (!ix->dev_x()) return fail(CULSH_ERR_INVALID_ARGUMENT, "null dataset and no dataset on the device");
     const int D = ix->D, K = s->K;
@@ -1482,6 +1517,7 @@ static void tune_to_c(const SearchTune& t, culsh_tuning* o) {
     o->ws_threads = t.ws_wt;
     o->ws_blocks_per_sm = t.ws_bps;
     o->ws_chunk = t.ws_chunk;
+    o->distance_bf16 = t.dist_bf16;
 }
 
 int culsh_search_get_tuning(culsh_search* s, culsh_tuning* out) {
@@ -1498,7 +1534,7 @@ int culsh_search_set_tuning(culsh_search* s, const culsh_tuning* in) {
                     (in->candidates_mode == 0 || in->candidates_mode == 1) &&
                     (in->ws_threads == 64 || in->ws_threads == 128 || in->ws_threads == 256) &&
                     in->ws_blocks_per_sm >= 0 && in->ws_blocks_per_sm <= 64 && in->ws_chunk >= 64 &&
-                    in->ws_chunk <= 65536;
+                    in->ws_chunk <= 65536 && (in->distance_bf16 == 0 || in->distance_bf16 == 1);
     if (!ok) return fail(CULSH_ERR_INVALID_ARGUMENT, "tuning value out of range");
     s->tune.proj_tile = in->proj_tile;
     s->tune.probe_pch = in->probe_batch;
@@ -1506,6 +1542,7 @@ int culsh_search_set_tuning(culsh_search* s, const culsh_tuning* in) {
     s->tune.ws_wt = in->ws_threads;
     s->tune.ws_bps = in->ws_blocks_per_sm;
     s->tune.ws_chunk = in->ws_chunk;
+    s->tune.dist_bf16 = in->distance_bf16;
     return CULSH_OK;
 }
 
@@ -1602,15 +1639,17 @@ int culsh_search_autotune(culsh_search* s, const float* d_queries, int Q, int* d
         t.cand_ws = 0;
         cands.push_back(t);
         const int wts[3] = {64, 128, 256}, chunks[3] = {512, 1024, 2048};
-        for (int a = 0; a < 3; ++a)
-            for (int b = 0; b < 3; ++b) {
-                SearchTune u = best;
-                u.cand_ws = 1;
-                u.ws_wt = wts[a];
-                u.ws_chunk = chunks[b];
-                u.ws_bps = 0;
-                cands.push_back(u);
-            }
+        for (int f = 0; f < 2; ++f)
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) {
+                    SearchTune u = best;
+                    u.cand_ws = 1;
+                    u.ws_wt = wts[a];
+                    u.ws_chunk = chunks[b];
+                    u.ws_bps = 0;
+                    u.dist_bf16 = f;
+                    cands.push_back(u);
+                }
     }
     bool first = true;
     for (const SearchTune& t : cands) {
@@ -1627,7 +1666,7 @@ int culsh_search_autotune(culsh_search* s, const float* d_queries, int Q, int* d
         }
     }
     if (best.cand_ws) {   // residency: half the occupancy limit as well
-        const int occ = ws_blocks_per_sm(s->ix->D, s->K, best.ws_wt);
+        const int occ = ws_blocks_per_sm(s->ix->D, s->K, best.ws_wt, best.dist_bf16);
         if (occ > 1) {
             SearchTune t = best;
             t.ws_bps = occ / 2;
@@ -1698,6 +1737,7 @@ int culsh_search_profile_get(culsh_search* s, culsh_search_profile* out) {
     out->key_words = s->ix ? s->ix->KW : 0;
     out->candidates_mode = s->ws_used ? (s->ws_overflow ? 2 : 1) : 0;
     out->graph_mode = s->graph_mode;
+    out->rechecked = s->rechecked;
     return CULSH_OK;
 }
 

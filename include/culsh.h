@@ -140,6 +140,9 @@ typedef struct culsh_tuning {
     int ws_threads;       /* work-stealing threads per item: 64, 128, 256               */
     int ws_blocks_per_sm; /* resident work-stealing CTAs per SM, 0 = occupancy limit     */
     int ws_chunk;         /* non-unique candidates per id partition (64 .. 65536)        */
+    int distance_bf16;    /* 1: candidate distances from a bf16 copy of the dataset, then
+                             an exact FP32 rerank of every candidate the proven error
+                             bound cannot exclude (same results as 0)                  */
     float search_ms;      /* culsh_search_autotune: median device ms of the choice       */
     int configs_tried;    /* culsh_search_autotune: configurations timed                 */
 } culsh_tuning;
@@ -187,6 +190,7 @@ typedef struct culsh_search_profile {
                             grid over id partitions; 2: work-stealing, re-run
                             per query after a partition overflowed            */
     int graph_mode;      /* 0: direct launches; 1: graph captured; 2: replayed */
+    long long rechecked; /* BF16 distance form: candidates re-read in FP32     */
 } culsh_search_profile;
 int culsh_search_profile_get(culsh_search* s, culsh_search_profile* out);
 

@@ -83,16 +83,71 @@ def test_every_tuning_configuration(culsh, name):
     st.search(c["queries"], dataset=c["X"])
     check_search(st, c)
     assert st.profile()["candidates_mode"] == 0
-    for wt, chunk, bps in itertools.product((64, 128, 256), (64, 1024, 4096), (0, 1)):
-        st.set_tuning(candidates_mode=1, ws_threads=wt, ws_chunk=chunk, ws_blocks_per_sm=bps)
+    for wt, chunk, bps, bf in itertools.product((64, 128, 256), (64, 1024, 4096), (0, 1), (0, 1)):
+        st.set_tuning(candidates_mode=1, ws_threads=wt, ws_chunk=chunk, ws_blocks_per_sm=bps, distance_bf16=bf)
         st.search(c["queries"], dataset=c["X"])
         check_search(st, c)
         np.testing.assert_array_equal(st.getKnnDistances(), c["knn_dists"])
 
 
+@pytest.mark.parametrize("name", ["int_dups", "mix_d16_t8", "odd_d13", "heavy", "m40_t70", "single_bucket",
+                                  "k_gt_cand"])
+def test_bf16_distance_form_is_exact(culsh, name):
+    """BF16 candidate distances + certified FP32 rerank return exactly the
+    FP32 form's results. Integer data are exact in bf16, so nothing is
+    re-read in FP32 there."""
+    c = load_case(name)
+    ht = build_index(culsh, c)
+    st = culsh.SearchTables()
+    st.reset(ht, int(c["K"]), int(c["T"]))
+    st.set_tuning(candidates_mode=1, distance_bf16=1)
+    st.search(c["queries"], dataset=c["X"])
+    check_search(st, c)
+    np.testing.assert_array_equal(st.getKnnDistances(), c["knn_dists"])
+    pr = st.profile()
+    assert pr["candidates_mode"] == 1
+    if np.array_equal(c["X"], np.round(c["X"])) and np.abs(c["X"]).max() <= 256:
+        assert pr["rechecked"] == 0
+    assert pr["rechecked"] <= st.getTotalCandidates_unique()
+
+
+def test_bf16_form_extreme_magnitudes_and_ties(culsh):
+    """Rows with nonzero magnitudes below 2^-100 (whole rows, or a few
+    entries of a row) are always re-read in FP32; many exact distance ties
+    (duplicated rows, distances that underflow to 0); both forms agree with
+    the oracle. (Magnitudes above 2^100 cannot be indexed: their codes leave
+    the int32 range.)"""
+    import oracle
+    rng = np.random.default_rng(3)
+    N, D, L, M, W = 3000, 16, 4, 3, 30.0
+    X = rng.normal(0, 2, (N, D)).astype(np.float32)
+    X[:40] = np.float32(1e-35) * rng.normal(0, 1, (40, D)).astype(np.float32)
+    X[40:80, :4] = np.float32(1e-33) * rng.normal(0, 1, (40, 4)).astype(np.float32)
+    X[80:400] = X[400:720]                     # duplicated rows: exact ties
+    X[720:1000] = np.round(X[720:1000] * 4) / 4  # exact in bf16
+    A = rng.normal(0, 1, (L, M, D)).astype(np.float32)
+    b = rng.uniform(0, W, (L, M)).astype(np.float32)
+    queries = np.concatenate([X[:5] * 3, X[400:420] + 0.01, X[720:730], X[40:45] * 0.5]).astype(np.float32)
+    K, T = 12, 4
+    ht = culsh.HashTables()
+    ht.reset(N, D, L, M, W, A=A, b=b)
+    ht.index(X)
+    ref = oracle.search(oracle.build_index(X, A, b, W), X, queries, K, T)
+    st = culsh.SearchTables()
+    st.reset(ht, K, T)
+    for bf in (0, 1):
+        st.set_tuning(candidates_mode=1, distance_bf16=bf)
+        st.search(queries, dataset=X)
+        np.testing.assert_array_equal(st.getKnnIds(), ref["knn_ids"])
+        np.testing.assert_array_equal(st.getKnnDistances(), ref["knn_dists"])
+        if bf:
+            assert st.profile()["rechecked"] > 0
+
+
 def test_tuning_rejects_out_of_range(culsh):
     st = culsh.SearchTables()
-    for bad in ({"probe_batch": 3}, {"proj_tile": 5}, {"ws_threads": 96}, {"ws_chunk": 8}, {"candidates_mode": 2}):
+    for bad in ({"probe_batch": 3}, {"proj_tile": 5}, {"ws_threads": 96}, {"ws_chunk": 8}, {"candidates_mode": 2},
+                {"distance_bf16": 2}):
         with pytest.raises(culsh.CulshError) as ei:
             st.set_tuning(**bad)
         assert ei.value.code == culsh.ERR_INVALID_ARGUMENT
@@ -112,7 +167,8 @@ def test_autotune_keeps_results(culsh):
     st.reset(ht, K, T)
     side = torch.cuda.Stream()
     tune = st.autotune(q.data_ptr(), q.shape[0], ids.data_ptr(), d.data_ptr(), side.cuda_stream)
-    assert tune["configs_tried"] >= 16 and tune["search_ms"] > 0
+    assert tune["configs_tried"] >= 25 and tune["search_ms"] > 0
+    assert tune["distance_bf16"] in (0, 1)
     assert tune["probe_batch"] in (1, 2, 4) and tune["ws_threads"] in (64, 128, 256)
     assert st.get_tuning()["probe_batch"] == tune["probe_batch"]
     torch.cuda.synchronize()

@@ -328,3 +328,8 @@ def test_work_stealing_large_candidate_sets(culsh):
     assert st.getTotalCandidates_unique() == int(ref["unique"].sum())
     assert st.getTotalCandidates_nonUnique() == int(ref["nonunique"].sum())
     assert int(ref["unique"][:5].min()) > 60000 and int(ref["nonunique"][5:8].max()) == 0
+    st.set_tuning(distance_bf16=1)
+    st.search(queries, dataset=X)
+    np.testing.assert_array_equal(st.getKnnIds(), ref["knn_ids"])
+    np.testing.assert_array_equal(st.getKnnDistances(), ref["knn_dists"])
+    assert st.profile()["rechecked"] < st.getTotalCandidates_unique() // 10
