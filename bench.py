@@ -61,6 +61,8 @@ def parse_args(argv=None):
     p.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per serving rate")
     p.add_argument("--no-recall-point", action="store_true",
                    help="skip the recall@10 >= 0.90 operating point (clustered 1M x 128, W chosen for recall)")
+    p.add_argument("--recall-point-only", action="store_true",
+                   help="run only the recall operating point and print its JSON (profiling)")
     return p.parse_args(argv)
 
 
@@ -318,7 +320,7 @@ def serve_run(culsh, ht, pool, rate, seconds, Ks, Ts, seed, slots=4):
             "peak_device_mb": round(st["peak_device_bytes"] / 2**20, 1), "failed": int(st["failed"]) + len(errors)}
 
 
-def recall_point(culsh, torch, dev, steps, warmup):
+def recall_point(culsh, torch, dev, steps, warmup, autotune=True):
     """Search throughput where LSH reaches recall@10 >= 0.90: the Gaussian-
     mixture generator (100 centres ~N(0,10^2), unit noise) at 1M x 128, L=8,
     M=8, T=16, K=10, with W=32 (the named W=4 leaves every held-out query
@@ -344,6 +346,9 @@ def recall_point(culsh, torch, dev, steps, warmup):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     forms = {}
     ref = None
+    tuned = None
+    if autotune:   # untimed; the tuner may pick either distance form, both are timed below
+        tuned = st.autotune(qt.data_ptr(), Q, ids.data_ptr(), dists.data_ptr(), sp)
     for name, bf in (("fp32", 0), ("bf16_rerank", 1)):
         st.set_tuning(candidates_mode=1, distance_bf16=bf)
         for _ in range(warmup):
@@ -374,7 +379,7 @@ def recall_point(culsh, torch, dev, steps, warmup):
     rec = recall_at_k(ref[:200], X, Qm[:200], K)
     return {"workload": f"gauss-mixture-1m-d128 N={N} L={L} M={M} W={W} T={T} K={K} Q={Q}",
             "recall_at_k": rec, "recall_sample": 200, "candidates_unique_per_query": round(uniq, 1),
-            "forms": forms}
+            "tuning": tuned, "forms": forms}
 
 
 def run_culsh(args):
@@ -551,6 +556,14 @@ def main(argv=None):
     args = parse_args(argv)
     if args.impl == "reference":
         return run_reference(args)
+    if args.recall_point_only:
+        import torch
+        import culsh_gb300 as culsh
+        dev = torch.device("cuda", 0)
+        torch.cuda.set_device(dev)
+        print(json.dumps({"recall_point": recall_point(culsh, torch, dev, args.steps, args.warmup,
+                                                       autotune=not args.no_autotune)}), flush=True)
+        return 0
     return run_culsh(args)
 
 

@@ -61,7 +61,8 @@ class _Profile(ctypes.Structure):
 class _Tuning(ctypes.Structure):
     _fields_ = [("proj_tile", ctypes.c_int), ("probe_batch", ctypes.c_int), ("candidates_mode", ctypes.c_int),
                 ("ws_threads", ctypes.c_int), ("ws_blocks_per_sm", ctypes.c_int), ("ws_chunk", ctypes.c_int),
-                ("distance_bf16", ctypes.c_int), ("search_ms", ctypes.c_float), ("configs_tried", ctypes.c_int)]
+                ("distance_bf16", ctypes.c_int), ("ws_set_slots", ctypes.c_int), ("search_ms", ctypes.c_float),
+                ("configs_tried", ctypes.c_int)]
 
 
 class _IndexProfile(ctypes.Structure):

@@ -4,8 +4,8 @@
 // Same results as k_candidates (query.cu), organised for heavy-tailed
 // candidate counts and for CUDA-graph capture (no host round trip):
 //  * k_plan_items turns every query with C > 0 non-unique candidates into
-//    P = min(64, ceil(C / 1024)) work items; item p of a query owns the
-//    candidate ids whose hash falls in partition p, so the items of a query
+//    P = min(64, ceil(C / chunk)) work items; item p of a query owns the
+//    candidate ids whose hash h (32 bits) has floor(h * P / 2^32) = p, so the items of a query
 //    deduplicate disjoint id sets (each fits the shared-memory set) and can be
 //    processed by different CTAs. Queries without candidates get their padded
 //    output ((-1, FLT_MAX) x K) right there.
@@ -32,8 +32,6 @@
 namespace culsh {
 namespace {
 
-constexpr int W_SLOTS = 4096;          // shared hash slots per item
-constexpr int W_CAP = W_SLOTS / 2;     // distinct ids per item
 constexpr uint32_t kPartSalt = 0x5bd1e995u;
 constexpr int GCH = 256;               // bucket slots scanned per gather chunk
 
@@ -102,9 +100,12 @@ __global__ void __launch_bounds__(PT_PLAN) k_plan_items(WsArgs a) {
 
 // WT threads per item: WT / 32 warps each keep a sorted top-K list over a
 // strided share of the item's candidates (tuned: 64, 128 or 256).
-template <int WT, bool kBF16>
+// W_SLOTS: shared hash-set slots per item (4096 or 8192, tuned); an item
+// holds at most W_CAP = W_SLOTS / 2 distinct ids.
+template <int WT, bool kBF16, int W_SLOTS>
 __global__ void __launch_bounds__(WT) k_candidates_ws(WsArgs a) {
     constexpr int WW = WT / 32;
+    constexpr int W_CAP = W_SLOTS / 2;
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ uint32_t s_ucount;
     __shared__ int s_item, s_last, s_wn[WW];
@@ -151,7 +152,7 @@ __global__ void __launch_bounds__(WT) k_candidates_ws(WsArgs a) {
         // Gather this item's id partition from every matched bucket.
         const BucketView bv{a.qbuckets, a.boff, a.starts, a.sizes, a.ids, a.N, L, T, a.Q};
         gather_bucket_ids<WT, GCH>(bv, q, s_gather, [&](uint32_t id) {
-            if (P > 1 && mix32(id ^ kPartSalt) % P != p) return;
+            if (P > 1 && (uint32_t)(((uint64_t)mix32(id ^ kPartSalt) * P) >> 32) != p) return;
             set_insert(hset, W_SLOTS - 1, ulist, W_CAP, &s_ucount, id);
         });
         __syncthreads();
@@ -450,9 +451,10 @@ __global__ void __launch_bounds__(WT) k_candidates_ws(WsArgs a) {
 
 }  // namespace
 
-size_t ws_smem_bytes(int D, int K, int wt, int bf16) {
-    return sizeof(float) * (size_t)((D + 3) & ~3) + sizeof(uint32_t) * (W_SLOTS + W_CAP) +
-           (size_t)(wt / 32) * K * (sizeof(float) + sizeof(uint32_t)) + (bf16 ? 2 * sizeof(float) * W_CAP : 0);
+size_t ws_smem_bytes(int D, int K, int wt, int bf16, int slots) {
+    const size_t cap = (size_t)slots / 2;
+    return sizeof(float) * (size_t)((D + 3) & ~3) + sizeof(uint32_t) * ((size_t)slots + cap) +
+           (size_t)(wt / 32) * K * (sizeof(float) + sizeof(uint32_t)) + (bf16 ? 2 * sizeof(float) * cap : 0);
 }
 
 cudaError_t launch_plan_items(const WsArgs& a, cudaStream_t st) {
@@ -462,45 +464,46 @@ cudaError_t launch_plan_items(const WsArgs& a, cudaStream_t st) {
 }
 
 namespace {
-template <int WT, bool kBF16>
+template <int WT, bool kBF16, int SL>
 cudaError_t launch_ws_v(const WsArgs& a, int grid, cudaStream_t st) {
-    const size_t smem = ws_smem_bytes(a.D, a.K, WT, kBF16);
+    const size_t smem = ws_smem_bytes(a.D, a.K, WT, kBF16, SL);
     static std::atomic<size_t> configured{0};   // largest dynamic shared memory opted into
     if (smem > 48 * 1024 && smem > configured) {
-        cudaError_t e =
-            cudaFuncSetAttribute(k_candidates_ws<WT, kBF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(k_candidates_ws<WT, kBF16, SL>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         configured = smem;
     }
-    k_candidates_ws<WT, kBF16><<<grid, WT, smem, st>>>(a);
+    k_candidates_ws<WT, kBF16, SL><<<grid, WT, smem, st>>>(a);
     return cudaGetLastError();
 }
 
-template <int WT, bool kBF16>
+template <int WT, bool kBF16, int SL>
 int ws_bps_v(int D, int K) {
     int n = 0;
-    const size_t smem = ws_smem_bytes(D, K, WT, kBF16);
+    const size_t smem = ws_smem_bytes(D, K, WT, kBF16, SL);
     if (smem > 48 * 1024)
-        cudaFuncSetAttribute(k_candidates_ws<WT, kBF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_candidates_ws<WT, kBF16>, WT, smem) != cudaSuccess) n = 1;
+        cudaFuncSetAttribute(k_candidates_ws<WT, kBF16, SL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_candidates_ws<WT, kBF16, SL>, WT, smem) != cudaSuccess)
+        n = 1;
     return n > 0 ? n : 1;
 }
 
-template <bool kBF16>
+template <bool kBF16, int SL>
 cudaError_t launch_ws_w(const WsArgs& a, int grid, cudaStream_t st) {
     switch (a.wt) {
-        case 64: return launch_ws_v<64, kBF16>(a, grid, st);
-        case 256: return launch_ws_v<256, kBF16>(a, grid, st);
-        default: return launch_ws_v<128, kBF16>(a, grid, st);
+        case 64: return launch_ws_v<64, kBF16, SL>(a, grid, st);
+        case 256: return launch_ws_v<256, kBF16, SL>(a, grid, st);
+        default: return launch_ws_v<128, kBF16, SL>(a, grid, st);
     }
 }
 
-template <bool kBF16>
+template <bool kBF16, int SL>
 int ws_bps_w(int D, int K, int wt) {
     switch (wt) {
-        case 64: return ws_bps_v<64, kBF16>(D, K);
-        case 256: return ws_bps_v<256, kBF16>(D, K);
-        default: return ws_bps_v<128, kBF16>(D, K);
+        case 64: return ws_bps_v<64, kBF16, SL>(D, K);
+        case 256: return ws_bps_v<256, kBF16, SL>(D, K);
+        default: return ws_bps_v<128, kBF16, SL>(D, K);
     }
 }
 
@@ -531,11 +534,13 @@ __global__ void k_bf16_rows(const float* __restrict__ X, int64_t N, int D, uint1
 }  // namespace
 
 cudaError_t launch_candidates_ws(const WsArgs& a, int grid, cudaStream_t st) {
-    return a.bf16 ? launch_ws_w<true>(a, grid, st) : launch_ws_w<false>(a, grid, st);
+    if (a.slots == 8192) return a.bf16 ? launch_ws_w<true, 8192>(a, grid, st) : launch_ws_w<false, 8192>(a, grid, st);
+    return a.bf16 ? launch_ws_w<true, 4096>(a, grid, st) : launch_ws_w<false, 4096>(a, grid, st);
 }
 
-int ws_blocks_per_sm(int D, int K, int wt, int bf16) {
-    return bf16 ? ws_bps_w<true>(D, K, wt) : ws_bps_w<false>(D, K, wt);
+int ws_blocks_per_sm(int D, int K, int wt, int bf16, int slots) {
+    if (slots == 8192) return bf16 ? ws_bps_w<true, 8192>(D, K, wt) : ws_bps_w<false, 8192>(D, K, wt);
+    return bf16 ? ws_bps_w<true, 4096>(D, K, wt) : ws_bps_w<false, 4096>(D, K, wt);
 }
 
 cudaError_t launch_bf16_rows(const float* X, int64_t N, int D, uint16_t* xb, uint8_t* flag, cudaStream_t st) {

@@ -185,6 +185,7 @@ struct SearchTune {
     int ws_bps = 0;        // resident work-stealing CTAs per SM (0: occupancy limit)
     int ws_chunk = 1024;   // non-unique candidates per id partition
     int dist_bf16 = 0;     // 1: BF16 candidate distances + certified FP32 rerank (work-stealing form)
+    int ws_slots = 4096;   // shared hash-set slots per work item (4096 or 8192)
 };
 constexpr size_t kPlanBytes = 1024;   // room for the graph key (checked below)
 
@@ -209,7 +210,7 @@ struct culsh_search {
     DevBuf<uint8_t> item_p;
     DevBuf<float> part_d;
     DevBuf<uint32_t> part_i;
-    int sms = 0, ws_used = 0, ws_overflow = 0;
+    int sms = 0, smem_optin = 0, ws_used = 0, ws_overflow = 0;
     long long rechecked = 0;   // BF16 form: candidates re-read in FP32 by the last search
     SearchTune tune;
     bool use_graphs = true;
@@ -811,6 +812,17 @@ int plan_search(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* 
     ca.nq = Q;
     P.use_ws = tu.cand_ws && !forced_per_query();
     if (P.use_ws) {
+        // A configuration whose item state exceeds the shared memory a block
+        // may opt into (large K or D with the wide set) runs per query.
+        if (s->smem_optin == 0) {
+            int dev = 0;
+            CU_TRY(cudaGetDevice(&dev));
+            CU_TRY(cudaDeviceGetAttribute(&s->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        }
+        const size_t need = ws_smem_bytes(D, K, tu.ws_wt, tu.dist_bf16 ? 1 : 0, tu.ws_slots) + 8192;
+        if (need > (size_t)s->smem_optin) P.use_ws = 0;
+    }
+    if (P.use_ws) {
         // Work-stealing buffers. stats[4] holds the item counter (low word)
         // and the overflow flag (high word), stats[5] the number of items.
         const int pmax = env_int("CULSH_WS_PARTITIONS", 1, kWsPartitions, kWsPartitions);
@@ -842,7 +854,7 @@ int plan_search(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* 
             CU_TRY(cudaStreamSynchronize(st));
             ix->xb_valid = true;
         }
-        const int occ = ws_blocks_per_sm(D, K, tu.ws_wt, bf16);
+        const int occ = ws_blocks_per_sm(D, K, tu.ws_wt, bf16, tu.ws_slots);
         const int bps = tu.ws_bps > 0 ? std::min(tu.ws_bps, occ) : occ;
         P.ws_grid = s->sms * bps;
         WsArgs& a = P.wa;
@@ -879,6 +891,7 @@ int plan_search(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* 
         a.overflow = reinterpret_cast<unsigned int*>(s->stats.p + 4) + 1;
         a.n_items = reinterpret_cast<unsigned int*>(s->stats.p + 5);
         a.wt = tu.ws_wt;
+        a.slots = tu.ws_slots;
         a.bf16 = bf16;
         if (bf16) {
             // |d~ - d| <= c1 d~ + c2 (2 rho b1 + rho^2 b2) with gamma_n = n u / (1 - n u),
@@ -1518,6 +1531,7 @@ static void tune_to_c(const SearchTune& t, culsh_tuning* o) {
     o->ws_blocks_per_sm = t.ws_bps;
     o->ws_chunk = t.ws_chunk;
     o->distance_bf16 = t.dist_bf16;
+    o->ws_set_slots = t.ws_slots;
 }
 
 int culsh_search_get_tuning(culsh_search* s, culsh_tuning* out) {
@@ -1534,7 +1548,8 @@ int culsh_search_set_tuning(culsh_search* s, const culsh_tuning* in) {
                     (in->candidates_mode == 0 || in->candidates_mode == 1) &&
                     (in->ws_threads == 64 || in->ws_threads == 128 || in->ws_threads == 256) &&
                     in->ws_blocks_per_sm >= 0 && in->ws_blocks_per_sm <= 64 && in->ws_chunk >= 64 &&
-                    in->ws_chunk <= 65536 && (in->distance_bf16 == 0 || in->distance_bf16 == 1);
+                    in->ws_chunk <= 65536 && (in->distance_bf16 == 0 || in->distance_bf16 == 1) &&
+                    (in->ws_set_slots == 4096 || in->ws_set_slots == 8192);
     if (!ok) return fail(CULSH_ERR_INVALID_ARGUMENT, "tuning value out of range");
     s->tune.proj_tile = in->proj_tile;
     s->tune.probe_pch = in->probe_batch;
@@ -1543,6 +1558,7 @@ int culsh_search_set_tuning(culsh_search* s, const culsh_tuning* in) {
     s->tune.ws_bps = in->ws_blocks_per_sm;
     s->tune.ws_chunk = in->ws_chunk;
     s->tune.dist_bf16 = in->distance_bf16;
+    s->tune.ws_slots = in->ws_set_slots;
     return CULSH_OK;
 }
 
@@ -1638,14 +1654,18 @@ int culsh_search_autotune(culsh_search* s, const float* d_queries, int Q, int* d
         SearchTune t = best;
         t.cand_ws = 0;
         cands.push_back(t);
-        const int wts[3] = {64, 128, 256}, chunks[3] = {512, 1024, 2048};
+        // (set slots, partition size): a partition of `chunk` non-unique
+        // candidates always fits a set of 2 * chunk slots
+        const int wts[3] = {64, 128, 256};
+        const int sets[5][2] = {{4096, 1024}, {4096, 2048}, {8192, 1024}, {8192, 2048}, {8192, 4096}};
         for (int f = 0; f < 2; ++f)
             for (int a = 0; a < 3; ++a)
-                for (int b = 0; b < 3; ++b) {
+                for (int b = 0; b < 5; ++b) {
                     SearchTune u = best;
                     u.cand_ws = 1;
                     u.ws_wt = wts[a];
-                    u.ws_chunk = chunks[b];
+                    u.ws_slots = sets[b][0];
+                    u.ws_chunk = sets[b][1];
                     u.ws_bps = 0;
                     u.dist_bf16 = f;
                     cands.push_back(u);
@@ -1666,7 +1686,7 @@ int culsh_search_autotune(culsh_search* s, const float* d_queries, int Q, int* d
         }
     }
     if (best.cand_ws) {   // residency: half the occupancy limit as well
-        const int occ = ws_blocks_per_sm(s->ix->D, s->K, best.ws_wt, best.dist_bf16);
+        const int occ = ws_blocks_per_sm(s->ix->D, s->K, best.ws_wt, best.dist_bf16, best.ws_slots);
         if (occ > 1) {
             SearchTune t = best;
             t.ws_bps = occ / 2;

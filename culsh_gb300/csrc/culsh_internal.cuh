@@ -258,6 +258,7 @@ struct WsArgs {
     unsigned int* next_item;           // work-stealing counter, zero before the launch
     unsigned int* overflow;            // nonzero: rerun with the per-query kernel
     int wt;                            // threads per item CTA: 64, 128 or 256
+    int slots;                         // shared hash-set slots per item: 4096 or 8192
     // BF16 form: approximate distances from xb, certified FP32 rerank
     int bf16;
     const uint16_t* xb;                // [N][D] bf16 copy of X
@@ -265,8 +266,8 @@ struct WsArgs {
     float e_c1, e_c2;                  // error-bound factors (rounded up)
     unsigned long long* rechecked;     // candidates whose FP32 row pass 2 re-read
 };
-size_t ws_smem_bytes(int D, int K, int wt, int bf16);
-int ws_blocks_per_sm(int D, int K, int wt, int bf16);
+size_t ws_smem_bytes(int D, int K, int wt, int bf16, int slots);
+int ws_blocks_per_sm(int D, int K, int wt, int bf16, int slots);
 cudaError_t launch_bf16_rows(const float* X, int64_t N, int D, uint16_t* xb, uint8_t* flag, cudaStream_t st);
 cudaError_t launch_plan_items(const WsArgs& a, cudaStream_t st);
 cudaError_t launch_candidates_ws(const WsArgs& a, int grid, cudaStream_t st);

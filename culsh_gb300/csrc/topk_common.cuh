@@ -138,15 +138,21 @@ __device__ __forceinline__ void gather_bucket_ids(const BucketView& v, int q, Ga
         }
         __syncthreads();
         const unsigned long long total = g.pre[n - 1];
+        // h: first bucket whose inclusive prefix exceeds i. i only grows, so
+        // h is kept between steps and searched for only when i leaves it.
+        uint32_t h = 0;
         for (unsigned long long i = tid; i < total; i += NT) {
-            uint32_t lo = 0, hi = n - 1;   // first bucket whose inclusive prefix exceeds i
-            while (lo < hi) {
-                const uint32_t mid = (lo + hi) >> 1;
-                if (g.pre[mid] > i) hi = mid;
-                else lo = mid + 1;
+            if (g.pre[h] <= i) {
+                uint32_t lo = h + 1, hi = n - 1;
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (g.pre[mid] > i) hi = mid;
+                    else lo = mid + 1;
+                }
+                h = lo;
             }
-            const uint64_t off = i - (lo ? g.pre[lo - 1] : 0ull);
-            f(__ldg(v.ids + g.base[lo] + off));
+            const uint64_t off = i - (h ? g.pre[h - 1] : 0ull);
+            f(__ldg(v.ids + g.base[h] + off));
         }
         __syncthreads();
     }

@@ -143,6 +143,7 @@ typedef struct culsh_tuning {
     int distance_bf16;    /* 1: candidate distances from a bf16 copy of the dataset, then
                              an exact FP32 rerank of every candidate the proven error
                              bound cannot exclude (same results as 0)                  */
+    int ws_set_slots;     /* work-stealing shared hash set per item: 4096 or 8192 slots */
     float search_ms;      /* culsh_search_autotune: median device ms of the choice       */
     int configs_tried;    /* culsh_search_autotune: configurations timed                 */
 } culsh_tuning;
