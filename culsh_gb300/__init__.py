@@ -72,7 +72,8 @@ class _IndexProfile(ctypes.Structure):
 
 
 class _ServerConfig(ctypes.Structure):
-    _fields_ = [("slots", ctypes.c_int), ("max_batch_queries", ctypes.c_int), ("memory_budget", ctypes.c_longlong)]
+    _fields_ = [("slots", ctypes.c_int), ("max_batch_queries", ctypes.c_int), ("memory_budget", ctypes.c_longlong),
+                ("graphs", ctypes.c_int)]
 
 
 class _ServerStats(ctypes.Structure):
@@ -385,10 +386,10 @@ class Server:
     concurrently on the device; each returns what a lone search returns."""
 
     def __init__(self, hashtables: HashTables, slots: int = 4, max_batch_queries: int = 8192,
-                 memory_budget: int = 0):
+                 memory_budget: int = 0, graphs: bool = False):
         self._ht = hashtables
         self._h = ctypes.c_void_p()
-        cfg = _ServerConfig(int(slots), int(max_batch_queries), int(memory_budget))
+        cfg = _ServerConfig(int(slots), int(max_batch_queries), int(memory_budget), 1 if graphs else 0)
         _check(lib().culsh_server_create(ctypes.byref(self._h), hashtables._h, ctypes.byref(cfg)))
         self._keep = {}
 

@@ -211,6 +211,8 @@ struct culsh_search {
     DevBuf<float> part_d;
     DevBuf<uint32_t> part_i;
     int sms = 0, smem_optin = 0, ws_used = 0, ws_overflow = 0;
+    long long occ_key = -1;
+    int occ_val = 1;
     long long rechecked = 0;   // BF16 form: candidates re-read in FP32 by the last search
     SearchTune tune;
     bool use_graphs = true;
@@ -854,7 +856,13 @@ int plan_search(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* 
             CU_TRY(cudaStreamSynchronize(st));
             ix->xb_valid = true;
         }
-        const int occ = ws_blocks_per_sm(D, K, tu.ws_wt, bf16, tu.ws_slots);
+        // resident CTAs per SM, cached per kernel shape
+        const long long okey = ((((long long)D * 4096 + K) * 512 + tu.ws_wt) * 2 + bf16) * 16384 + tu.ws_slots;
+        if (s->occ_key != okey) {
+            s->occ_val = ws_blocks_per_sm(D, K, tu.ws_wt, bf16, tu.ws_slots);
+            s->occ_key = okey;
+        }
+        const int occ = s->occ_val;
         const int bps = tu.ws_bps > 0 ? std::min(tu.ws_bps, occ) : occ;
         P.ws_grid = s->sms * bps;
         WsArgs& a = P.wa;

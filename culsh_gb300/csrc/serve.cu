@@ -72,7 +72,7 @@ struct Slot {
 struct culsh_server {
     culsh_index* ix = nullptr;
     int D = 0, L = 0;
-    int n_slots = 4, max_batch = 8192;
+    int n_slots = 4, max_batch = 8192, graphs = 0;
     long long budget = 0;
     std::mutex mu;
     std::condition_variable cv_sched, cv_done;
@@ -361,6 +361,7 @@ int culsh_server_create(culsh_server** out, culsh_index* ix, const culsh_server_
         if (cfg->slots) v->n_slots = cfg->slots;
         if (cfg->max_batch_queries) v->max_batch = cfg->max_batch_queries;
         v->budget = cfg->memory_budget;
+        v->graphs = cfg->graphs != 0;
     }
     if (v->budget == 0) {
         size_t freeb = 0, totalb = 0;
@@ -379,6 +380,7 @@ int culsh_server_create(culsh_server** out, culsh_index* ix, const culsh_server_
             if (sl->s) culsh_search_destroy(sl->s);
             return culsh::set_last_error(CULSH_ERR_CUDA, "serving: slot creation failed");
         }
+        culsh_search_set_graphs(sl->s, v->graphs);
         v->slots.push_back(std::move(sl));
     }
     culsh_server* p = v.release();

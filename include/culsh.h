@@ -232,6 +232,9 @@ typedef struct culsh_server_config {
     int slots;                /* batches on the device at once, 1..64 (0: 4)          */
     int max_batch_queries;    /* queries merged into one batch (0: 8192)              */
     long long memory_budget;  /* device bytes for all slots (0: 80% of free memory)   */
+    int graphs;               /* 1: slots replay CUDA graphs of their searches (pays off
+                                 when batch sizes repeat); 0: direct launches, since a
+                                 new batch size would re-capture the graph             */
 } culsh_server_config;
 typedef struct culsh_server_stats {
     long long requests;       /* completed requests (including failed ones)           */

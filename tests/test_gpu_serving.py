@@ -35,13 +35,13 @@ def mixed_requests(c, n, seed):
     return reqs
 
 
-@pytest.mark.parametrize("name", ["heavy", "mix_d16_t8"])
-def test_each_result_same_alone_and_in_the_mix(culsh, name):
+@pytest.mark.parametrize("name,graphs", [("heavy", False), ("mix_d16_t8", False), ("heavy", True)])
+def test_each_result_same_alone_and_in_the_mix(culsh, name, graphs):
     c = load_case(name)
     ht = build_index(culsh, c)
     reqs = mixed_requests(c, 40, seed=5)
     ref = [alone(culsh, ht, c["X"], q, K, T) for q, K, T in reqs]
-    with culsh.Server(ht, slots=4, max_batch_queries=64) as srv:
+    with culsh.Server(ht, slots=4, max_batch_queries=64, graphs=graphs) as srv:
         tickets = [srv.submit(q, K, T) for q, K, T in reqs]
         for t, (ids0, d0) in zip(tickets, ref):
             ids, d = srv.wait(t, timeout=120)
