@@ -465,15 +465,16 @@ cudaError_t launch_plan_items(const WsArgs& a, cudaStream_t st) {
 
 namespace {
 template <int WT, bool kBF16, int SL>
+std::atomic<size_t>& ws_smem_cap() {
+    static std::atomic<size_t> cap{0};   // dynamic shared memory this kernel is opted into
+    return cap;
+}
+
+template <int WT, bool kBF16, int SL>
 cudaError_t launch_ws_v(const WsArgs& a, int grid, cudaStream_t st) {
     const size_t smem = ws_smem_bytes(a.D, a.K, WT, kBF16, SL);
-    static std::atomic<size_t> configured{0};   // largest dynamic shared memory opted into
-    if (smem > 48 * 1024 && smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_candidates_ws<WT, kBF16, SL>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        configured = smem;
-    }
+    const cudaError_t e = opt_in_smem(k_candidates_ws<WT, kBF16, SL>, smem, ws_smem_cap<WT, kBF16, SL>());
+    if (e != cudaSuccess) return e;
     k_candidates_ws<WT, kBF16, SL><<<grid, WT, smem, st>>>(a);
     return cudaGetLastError();
 }
@@ -482,8 +483,7 @@ template <int WT, bool kBF16, int SL>
 int ws_bps_v(int D, int K) {
     int n = 0;
     const size_t smem = ws_smem_bytes(D, K, WT, kBF16, SL);
-    if (smem > 48 * 1024)
-        cudaFuncSetAttribute(k_candidates_ws<WT, kBF16, SL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (opt_in_smem(k_candidates_ws<WT, kBF16, SL>, smem, ws_smem_cap<WT, kBF16, SL>()) != cudaSuccess) return 1;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_candidates_ws<WT, kBF16, SL>, WT, smem) != cudaSuccess)
         n = 1;
     return n > 0 ? n : 1;

@@ -19,6 +19,7 @@
 //   hmask    [L]     u32    power-of-two group count - 1
 #pragma once
 
+#include <atomic>
 #include <cstdint>
 #include <mutex>
 #include <cuda_runtime.h>
@@ -271,6 +272,21 @@ int ws_blocks_per_sm(int D, int K, int wt, int bf16, int slots);
 cudaError_t launch_bf16_rows(const float* X, int64_t N, int D, uint16_t* xb, uint8_t* flag, cudaStream_t st);
 cudaError_t launch_plan_items(const WsArgs& a, cudaStream_t st);
 cudaError_t launch_candidates_ws(const WsArgs& a, int grid, cudaStream_t st);
+
+// Opts `func` into `dyn` bytes of dynamic shared memory when static plus
+// dynamic shared memory could pass the 48 KB default (the kernels here keep
+// at most 12 KB static). The opted-in size only grows (`cap` records it per
+// kernel), so a smaller configuration launched later stays valid.
+template <class F>
+cudaError_t opt_in_smem(F* func, size_t dyn, std::atomic<size_t>& cap) {
+    if (dyn + 12 * 1024 <= 48 * 1024 || dyn <= cap.load()) return cudaSuccess;
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lk(mu);
+    if (dyn <= cap.load()) return cudaSuccess;
+    const cudaError_t e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    if (e == cudaSuccess) cap = dyn;
+    return e;
+}
 
 // Process-wide lock held while a search plans (and grows) its buffers and
 // captures its graph: no thread frees device memory while another captures.

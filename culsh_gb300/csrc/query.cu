@@ -192,7 +192,7 @@ __global__ void __launch_bounds__(128) k_probe(ProbeArgs a) {
 
 
 // ---------------------------------------------------------------------------
-// Fast multiprobe path for the common shapes: M <= 32 columns, T <= 32
+// Fast multiprobe path for the common shapes: M <= 32 columns, T <= 64
 // probes, packed keys of at most 128 bits and codes below 2^24 in magnitude
 // (so that the reference's float +-1 on a code equals integer +-1).
 //
@@ -513,13 +513,9 @@ __global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
 template <typename MaskT, int PCH>
 cudaError_t launch_probe_fast_v(const ProbeArgs& a, cudaStream_t st) {
     const size_t smem = (size_t)PF * probe_fast_bytes_per_thread<MaskT>(a.lv.M, a.T);
-    static std::atomic<size_t> configured{0};   // largest dynamic shared memory opted into
-    if (smem > 48 * 1024 && smem > configured) {
-        cudaError_t e =
-            cudaFuncSetAttribute(k_probe_fast<MaskT, PCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        configured = smem;
-    }
+    static std::atomic<size_t> cap{0};   // dynamic shared memory this kernel is opted into
+    const cudaError_t e = opt_in_smem(k_probe_fast<MaskT, PCH>, smem, cap);
+    if (e != cudaSuccess) return e;
     const int64_t n = (int64_t)a.lv.L * a.Q;
     k_probe_fast<MaskT, PCH><<<(unsigned)((n + PF - 1) / PF), PF, smem, st>>>(a);
     return cudaGetLastError();
@@ -698,7 +694,13 @@ cudaError_t launch_probe(const ProbeArgs& a, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     // CULSH_PROBE_GENERIC forces the general kernel (the tests run both).
     const bool generic_only = getenv("CULSH_PROBE_GENERIC") != nullptr;
-    if (!generic_only && a.small_codes && a.lv.KW <= 4 && a.T <= 32 && a.lv.M <= 32) return launch_probe_fast(a, st);
+    // The fast kernel keeps per-thread state in shared memory: used while a
+    // block's slice stays within 100 KB (two blocks per SM), i.e. T <= 64
+    // for M <= 16.
+    const size_t fast_bytes = (size_t)PF * (a.lv.M <= 16 ? probe_fast_bytes_per_thread<uint32_t>(a.lv.M, a.T)
+                                                         : probe_fast_bytes_per_thread<uint64_t>(a.lv.M, a.T));
+    if (!generic_only && a.small_codes && a.lv.KW <= 4 && a.T <= 64 && a.lv.M <= 32 && fast_bytes <= 100 * 1024)
+        return launch_probe_fast(a, st);
     k_probe<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(a);
     return cudaGetLastError();
 }
@@ -717,12 +719,9 @@ cudaError_t launch_candidates(const CandArgs& a, cudaStream_t st) {
     if (nblk <= 0) return cudaSuccess;
     const size_t smem = sizeof(float) * (size_t)((a.D + 3) & ~3) + sizeof(uint32_t) * (SM_SLOTS + SM_CAP) +
                         (size_t)CW * a.K * (sizeof(float) + sizeof(uint32_t));
-    static std::atomic<size_t> configured{0};   // largest dynamic shared memory opted into
-    if (smem > 48 * 1024 && smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_candidates, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        configured = smem;
-    }
+    static std::atomic<size_t> cap{0};   // dynamic shared memory this kernel is opted into
+    const cudaError_t e = opt_in_smem(k_candidates, smem, cap);
+    if (e != cudaSuccess) return e;
     k_candidates<<<nblk, CT, smem, st>>>(a);
     return cudaGetLastError();
 }

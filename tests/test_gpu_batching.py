@@ -182,3 +182,30 @@ def test_autotune_keeps_results(culsh):
         side.synchronize()
         np.testing.assert_array_equal(ids.cpu().numpy(), c["knn_ids"])
     assert st.profile()["graph_mode"] == 2
+
+
+def test_wide_rows_shared_memory_opt_in(culsh):
+    """D = 900: an item's dynamic shared memory plus the kernel's static
+    shared memory passes the 48 KB default in several configurations; each
+    runs (opted in as needed, in any order) and matches the oracle."""
+    import oracle
+    rng = np.random.default_rng(9)
+    N, D, L, M, W = 2500, 900, 3, 4, 60.0
+    centers = rng.normal(0, 4, (8, D)).astype(np.float32)
+    X = (centers[rng.integers(0, 8, N)] + rng.normal(0, 1, (N, D))).astype(np.float32)
+    A = rng.normal(0, 1, (L, M, D)).astype(np.float32)
+    b = rng.uniform(0, W, (L, M)).astype(np.float32)
+    queries = (X[:24] + rng.normal(0, 0.3, (24, D))).astype(np.float32)
+    K, T = 10, 4
+    ht = culsh.HashTables()
+    ht.reset(N, D, L, M, W, A=A, b=b)
+    ht.index(X)
+    ref = oracle.search(oracle.build_index(X, A, b, W), X, queries, K, T)
+    assert int(ref["unique"].max()) > 0
+    st = culsh.SearchTables()
+    st.reset(ht, K, T)
+    for sl, bf, wt in itertools.product((8192, 4096), (1, 0), (256, 64, 128)):
+        st.set_tuning(candidates_mode=1, ws_set_slots=sl, distance_bf16=bf, ws_threads=wt)
+        st.search(queries, dataset=X)
+        np.testing.assert_array_equal(st.getKnnIds(), ref["knn_ids"])
+        np.testing.assert_array_equal(st.getKnnDistances(), ref["knn_dists"])
