@@ -145,6 +145,7 @@ struct culsh_index {
     DevBuf<uint8_t> fbits;
     DevBuf<uint16_t> foff;
     DevBuf<unsigned long long> funit;   // [L*M][2]: 2^foff as two 64-bit words
+    DevBuf<unsigned long long> rmul;    // [L*M]: lookup-hash field multipliers
     DevBuf<uint32_t> ids, starts, sizes, ukeys;
     std::vector<uint64_t> h_boff, h_hoff;
     std::vector<uint32_t> h_hmask;
@@ -159,6 +160,7 @@ struct culsh_index {
     DevBuf<uint16_t> ws_ah, ws_al, ws_xh, ws_xl;   // bf16 splits for the tensor-core projection
     DevBuf<float> ws_anorm, ws_xnorm;
     DevBuf<int> ws_tcflags;
+    double tc_predicted_open = 0.0;   // predicted share of codes the tensor-core bound leaves open
     DevBuf<unsigned long long> ws_relist;
     DevBuf<unsigned int> ws_relist_cnt;
     long long tc_recomputed = -1;   // codes recomputed after the tensor-core pass (-1: SIMT path)
@@ -333,7 +335,11 @@ int upload_layout(culsh_index* ix, cudaStream_t st) {
     }
     CU_TRY(ix->funit.reserve(2 * LM));
     CU_TRY(cudaMemcpyAsync(ix->funit.p, unit.data(), 16 * LM, cudaMemcpyHostToDevice, st));
-    CU_TRY(cudaStreamSynchronize(st));   // `unit` is a pageable temporary
+    std::vector<unsigned long long> rm(LM);
+    for (size_t c = 0; c < LM; ++c) rm[c] = field_mult((int)c);
+    CU_TRY(ix->rmul.reserve(LM));
+    CU_TRY(cudaMemcpyAsync(ix->rmul.p, rm.data(), 8 * LM, cudaMemcpyHostToDevice, st));
+    CU_TRY(cudaStreamSynchronize(st));   // `unit` and `rm` are pageable temporaries
     return CULSH_OK;
 }
 
@@ -357,7 +363,8 @@ int build_hash(culsh_index* ix, cudaStream_t st) {
     CU_TRY(cudaMemcpyAsync(ix->hoff.p, ix->h_hoff.data(), 8 * (L + 1), cudaMemcpyHostToDevice, st));
     CU_TRY(cudaMemcpyAsync(ix->hmask.p, ix->h_hmask.data(), 4 * L, cudaMemcpyHostToDevice, st));
     CU_TRY(cudaMemsetAsync(ix->hslots.p, 0xFF, 8 * ix->h_hoff[L], st));
-    CU_TRY(launch_hash_build(ix->boff.p, ix->ukeys.p, L, ix->KW, maxB, ix->hoff.p, ix->hmask.p, ix->hslots.p,
+    CU_TRY(launch_hash_build(ix->boff.p, ix->ukeys.p, L, ix->M, ix->KW, maxB, ix->foff.p, ix->fbits.p, ix->rmul.p,
+                             ix->hoff.p, ix->hmask.p, ix->hslots.p,
                              ix->err.p, st));
     return CULSH_OK;
 }
@@ -391,8 +398,15 @@ int project_tensor_cores(culsh_index* ix, const float* dX, cudaStream_t st, bool
     CU_TRY(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     CU_TRY(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
     if (major < 10) return CULSH_OK;
-    const TcPlan p = tc_plan(N, D, LM, sms, maxsm);
-    if (!p.ok) return CULSH_OK;
+    // Resident form when the bf16 projection matrix fits shared memory,
+    // streaming form (K slices of X and A, column blocks) otherwise.
+    const TcPlan rp = tc_plan(N, D, LM, sms, maxsm);
+    const TcStreamPlan sp = rp.ok ? TcStreamPlan{} : tc_plan_stream(N, D, LM, sms, maxsm);
+    if (!rp.ok && !sp.ok) return CULSH_OK;
+    const bool stream = !rp.ok;
+    struct {
+        int Dp, LMp, grid;
+    } p = {stream ? sp.Dp : rp.Dp, stream ? sp.LMp : rp.LMp, stream ? sp.grid : rp.grid};
     // Host split of the projection matrix and upper bounds of its column norms.
     std::vector<uint16_t> ah((size_t)p.LMp * p.Dp, 0), al((size_t)p.LMp * p.Dp, 0);
     std::vector<float> an(LM);
@@ -425,12 +439,6 @@ int project_tensor_cores(culsh_index* ix, const float* dX, cudaStream_t st, bool
     CU_TRY(cudaStreamSynchronize(st));
     if (flags & 2) return CULSH_OK;   // non-finite data: the SIMT kernel reports it
     const int need_lo = flags & 1;
-    // One recomputation region per CTA, sized for 1/6 of its codes.
-    const unsigned long long cap = ((unsigned long long)N * LM / 6) / p.grid + 4096;
-    CU_TRY(ix->ws_relist.reserve(cap * p.grid));
-    CU_TRY(ix->ws_relist_cnt.reserve(p.grid));
-    CU_TRY(ix->ws_pmin.reserve((size_t)p.grid * LM));
-    CU_TRY(ix->ws_pmax.reserve((size_t)p.grid * LM));
     // Bound on |tensor-core sum - canonical FP32 chain| per unit of sum|x||a|
     // (bounded by |x|_2 |a|_2): split residue, one rounding per summed
     // product, the canonical chain's rounding; 1.25 margin.
@@ -438,9 +446,37 @@ int project_tensor_cores(culsh_index* ix, const float* dX, cudaStream_t st, bool
     const double split = need_lo ? 3.02 * u16 : 1.01 * u16;
     const double accum = ((need_lo ? 3.0 : 2.0) * D + 16) * u23;
     const float kappa = (float)(1.25 * ((D + 2) * u24 + split + accum));
-    CU_TRY(launch_project_tc(p, need_lo, N, D, LM, ix->ws_xh.p, ix->ws_xl.p, ix->ws_ah.p, ix->ws_al.p, ix->db.p,
-                             ix->ws_anorm.p, ix->ws_xnorm.p, ix->W, kappa, ix->ws_codes.p, ix->ws_pmin.p, ix->ws_pmax.p,
-                             ix->ws_relist.p, cap, ix->ws_relist_cnt.p, ix->err.p, st));
+    {
+        // Predicted share of codes the bound leaves open: a code is open when
+        // an integer lies within E / W of its value, E = kappa |x| |a|. Above
+        // 6 % the FP32 recomputation costs more than the SIMT projection
+        // itself (e.g. D = 960, W = 0.25: 14 %), so the SIMT kernel runs.
+        const int ns = (int)std::min<int64_t>(N, 4096);
+        std::vector<float> xs(ns);
+        CU_TRY(cudaMemcpyAsync(xs.data(), ix->ws_xnorm.p, 4 * (size_t)ns, cudaMemcpyDeviceToHost, st));
+        CU_TRY(cudaStreamSynchronize(st));
+        std::vector<float> as(an.begin(), an.end());
+        std::nth_element(xs.begin(), xs.begin() + ns / 2, xs.end());
+        std::nth_element(as.begin(), as.begin() + LM / 2, as.end());
+        const double open = 2.0 * (double)kappa * xs[ns / 2] * as[LM / 2] / (double)ix->W;
+        ix->tc_predicted_open = open;
+        if (open > 0.06 && !getenv("CULSH_PROJECT_TC")) return CULSH_OK;
+    }
+    // One recomputation region per CTA, sized for 1/6 of its codes.
+    const unsigned long long cap = ((unsigned long long)N * LM / 6) / p.grid + 4096;
+    CU_TRY(ix->ws_relist.reserve(cap * p.grid));
+    CU_TRY(ix->ws_relist_cnt.reserve(p.grid));
+    CU_TRY(ix->ws_pmin.reserve((size_t)p.grid * LM));
+    CU_TRY(ix->ws_pmax.reserve((size_t)p.grid * LM));
+    if (stream)
+        CU_TRY(launch_project_tc_stream(sp, need_lo, N, D, LM, ix->ws_xh.p, ix->ws_xl.p, ix->ws_ah.p, ix->ws_al.p,
+                                        ix->db.p, ix->ws_anorm.p, ix->ws_xnorm.p, ix->W, kappa, ix->ws_codes.p,
+                                        ix->ws_pmin.p, ix->ws_pmax.p, ix->ws_relist.p, cap, ix->ws_relist_cnt.p,
+                                        ix->err.p, st));
+    else
+        CU_TRY(launch_project_tc(rp, need_lo, N, D, LM, ix->ws_xh.p, ix->ws_xl.p, ix->ws_ah.p, ix->ws_al.p, ix->db.p,
+                                 ix->ws_anorm.p, ix->ws_xnorm.p, ix->W, kappa, ix->ws_codes.p, ix->ws_pmin.p,
+                                 ix->ws_pmax.p, ix->ws_relist.p, cap, ix->ws_relist_cnt.p, ix->err.p, st));
     CU_TRY(launch_minmax_reduce(ix->ws_pmin.p, ix->ws_pmax.p, p.grid, LM, ix->cmin.p, ix->cmax.p, st));
     std::vector<unsigned int> cnt(p.grid);
     int err = 0;
@@ -676,6 +712,7 @@ LookupView lookup_view(const culsh_index* ix) {
     lv.hoff = ix->hoff.p;
     lv.hmask = ix->hmask.p;
     lv.funit = ix->funit.p;
+    lv.rmul = ix->rmul.p;
     return lv;
 }
 

@@ -66,16 +66,16 @@ __host__ __device__ __forceinline__ uint32_t mix32(uint32_t h) { return (uint32_
 
 constexpr uint64_t kHashSeed = 0x2545f4914f6cdd1dull;
 
-// 64-bit hash of a packed key of KW 32-bit words, folded as 64-bit chunks:
-// the low 32 bits pick the hash slot, the high 32 bits are the fingerprint.
-__host__ __device__ __forceinline__ uint64_t key_hash64(const uint32_t* k, int KW) {
-    uint64_t h = kHashSeed;
-    for (int w = 0; w < KW; w += 2) {
-        const uint64_t c = (uint64_t)k[w] | (w + 1 < KW ? (uint64_t)k[w + 1] << 32 : 0ull);
-        h = mix64(h ^ c);
-    }
-    return h;
+// Lookup hash of a bucket key, additive in its fields: h = sum_m f_m * R_c
+// (mod 2^64) over the fields f_m = code_m - cmin_m of table l, with R_c an
+// odd 64-bit multiplier per column c = l * M + m, then one mix. A multiprobe
+// key differs from its home key by +-1 in some fields, so its hash is the
+// home sum +- R_c before the mix. Equal keys hash equally; a lookup verifies
+// the stored key on every fingerprint match, so collisions cost time only.
+__host__ __device__ __forceinline__ uint64_t field_mult(int c) {
+    return mix64(kHashSeed ^ (0x9E3779B97F4A7C15ull * (uint64_t)(c + 1))) | 1ull;
 }
+__host__ __device__ __forceinline__ uint64_t hash_finish(uint64_t h) { return mix64(h ^ kHashSeed); }
 
 // Place a field of `bits` bits (<= 32) at bit offset `off` of a little-endian
 // multi-word key.
@@ -108,6 +108,7 @@ struct LookupView {
     const uint64_t* hoff;
     const uint32_t* hmask;
     const unsigned long long* funit;   // [L*M][2]: 2^foff as (low, high) 64-bit words
+    const unsigned long long* rmul;    // [L*M]: field multipliers of the lookup hash
 };
 
 // ---------------------------------------------------------------------------
@@ -135,6 +136,21 @@ struct TcPlan {
     size_t smem[2];
 };
 TcPlan tc_plan(int64_t N, int D, int LM, int num_sms, int max_smem);
+// Streaming form for projections whose matrix does not fit shared memory:
+// column blocks of blk[need_lo] per launch, any Dp.
+struct TcStreamPlan {
+    bool ok;
+    int Dp, LMp, ntiles, grid;
+    int blk[2], stages[2];
+    size_t smem[2];
+};
+TcStreamPlan tc_plan_stream(int64_t N, int D, int LM, int num_sms, int max_smem);
+cudaError_t launch_project_tc_stream(const TcStreamPlan& p, int need_lo, int64_t N, int D, int LM, const void* xh,
+                                     const void* xl, const void* ah, const void* al, const float* b,
+                                     const float* anorm, const float* xnorm, float W, float kappa, int32_t* codes,
+                                     int32_t* pmin, int32_t* pmax, unsigned long long* relist,
+                                     unsigned long long relist_cap, unsigned int* relist_cnt, int* err,
+                                     cudaStream_t st);
 cudaError_t launch_split_rows(const float* X, int64_t N, int D, int Dp, void* xh, void* xl, float* xnorm, int* flags,
                               cudaStream_t st);
 cudaError_t launch_project_tc(const TcPlan& p, int need_lo, int64_t N, int D, int LM, const void* xh, const void* xl,
@@ -174,7 +190,8 @@ cudaError_t launch_rl_write(const uint32_t* keys, int64_t N, int L, int KW, cons
                             const uint64_t* boff, uint32_t* starts, uint32_t* ukeys, cudaStream_t st);
 cudaError_t launch_bucket_sizes(const uint64_t* boff, const uint32_t* starts, int64_t N, int L, int64_t maxB,
                                 uint32_t* sizes, cudaStream_t st);
-cudaError_t launch_hash_build(const uint64_t* boff, const uint32_t* ukeys, int L, int KW, int64_t maxB,
+cudaError_t launch_hash_build(const uint64_t* boff, const uint32_t* ukeys, int L, int M, int KW, int64_t maxB,
+                              const uint16_t* foff, const uint8_t* fbits, const unsigned long long* rmul,
                               const uint64_t* hoff, const uint32_t* hmask, unsigned long long* hslots, int* err,
                               cudaStream_t st);
 // Bucket codes [M][B_l] per table (float, the reference's layout) decoded from ukeys.

@@ -63,6 +63,13 @@ struct TcArgs {
     float inv_w;                          // 1/W rounded to nearest
     int* err;
     uint32_t b_bytes, x_bytes;    // one bf16 operand region of A (LMp x Dp) / of an X tile (128 x Dp)
+    // Streaming form (A too large to keep in shared memory): this launch
+    // covers columns [col0, col0 + LM) of LMtot; each ring stage holds one
+    // 64-wide K slice of Xh (Xl) and of Ah, Al.
+    int col0, LMtot;
+    uint32_t stage_bytes;         // streaming: bytes of one ring stage
+    uint32_t a_chunk;             // streaming: bytes of one A slice (LMp x 64 bf16)
+    int list_continue;            // streaming: recompute lists continue from relist_cnt
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -141,6 +148,10 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// kStream = false: A resident in shared memory (Dp, LMp <= 256), X tiles
+// ring-buffered. kStream = true: X and A both streamed in 64-wide K slices,
+// for any Dp; a launch covers at most 256 columns. Same epilogue.
+template <bool kStream>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_project_tc(const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CUtensorMap tm_xl,
                  const __grid_constant__ CUtensorMap tm_ah, const __grid_constant__ CUtensorMap tm_al, TcArgs a) {
@@ -148,9 +159,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // 1024-byte aligned operand regions (the swizzle atoms assume it).
     unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
     unsigned char* sAh = base;
-    unsigned char* sAl = sAh + a.b_bytes;
-    unsigned char* sX = sAl + a.b_bytes;   // stage s: Xh at s*(1+need_lo)*x_bytes, Xl right after
-    const uint32_t stage_bytes = a.x_bytes * (a.need_lo ? 2u : 1u);
+    unsigned char* sAl = sAh + (kStream ? 0 : a.b_bytes);
+    // resident: stage s = Xh at s*(1+need_lo)*x_bytes, Xl right after;
+    // streaming: stage s = [Xh slice][Xl slice][Ah slice][Al slice]
+    unsigned char* sX = kStream ? base : sAl + a.b_bytes;
+    const uint32_t stage_bytes = kStream ? a.stage_bytes : a.x_bytes * (a.need_lo ? 2u : 1u);
     unsigned char* tail = sX + (size_t)a.stages * stage_bytes;
     uint64_t* full = reinterpret_cast<uint64_t*>(tail);
     uint64_t* empty = full + 2;
@@ -176,14 +189,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
         mbar_init(bfull, 1);
         *abort_flag = 0;
-        *list_top = 0;
+        *list_top = a.list_continue ? a.relist_cnt[blockIdx.x] : 0u;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     for (int c = tid; c < a.LMp; c += TC_THREADS) {
         cmin[c] = INT_MAX;
         cmax[c] = INT_MIN;
-        s_an[c] = c < a.LM ? __ldg(a.anorm + c) : 0.0f;
-        s_b[c] = c < a.LM ? __ldg(a.b + c) : 0.0f;
+        s_an[c] = c < a.LM ? __ldg(a.anorm + a.col0 + c) : 0.0f;
+        s_b[c] = c < a.LM ? __ldg(a.b + a.col0 + c) : 0.0f;
     }
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_ptr)),
@@ -197,7 +210,57 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const uint32_t tmem = *tmem_ptr;
     const int katoms = a.Dp / 64, ksteps = a.Dp / 16;
 
-    if (warp == 0 && lane == 0) {
+    if (kStream && warp == 0 && lane == 0) {
+        // ---- TMA producer, streaming: every tile, every K slice of X and A ----
+        const uint32_t xb = 16384u;   // one X slice: 128 rows x 128 bytes
+        int i = 0;
+        for (int tile = blockIdx.x; tile < a.ntiles && !*abort_flag; tile += gridDim.x) {
+            for (int k = 0; k < katoms; ++k, ++i) {
+                const int s = i % a.stages;
+                if (i >= a.stages &&
+                    !mbar_wait(empty + s, (uint32_t)((i / a.stages - 1) & 1), abort_flag, a.err, true))
+                    break;
+                unsigned char* st = sX + (size_t)s * stage_bytes;
+                unsigned char* sa = st + xb * (a.need_lo ? 2u : 1u);
+                mbar_expect_tx(full + s, stage_bytes);
+                tma_load_2d(st, &tm_xh, full + s, k * 64, tile * TC_M);
+                if (a.need_lo) tma_load_2d(st + xb, &tm_xl, full + s, k * 64, tile * TC_M);
+                tma_load_2d(sa, &tm_ah, full + s, k * 64, a.col0);
+                tma_load_2d(sa + a.a_chunk, &tm_al, full + s, k * 64, a.col0);
+            }
+        }
+    } else if (kStream && warp == 1 && lane == 0) {
+        // ---- MMA issuer, streaming ----
+        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(a.LMp >> 3) << 17) |
+                               ((uint32_t)(TC_M >> 4) << 24);
+        const uint32_t xb = 16384u;
+        int i = 0, t = 0;
+        bool ok = true;
+        for (int tile = blockIdx.x; tile < a.ntiles && ok; tile += gridDim.x, ++t) {
+            const int acc = t & 1;
+            if (t >= 2 && !mbar_wait(tempty + acc, (uint32_t)(((t >> 1) - 1) & 1), abort_flag, a.err, true)) break;
+            const uint32_t d = tmem + (uint32_t)(acc * a.LMp);
+            for (int k = 0; k < katoms; ++k, ++i) {
+                const int s = i % a.stages;
+                if (!mbar_wait(full + s, (uint32_t)((i / a.stages) & 1), abort_flag, a.err, true)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t xh = smem_u32(sX + (size_t)s * stage_bytes);
+                const uint32_t ah = xh + xb * (a.need_lo ? 2u : 1u), al = ah + a.a_chunk;
+                for (int ks = 0; ks < 4; ++ks) {
+                    const uint32_t o = (uint32_t)(ks * 32);
+                    umma_bf16(d, sw128_desc(xh + o), sw128_desc(ah + o), idesc, (k > 0 || ks > 0) ? 1u : 0u);
+                    umma_bf16(d, sw128_desc(xh + o), sw128_desc(al + o), idesc, 1u);
+                    if (a.need_lo) umma_bf16(d, sw128_desc(xh + xb + o), sw128_desc(ah + o), idesc, 1u);
+                }
+                umma_commit(empty + s);
+            }
+            if (!ok) break;
+            umma_commit(tfull + acc);
+        }
+    } else if (!kStream && warp == 0 && lane == 0) {
         // ---- TMA producer ----
         mbar_expect_tx(bfull, 2 * a.b_bytes);
         for (int k = 0; k < katoms; ++k) {
@@ -216,7 +279,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 if (a.need_lo) tma_load_2d(xh + a.x_bytes + (size_t)k * TC_M * 128, &tm_xl, full + s, k * 64, tile * TC_M);
             }
         }
-    } else if (warp == 1 && lane == 0) {
+    } else if (!kStream && warp == 1 && lane == 0) {
         // ---- MMA issuer ----
         // kind::f16 instruction descriptor: FP32 accumulator, bf16 A and B,
         // both K-major, N = LMp, M = 128.
@@ -266,7 +329,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 const int c0 = ch * 16;
                 uint32_t r[16];
                 tmem_ld16(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(acc * a.LMp + c0), r);
-                int32_t* out = a.codes + (int64_t)c0 * a.N + n;
+                int32_t* out = a.codes + (int64_t)(a.col0 + c0) * a.N + n;
                 uint32_t unsure = 0;
                 int32_t mylo = INT_MAX, myhi = INT_MIN;
 #pragma unroll
@@ -330,7 +393,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 const int nwords = (ch1 - ch0 + 1) >> 1;
                 for (int w = 0; w < nwords && nuns; ++w) {
                     for (uint32_t m = my_mask[w * TC_EPI_WARPS * 32]; m; m &= m - 1) {
-                        const int c = ch0 * 16 + w * 32 + (__ffs(m) - 1);
+                        const int c = a.col0 + ch0 * 16 + w * 32 + (__ffs(m) - 1);
                         if (pos < a.relist_cap) region[pos] = ((unsigned long long)n << 16) | (unsigned)c;
                         ++pos;
                     }
@@ -340,8 +403,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
     __syncthreads();
     for (int c = tid; c < a.LM; c += TC_THREADS) {
-        a.pmin[(int64_t)blockIdx.x * a.LM + c] = cmin[c];
-        a.pmax[(int64_t)blockIdx.x * a.LM + c] = cmax[c];
+        a.pmin[(int64_t)blockIdx.x * a.LMtot + a.col0 + c] = cmin[c];
+        a.pmax[(int64_t)blockIdx.x * a.LMtot + a.col0 + c] = cmax[c];
     }
     if (tid == 0) a.relist_cnt[blockIdx.x] = *list_top;
     tc_fence_after();
@@ -555,11 +618,104 @@ cudaError_t launch_project_tc(const TcPlan& p, int need_lo, int64_t N, int D, in
     a.err = err;
     a.b_bytes = p.b_bytes;
     a.x_bytes = p.x_bytes;
+    a.col0 = 0;
+    a.LMtot = LM;
+    a.stage_bytes = 0;
+    a.a_chunk = 0;
+    a.list_continue = 0;
     const int smem = (int)p.smem[need_lo];
-    cudaError_t e = cudaFuncSetAttribute(k_project_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaError_t e = cudaFuncSetAttribute(k_project_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
-    k_project_tc<<<p.grid, TC_THREADS, smem, st>>>(mxh, mxl, mah, mal, a);
+    k_project_tc<false><<<p.grid, TC_THREADS, smem, st>>>(mxh, mxl, mah, mal, a);
     return cudaGetLastError();
+}
+
+TcStreamPlan tc_plan_stream(int64_t N, int D, int LM, int num_sms, int max_smem) {
+    TcStreamPlan p{};
+    p.Dp = (D + 63) / 64 * 64;
+    p.LMp = (LM + 15) / 16 * 16;
+    p.ok = N >= 1024 && p.Dp <= 16384 && LM <= 65535 && N < (1ll << 47);
+    if (!p.ok) return p;
+    p.ntiles = (int)((N + TC_M - 1) / TC_M);
+    p.grid = std::min(p.ntiles, num_sms);
+    p.ok = false;
+    for (int need_lo = 0; need_lo < 2; ++need_lo) {
+        // widest column block whose two-stage (or one-stage) ring fits
+        for (int blk = 256; blk >= 16; blk -= 16) {
+            const size_t stage = 16384u * (need_lo ? 2u : 1u) + 2u * (size_t)blk * 128u;
+            const size_t tail = 128 + 16 * (size_t)blk + 8 * 4 * TC_EPI_WARPS * 32;
+            int stages = 2;
+            while (stages > 0 && 1024 + stages * stage + tail > (size_t)max_smem) --stages;
+            if (stages == 0) continue;
+            p.blk[need_lo] = std::min(blk, p.LMp);
+            p.stages[need_lo] = stages;
+            p.smem[need_lo] = 1024 + stages * (16384u * (need_lo ? 2u : 1u) + 2u * (size_t)p.blk[need_lo] * 128u) +
+                              128 + 16 * (size_t)p.blk[need_lo] + 8 * 4 * TC_EPI_WARPS * 32;
+            break;
+        }
+    }
+    p.ok = p.stages[1] >= 1 && p.stages[0] >= 1;
+    return p;
+}
+
+cudaError_t launch_project_tc_stream(const TcStreamPlan& p, int need_lo, int64_t N, int D, int LM, const void* xh,
+                                     const void* xl, const void* ah, const void* al, const float* b,
+                                     const float* anorm, const float* xnorm, float W, float kappa, int32_t* codes,
+                                     int32_t* pmin, int32_t* pmax, unsigned long long* relist,
+                                     unsigned long long relist_cap, unsigned int* relist_cnt, int* err,
+                                     cudaStream_t st) {
+    const int blk = p.blk[need_lo];
+    CUtensorMap mxh, mxl;
+    if (!make_map(&mxh, xh, p.Dp, N, TC_M) || !make_map(&mxl, xl, p.Dp, N, TC_M)) return cudaErrorNotSupported;
+    const int smem = (int)p.smem[need_lo];
+    cudaError_t e = cudaFuncSetAttribute(k_project_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(relist_cnt, 0, sizeof(unsigned int) * (size_t)p.grid, st);
+    if (e != cudaSuccess) return e;
+    for (int col0 = 0; col0 < LM; col0 += blk) {
+        const int lmc = std::min(blk, LM - col0);      // columns of this launch
+        const int lmp = (lmc + 15) / 16 * 16;           // padded to the MMA's N granularity
+        CUtensorMap mah, mal;
+        if (!make_map(&mah, ah, p.Dp, (uint64_t)p.LMp, (uint32_t)lmp) ||
+            !make_map(&mal, al, p.Dp, (uint64_t)p.LMp, (uint32_t)lmp))
+            return cudaErrorNotSupported;
+        TcArgs a;
+        a.N = N;
+        a.D = D;
+        a.Dp = p.Dp;
+        a.LM = lmc;
+        a.LMp = lmp;
+        a.ntiles = p.ntiles;
+        a.need_lo = need_lo;
+        a.stages = p.stages[need_lo];
+        int tc = 32;
+        while (tc < 2 * lmp) tc <<= 1;
+        a.tmem_cols = tc;
+        a.W = W;
+        a.kappa = kappa;
+        a.b = b;
+        a.anorm = anorm;
+        a.xnorm = xnorm;
+        a.codes = codes;
+        a.pmin = pmin;
+        a.pmax = pmax;
+        a.relist = relist;
+        a.relist_cap = relist_cap;
+        a.relist_cnt = relist_cnt;
+        a.inv_w = 1.0f / W;
+        a.err = err;
+        a.b_bytes = 0;
+        a.x_bytes = 16384u;
+        a.col0 = col0;
+        a.LMtot = LM;
+        a.a_chunk = (uint32_t)lmp * 128u;
+        a.stage_bytes = 16384u * (need_lo ? 2u : 1u) + 2u * a.a_chunk;
+        a.list_continue = 1;
+        k_project_tc<true><<<p.grid, TC_THREADS, smem, st>>>(mxh, mxl, mah, mal, a);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t launch_tc_recompute(const float* X, int64_t N, int D, int LM, const float* A, const float* b, float W,

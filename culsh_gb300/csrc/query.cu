@@ -68,6 +68,7 @@ __device__ int32_t lookup_row(const LookupView& lv, int l, const float* row) {
 #pragma unroll
     for (int w = 0; w < kMaxKW; ++w) key[w] = 0;
     const int M = lv.M, KW = lv.KW;
+    uint64_t hs = 0;
     for (int m = 0; m < M; ++m) {
         const int c = l * M + m;
         const float f = row[m];
@@ -77,9 +78,10 @@ __device__ int32_t lookup_row(const LookupView& lv, int l, const float* row) {
         if (ci < lo || ci > __ldg(lv.cmax + c)) return -1;
         const int bits = __ldg(lv.fbits + c);
         if (bits) key_put(key, __ldg(lv.foff + c), bits, (uint32_t)(ci - lo));
+        hs += (uint64_t)(uint32_t)(ci - lo) * __ldg(lv.rmul + c);
     }
     const uint32_t gmask = __ldg(lv.hmask + l);
-    const uint64_t hh = key_hash64(key, KW);
+    const uint64_t hh = hash_finish(hs);
     const uint32_t h = (uint32_t)hh;
     const uint32_t fp = slot_fp(hh);
     const unsigned long long* slots = lv.hslots + __ldg(lv.hoff + l);
@@ -219,9 +221,11 @@ __device__ __forceinline__ int highest_bit(uint64_t b) { return 63 - __clzll((lo
 
 struct FastProbeCtx {
     u128 hkey;
+    uint64_t h0;                        // additive lookup hash of the home key (before the mix)
     uint32_t ok0, okUp, okDn, allM;     // per-column range validity (M <= 32)
     const uint8_t* enc;                 // sorted delta i -> column | (up << 7); strided slice
     const unsigned long long* funit;    // this table's field units 2^foff (low, high)
+    const unsigned long long* rmul;     // this table's hash multipliers
 };
 
 __device__ __forceinline__ u128 unit_of(const unsigned long long* funit, int m) {
@@ -247,10 +251,23 @@ __device__ __forceinline__ bool probe_key(const FastProbeCtx& c, MaskT mask, u12
     return true;
 }
 
-__device__ __forceinline__ uint64_t key_hash128(u128 k, int KW) {
-    uint64_t h = mix64(kHashSeed ^ (uint64_t)k);
-    if (KW > 2) h = mix64(h ^ (uint64_t)(k >> 64));
-    return h;
+// Lookup hash of a probe mask (the home hash +- the multiplier of every
+// perturbed column); returns false when a column leaves [cmin, cmax].
+template <typename MaskT>
+__device__ __forceinline__ bool probe_hash(const FastProbeCtx& c, MaskT mask, uint64_t& hh) {
+    uint32_t up = 0, dn = 0;
+    for (MaskT b = mask; b; b &= b - 1) {
+        const int e = c.enc[lowest_bit(b) * PF];
+        if (e & 0x80) up |= 1u << (e & 0x3f);
+        else dn |= 1u << (e & 0x3f);
+    }
+    const uint32_t nu = up & ~dn, nd = dn & ~up;
+    if ((~(nu | nd) & c.allM & ~c.ok0) | (nu & ~c.okUp) | (nd & ~c.okDn)) return false;
+    uint64_t h = c.h0;
+    for (uint32_t b = nu; b; b &= b - 1) h += __ldg(c.rmul + lowest_bit(b));
+    for (uint32_t b = nd; b; b &= b - 1) h -= __ldg(c.rmul + lowest_bit(b));
+    hh = hash_finish(h);
+    return true;
 }
 
 __device__ __forceinline__ bool key_matches(const uint32_t* uk, u128 k, int KW) {
@@ -356,6 +373,8 @@ __global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
     c.allM = M >= 32 ? ~0u : ((1u << M) - 1);
     c.enc = enc;
     c.funit = lv.funit + 2 * l * M;
+    c.rmul = lv.rmul + l * M;
+    c.h0 = 0;
     bool distinct = true;
     for (int m = 0; m < M; ++m) {
         const int col = l * M + m;
@@ -371,6 +390,7 @@ __global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
         c.okUp |= (uint32_t)(h + 1 >= lo && h + 1 <= hi) << m;
         c.okDn |= (uint32_t)(h - 1 >= lo && h - 1 <= hi) << m;
         c.hkey += field_term(h - lo, __ldg(lv.foff + col));
+        c.h0 += (uint64_t)(h - lo) * __ldg(c.rmul + m);
     }
 
     if (T > 1) {
@@ -463,9 +483,8 @@ __global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
                     }
                 }
                 pm[j] = probe;
-                u128 k;
-                if (probe_key(c, probe, k)) {
-                    const uint64_t hh = key_hash128(k, KW);
+                uint64_t hh;
+                if (probe_hash(c, probe, hh)) {
                     hsv[j] = (uint32_t)hh & gmask;
                     fpv[j] = slot_fp(hh);
                     fw[j] = __ldg(slots + (uint64_t)hsv[j] * kGroupWords);

@@ -310,9 +310,10 @@ __global__ void k_bucket_sizes(const uint64_t* __restrict__ boff, const uint32_t
     sizes[g] = (uint32_t)(end - (int64_t)starts[g]);
 }
 
-__global__ void k_hash_build(const uint64_t* __restrict__ boff, const uint32_t* __restrict__ ukeys, int KW,
-                             const uint64_t* __restrict__ hoff, const uint32_t* __restrict__ hmask,
-                             unsigned long long* __restrict__ hslots, int* err) {
+__global__ void k_hash_build(const uint64_t* __restrict__ boff, const uint32_t* __restrict__ ukeys, int M, int KW,
+                             const uint16_t* __restrict__ foff, const uint8_t* __restrict__ fbits,
+                             const unsigned long long* __restrict__ rmul, const uint64_t* __restrict__ hoff,
+                             const uint32_t* __restrict__ hmask, unsigned long long* __restrict__ hslots, int* err) {
     const int l = blockIdx.y;
     const int64_t j = (int64_t)blockIdx.x * NT + threadIdx.x;
     const int64_t B = (int64_t)(boff[l + 1] - boff[l]);
@@ -321,7 +322,12 @@ __global__ void k_hash_build(const uint64_t* __restrict__ boff, const uint32_t* 
     uint32_t k[kMaxKW];
     for (int w = 0; w < KW; ++w) k[w] = key[w];
     const uint32_t gmask = hmask[l];
-    const uint64_t hh = key_hash64(k, KW);
+    uint64_t hs = 0;   // additive lookup hash over the key's fields
+    for (int m = 0; m < M; ++m) {
+        const int c = l * M + m;
+        hs += (uint64_t)key_get(k, __ldg(foff + c), __ldg(fbits + c)) * __ldg(rmul + c);
+    }
+    const uint64_t hh = hash_finish(hs);
     const uint32_t h = (uint32_t)hh;
     const uint32_t fp = slot_fp(hh);
     unsigned long long* slots = hslots + hoff[l];
@@ -539,11 +545,13 @@ cudaError_t launch_bucket_sizes(const uint64_t* boff, const uint32_t* starts, in
     return cudaGetLastError();
 }
 
-cudaError_t launch_hash_build(const uint64_t* boff, const uint32_t* ukeys, int L, int KW, int64_t maxB,
+cudaError_t launch_hash_build(const uint64_t* boff, const uint32_t* ukeys, int L, int M, int KW, int64_t maxB,
+                              const uint16_t* foff, const uint8_t* fbits, const unsigned long long* rmul,
                               const uint64_t* hoff, const uint32_t* hmask, unsigned long long* hslots, int* err,
                               cudaStream_t st) {
     if (maxB <= 0) return cudaSuccess;
-    k_hash_build<<<dim3(blocks_for(maxB), L), NT, 0, st>>>(boff, ukeys, KW, hoff, hmask, hslots, err);
+    k_hash_build<<<dim3(blocks_for(maxB), L), NT, 0, st>>>(boff, ukeys, M, KW, foff, fbits, rmul, hoff, hmask,
+                                                          hslots, err);
     return cudaGetLastError();
 }
 
