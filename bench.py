@@ -515,7 +515,7 @@ def run_culsh(args):
         from culsh_gb300 import synth
         pool = synth.dataset(args.config, n=16, q=max(65536, Q))[1]
         Ks = sorted({K, 10, 100})
-        Ts = sorted({1, T})
+        Ts = [1, 8, 32] if args.config == 5 else sorted({1, T})   # the serving workload's T mix
         serving = {"arrivals": "Poisson", "request_queries": "log-uniform 1..4096", "K": Ks, "T": Ts,
                    "slots": 4, "index": "the resident index above",
                    "runs": [serve_run(culsh, ht, pool, r, args.serve_seconds, Ks, Ts, seed=17 + i)

@@ -450,11 +450,12 @@ __global__ void k_tc_recompute(const float* __restrict__ X, int64_t N, int D, co
                                unsigned long long cap, const unsigned int* __restrict__ cnt, int regions, int LM,
                                int stage_a, int32_t* __restrict__ codes, int32_t* __restrict__ cmin,
                                int32_t* __restrict__ cmax, int* __restrict__ err) {
-    // A staged in shared memory with rows padded to D + 1 floats, so that
-    // the lanes of a warp (different columns, same d) hit different banks.
-    extern __shared__ float sA[];
+    // A staged in shared memory with padded rows, so that the lanes of a warp
+    // (different columns, same d) hit different banks: D + 4 floats when
+    // D % 4 == 0 (16-byte reads; column c starts at bank 4c mod 32), else D + 1.
+    extern __shared__ __align__(16) float sA[];
     __shared__ int32_t smin[1024], smax[1024];   // per-column ranges of this block (LM <= 1024 here)
-    const int Dq = D + 1;
+    const int Dq = (D & 3) == 0 ? D + 4 : D + 1;
     const bool block_range = LM <= 1024;
     if (block_range)
         for (int c = threadIdx.x; c < LM; c += blockDim.x) {
@@ -478,10 +479,11 @@ __global__ void k_tc_recompute(const float* __restrict__ X, int64_t N, int D, co
             const float* av = sA + (int64_t)c * Dq;
             for (int d = 0; d < D; d += 4) {
                 const float4 x4 = __ldg(reinterpret_cast<const float4*>(x + d));
-                acc = __fmaf_rn(x4.x, av[d], acc);
-                acc = __fmaf_rn(x4.y, av[d + 1], acc);
-                acc = __fmaf_rn(x4.z, av[d + 2], acc);
-                acc = __fmaf_rn(x4.w, av[d + 3], acc);
+                const float4 a4 = *reinterpret_cast<const float4*>(av + d);
+                acc = __fmaf_rn(x4.x, a4.x, acc);
+                acc = __fmaf_rn(x4.y, a4.y, acc);
+                acc = __fmaf_rn(x4.z, a4.z, acc);
+                acc = __fmaf_rn(x4.w, a4.w, acc);
             }
         } else if (stage_a) {
             const float* av = sA + (int64_t)c * Dq;
@@ -721,7 +723,7 @@ cudaError_t launch_project_tc_stream(const TcStreamPlan& p, int need_lo, int64_t
 cudaError_t launch_tc_recompute(const float* X, int64_t N, int D, int LM, const float* A, const float* b, float W,
                                 const unsigned long long* list, unsigned long long cap, const unsigned int* cnt,
                                 int regions, int32_t* codes, int32_t* cmin, int32_t* cmax, int* err, cudaStream_t st) {
-    const size_t smem = sizeof(float) * (size_t)LM * (D + 1);
+    const size_t smem = sizeof(float) * (size_t)LM * ((D & 3) == 0 ? D + 4 : D + 1);
     const int stage_a = smem <= 200 * 1024;
     if (stage_a) {
         cudaError_t e = cudaFuncSetAttribute(k_tc_recompute, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

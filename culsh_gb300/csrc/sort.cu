@@ -14,7 +14,8 @@
 // then emits bucket starts, sizes and unique keys, and an open-addressing hash
 // over the unique keys serves exact-code lookups at query time.
 //
-// Every pass streams keys and ids once in and once out: HBM bound.
+// Every pass streams keys and ids once in and once out (the digit's own
+// word is read once): HBM bound.
 #include <algorithm>
 #include <climits>
 
@@ -125,7 +126,7 @@ __global__ void k_sort_digit_base(const uint32_t* __restrict__ hist, uint32_t* _
 // One LSD digit pass over all tables. Tiles are taken in launch order from a
 // global counter, so every tile's predecessors have started before it and the
 // look-back wait always ends; it is bounded anyway (kErrSpin).
-__global__ void __launch_bounds__(NT) k_sort_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+__global__ void __launch_bounds__(NT, 3) k_sort_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
                                                   uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
                                                   int64_t N, int L, int KW, int tiles, int word, int shift,
                                                   const uint32_t* __restrict__ base, int passes, int pass,
@@ -134,6 +135,7 @@ __global__ void __launch_bounds__(NT) k_sort_pass(const uint32_t* __restrict__ k
     __shared__ uint32_t tstart[256];
     __shared__ uint32_t gadd[256];
     __shared__ uint32_t buf[SP_TILE];
+    __shared__ uint32_t wtile[SP_TILE];
     __shared__ uint8_t sdig[SP_TILE];
     __shared__ uint32_t ws[SP_WARPS];
     __shared__ uint32_t s_vb;
@@ -153,7 +155,9 @@ __global__ void __launch_bounds__(NT) k_sort_pass(const uint32_t* __restrict__ k
 #pragma unroll
     for (int i = 0; i < SP_ITEMS; ++i) {
         const int e = warp * (32 * SP_ITEMS) + i * 32 + lane;
-        dig[i] = (e < nvalid) ? ((kw[e] >> shift) & 255u) : 256u;
+        const uint32_t w = (e < nvalid) ? kw[e] : 0u;
+        wtile[e] = w;   // the digit's key word, kept for its own scatter
+        dig[i] = (e < nvalid) ? ((w >> shift) & 255u) : 256u;
     }
     // Stable warp-level ranking: element order inside a warp chunk is
     // (item, lane), which is the element order of the tile.
@@ -219,18 +223,41 @@ __global__ void __launch_bounds__(NT) k_sort_pass(const uint32_t* __restrict__ k
             sdig[pos[i]] = (uint8_t)d;
         }
     }
+    __syncthreads();
+    // Global destination of tile position s = tid + k * NT (digit runs are
+    // contiguous), computed once for all components.
+    uint32_t doff[SP_ITEMS];
+#pragma unroll
+    for (int k = 0; k < SP_ITEMS; ++k) {
+        const int sp = tid + k * NT;
+        doff[k] = sp < nvalid ? gadd[sdig[sp]] + (uint32_t)sp : 0u;
+    }
     // Scatter each component (ids, then key words) through shared memory so
-    // that the global writes of one digit run are contiguous.
-    for (int comp = 0; comp <= KW; ++comp) {
+    // that the global writes of one digit run are contiguous; the next
+    // component's loads are issued before the current one is written out.
+    auto load_comp = [&](int comp, uint32_t (&v)[SP_ITEMS]) {
         const uint32_t* src = (comp == 0 ? vin : kin + (comp - 1) * LN) + seg + t0;
-        uint32_t* dst = (comp == 0 ? vout : kout + (comp - 1) * LN) + seg;
 #pragma unroll
         for (int i = 0; i < SP_ITEMS; ++i) {
             const int e = warp * (32 * SP_ITEMS) + i * 32 + lane;
-            if (dig[i] < 256) buf[pos[i]] = src[e];
+            // the digit's own word is already in shared memory
+            v[i] = dig[i] < 256 ? (comp == word + 1 ? wtile[e] : src[e]) : 0u;
         }
+    };
+    uint32_t cur[SP_ITEMS];
+    load_comp(0, cur);
+    for (int comp = 0; comp <= KW; ++comp) {
+        uint32_t* dst = (comp == 0 ? vout : kout + (comp - 1) * LN) + seg;
+#pragma unroll
+        for (int i = 0; i < SP_ITEMS; ++i)
+            if (dig[i] < 256) buf[pos[i]] = cur[i];
+        if (comp < KW) load_comp(comp + 1, cur);
         __syncthreads();
-        for (int s = tid; s < nvalid; s += NT) dst[gadd[sdig[s]] + s] = buf[s];
+#pragma unroll
+        for (int k = 0; k < SP_ITEMS; ++k) {
+            const int sp = tid + k * NT;
+            if (sp < nvalid) dst[doff[k]] = buf[sp];
+        }
         __syncthreads();
     }
 }
