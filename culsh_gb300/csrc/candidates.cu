@@ -47,11 +47,15 @@ __global__ void __launch_bounds__(PT_PLAN) k_plan_items(WsArgs a) {
     const int q0 = blockIdx.x * PT_PLAN;
     const int q = q0 + tid;
     uint32_t P = 0;
+    bool dense = false;
     if (q < a.Q) {
         const unsigned long long C = a.cnu[q];
-        P = C == 0 ? 0u : (uint32_t)min((unsigned long long)a.pmax, (C + a.chunk - 1) / a.chunk);
+        // near-exhaustive candidate sets go to the bitmap kernel instead
+        dense = C >= a.dense_min;
+        P = (C == 0 || dense) ? 0u : (uint32_t)min((unsigned long long)a.pmax, (C + a.chunk - 1) / a.chunk);
+        if (dense) a.dense_q[atomicAdd(a.n_dense, 1u)] = q;
     }
-    s_empty[tid] = q < a.Q && P == 0;
+    s_empty[tid] = q < a.Q && P == 0 && !dense;
     uint32_t x = P;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -169,70 +173,8 @@ __global__ void __launch_bounds__(WT) k_candidates_ws(WsArgs a) {
         float thr_d = FLT_MAX;
         uint32_t thr_i = 0;
         auto fp32_pass = [&](uint32_t cnt, auto idx_of, auto pre) {
-            const int per = vec ? 16 : 4;
-            for (uint32_t base = warp * per; base < cnt; base += WW * per) {
-                float dist = 0.f;
-                uint32_t id = 0;
-                bool own;
-                if (vec) {
-                    const uint32_t j = base + (lane >> 1);
-                    const int h = lane & 1;
-                    bool valid = j < cnt;
-                    const uint32_t ci = valid ? idx_of(j) : 0u;
-                    id = valid ? ulist[ci] : 0u;
-                    float pd = 0.f;
-                    const bool have = valid && pre(ci, pd);
-                    const float* rowp = a.X + (int64_t)id * D;
-                    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
-                    if (valid && !have) {
-                        for (int c = 4 * h; c < D; c += 8) {
-                            const float4 x = __ldg(reinterpret_cast<const float4*>(rowp + c));
-                            const float4 qv = *reinterpret_cast<const float4*>(qs + c);
-                            const float d0 = __fsub_rn(qv.x, x.x), d1 = __fsub_rn(qv.y, x.y);
-                            const float d2 = __fsub_rn(qv.z, x.z), d3 = __fsub_rn(qv.w, x.w);
-                            s0 = __fmaf_rn(d0, d0, s0);
-                            s1 = __fmaf_rn(d1, d1, s1);
-                            s2 = __fmaf_rn(d2, d2, s2);
-                            s3 = __fmaf_rn(d3, d3, s3);
-                        }
-                    }
-                    const float o0 = __shfl_xor_sync(0xffffffffu, s0, 1), o1 = __shfl_xor_sync(0xffffffffu, s1, 1);
-                    const float o2 = __shfl_xor_sync(0xffffffffu, s2, 1), o3 = __shfl_xor_sync(0xffffffffu, s3, 1);
-                    const float t0 = __fadd_rn(s0, o0), t1 = __fadd_rn(s1, o1), t2 = __fadd_rn(s2, o2),
-                                t3 = __fadd_rn(s3, o3);
-                    dist = have ? pd : __fadd_rn(__fadd_rn(t0, t2), __fadd_rn(t1, t3));
-                    own = valid && h == 0;
-                } else {
-                    const uint32_t j = base + (lane >> 3);
-                    const int r = lane & 7;
-                    const bool valid = j < cnt;
-                    const uint32_t ci = valid ? idx_of(j) : 0u;
-                    id = valid ? ulist[ci] : 0u;
-                    float pd = 0.f;
-                    const bool have = valid && pre(ci, pd);
-                    const float* rowp = a.X + (int64_t)id * D;
-                    float sacc = 0.f;
-                    if (valid && !have)
-                        for (int c = r; c < D; c += 8) {
-                            const float df = __fsub_rn(qs[c], __ldg(rowp + c));
-                            sacc = __fmaf_rn(df, df, sacc);
-                        }
-                    // every lane takes part in all three shuffles, whatever `have` is
-                    const float t = __fadd_rn(sacc, __shfl_xor_sync(0xffffffffu, sacc, 4));
-                    const float u = __fadd_rn(t, __shfl_xor_sync(0xffffffffu, t, 2));
-                    const float v = __fadd_rn(u, __shfl_xor_sync(0xffffffffu, u, 1));
-                    dist = have ? pd : v;
-                    own = valid && r == 0;
-                }
-                uint32_t want = __ballot_sync(0xffffffffu, own && lessp(dist, id, thr_d, thr_i));
-                while (want) {
-                    const int src = __ffs(want) - 1;
-                    want &= want - 1;
-                    const float cdv = __shfl_sync(0xffffffffu, dist, src);
-                    const uint32_t cid = __shfl_sync(0xffffffffu, id, src);
-                    if (lessp(cdv, cid, thr_d, thr_i)) warp_insert(wd, wi, n, K, cdv, cid, thr_d, thr_i);
-                }
-            }
+            fp32_dist_pass<WW>(a.X, D, qs, vec, cnt, idx_of, [&](uint32_t ci) { return ulist[ci]; }, pre, wd, wi, K,
+                               n, thr_d, thr_i);
         };
         if constexpr (!kBF16) {
             fp32_pass(U, [](uint32_t j) { return j; }, [](uint32_t, float&) { return false; });
@@ -451,6 +393,116 @@ __global__ void __launch_bounds__(WT) k_candidates_ws(WsArgs a) {
 
 }  // namespace
 
+// Dense form: a query whose non-unique candidates reach dense_min (a large
+// share of the dataset) is deduplicated in an N-bit bitmap in shared memory
+// rather than in id partitions; the bitmap is then compacted 8,192 bits at a
+// time into a candidate list for the exact distance pass. Persistent grid,
+// one query per CTA at a time.
+constexpr int DT = 256;
+constexpr int DW = DT / 32;
+
+__global__ void __launch_bounds__(DT, 1) k_candidates_dense(WsArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ GatherSmem<DT, GCH> s_gather;
+    __shared__ int s_q;
+    __shared__ uint32_t s_ws[DW], s_wn[DW];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int D = a.D, K = a.K, L = a.L, T = a.T;
+    const int Dp = (D + 3) & ~3;
+    const uint32_t nwords = (uint32_t)((a.N + 31) >> 5);
+    const uint32_t nwp = (nwords + 3) & ~3u;
+    float* qs = reinterpret_cast<float*>(smem);
+    uint32_t* bits = reinterpret_cast<uint32_t*>(qs + Dp);
+    uint32_t* clist = bits + nwp;                       // DT * 32 candidate ids
+    float* wd_all = reinterpret_cast<float*>(clist + DT * 32);
+    uint32_t* wi_all = reinterpret_cast<uint32_t*>(wd_all + DW * K);
+    float* wd = wd_all + warp * K;
+    uint32_t* wi = wi_all + warp * K;
+    const bool vec = (D & 3) == 0;
+    const unsigned int ndense = *a.n_dense;
+
+    for (;;) {
+        if (tid == 0) {
+            const unsigned int k = atomicAdd(a.dense_next, 1u);
+            s_q = k < ndense ? a.dense_q[k] : -1;
+        }
+        __syncthreads();
+        const int q = s_q;
+        if (q < 0) break;
+        for (int i = tid; i < Dp; i += DT) qs[i] = i < D ? a.queries[(int64_t)q * D + i] : 0.0f;
+        for (uint32_t i = tid; i < nwords; i += DT) bits[i] = 0u;
+        __syncthreads();
+        const BucketView bv{a.qbuckets, a.boff, a.starts, a.sizes, a.ids, a.N, L, T, a.Q};
+        gather_bucket_ids<DT, GCH>(bv, q, s_gather,
+                                   [&](uint32_t id) { atomicOr(&bits[id >> 5], 1u << (id & 31)); });
+        __syncthreads();
+
+        int n = 0;
+        float thr_d = FLT_MAX;
+        uint32_t thr_i = 0;
+        unsigned long long U = 0;   // unique candidates (summed by every thread alike)
+        for (uint32_t w0 = 0; w0 < nwords; w0 += DT) {
+            const uint32_t w = w0 + tid;
+            const uint32_t word = w < nwords ? bits[w] : 0u;
+            // block exclusive scan of the set-bit counts
+            const uint32_t c = __popc(word);
+            uint32_t x = c;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            if (lane == 31) s_ws[warp] = x;
+            __syncthreads();
+            uint32_t before = 0, total = 0;
+            for (int i = 0; i < DW; ++i) {
+                const uint32_t v = s_ws[i];
+                before += i < warp ? v : 0u;
+                total += v;
+            }
+            uint32_t k = before + x - c;
+            for (uint32_t m = word; m; m &= m - 1) clist[k++] = w * 32 + (uint32_t)(__ffs((int)m) - 1);
+            __syncthreads();
+            fp32_dist_pass<DW>(a.X, D, qs, vec, total, [](uint32_t j) { return j; },
+                               [&](uint32_t ci) { return clist[ci]; }, [](uint32_t, float&) { return false; }, wd,
+                               wi, K, n, thr_d, thr_i);
+            U += total;
+            __syncthreads();
+        }
+        if (lane == 0) s_wn[warp] = n;
+        __syncthreads();
+        if (warp == 0) {
+            for (int ww = 1; ww < DW; ++ww) {
+                const int nw = s_wn[ww];
+                for (int e = 0; e < nw; ++e) {
+                    const float d = wd_all[ww * K + e];
+                    const uint32_t id = wi_all[ww * K + e];
+                    if (!lessp(d, id, thr_d, thr_i)) break;
+                    warp_insert(wd, wi, n, K, d, id, thr_d, thr_i);
+                }
+            }
+            int32_t* oid = a.out_ids + (int64_t)q * K;
+            float* od = a.out_d + (int64_t)q * K;
+            for (int k2 = lane; k2 < K; k2 += 32) {
+                oid[k2] = k2 < n ? (int32_t)wi[k2] : -1;
+                od[k2] = k2 < n ? wd[k2] : FLT_MAX;
+            }
+            if (lane == 0) {
+                a.cu[q] = U;
+                atomicAdd(a.totals + 0, U);
+                atomicAdd(a.totals + 1, a.cnu[q]);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+size_t dense_smem_bytes(int64_t N, int D, int K) {
+    const size_t nwp = (size_t)((((N + 31) >> 5) + 3) & ~3ll);
+    return sizeof(float) * (size_t)((D + 3) & ~3) + 4 * nwp + 4 * (size_t)DT * 32 +
+           (size_t)DW * K * (sizeof(float) + sizeof(uint32_t));
+}
+
 size_t ws_smem_bytes(int D, int K, int wt, int bf16, int slots) {
     const size_t cap = (size_t)slots / 2;
     return sizeof(float) * (size_t)((D + 3) & ~3) + sizeof(uint32_t) * ((size_t)slots + cap) +
@@ -541,6 +593,15 @@ cudaError_t launch_candidates_ws(const WsArgs& a, int grid, cudaStream_t st) {
 int ws_blocks_per_sm(int D, int K, int wt, int bf16, int slots) {
     if (slots == 8192) return bf16 ? ws_bps_w<true, 8192>(D, K, wt) : ws_bps_w<false, 8192>(D, K, wt);
     return bf16 ? ws_bps_w<true, 4096>(D, K, wt) : ws_bps_w<false, 4096>(D, K, wt);
+}
+
+cudaError_t launch_candidates_dense(const WsArgs& a, int grid, cudaStream_t st) {
+    static std::atomic<size_t> cap{0};   // dynamic shared memory this kernel is opted into
+    const size_t smem = dense_smem_bytes(a.N, a.D, a.K);
+    const cudaError_t e = opt_in_smem(k_candidates_dense, smem, cap);
+    if (e != cudaSuccess) return e;
+    k_candidates_dense<<<grid, DT, smem, st>>>(a);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_bf16_rows(const float* X, int64_t N, int D, uint16_t* xb, uint8_t* flag, cudaStream_t st) {

@@ -161,6 +161,8 @@ struct culsh_index {
     DevBuf<float> ws_anorm, ws_xnorm;
     DevBuf<int> ws_tcflags;
     double tc_predicted_open = 0.0;   // predicted share of codes the tensor-core bound leaves open
+    DevBuf<uint32_t> maxb;
+    uint32_t max_bucket = 0;          // largest bucket of any table (gates the dense candidate kernel)
     DevBuf<unsigned long long> ws_relist;
     DevBuf<unsigned int> ws_relist_cnt;
     long long tc_recomputed = -1;   // codes recomputed after the tensor-core pass (-1: SIMT path)
@@ -207,7 +209,7 @@ struct culsh_search {
     DevBuf<int> deferred;
     DevBuf<uint32_t> arena;
     // work-stealing candidate stage
-    DevBuf<int> q_items, q_off, item_q, part_n;
+    DevBuf<int> q_items, q_off, item_q, part_n, dense_q;
     DevBuf<unsigned int> q_done;
     DevBuf<uint8_t> item_p;
     DevBuf<float> part_d;
@@ -216,6 +218,7 @@ struct culsh_search {
     long long occ_key = -1;
     int occ_val = 1;
     long long rechecked = 0;   // BF16 form: candidates re-read in FP32 by the last search
+    int dense_queries = 0;     // queries of the last search that took the bitmap kernel
     SearchTune tune;
     bool use_graphs = true;
     cudaGraphExec_t gexec = nullptr;     // cached search graph and the plan it was captured from
@@ -590,7 +593,10 @@ int build_device(culsh_index* ix, const float* dX, cudaStream_t st, FILE* dbg) {
     CU_TRY(ix->sizes.reserve(totB));
     CU_TRY(ix->ukeys.reserve(totB * ix->KW));
     CU_TRY(launch_rl_write(skeys, N, L, ix->KW, ix->ws_toff.p, ix->boff.p, ix->starts.p, ix->ukeys.p, st));
-    CU_TRY(launch_bucket_sizes(ix->boff.p, ix->starts.p, N, L, maxB, ix->sizes.p, st));
+    CU_TRY(ix->maxb.reserve(1));
+    CU_TRY(cudaMemsetAsync(ix->maxb.p, 0, sizeof(uint32_t), st));
+    CU_TRY(launch_bucket_sizes(ix->boff.p, ix->starts.p, N, L, maxB, ix->sizes.p, ix->maxb.p, st));
+    CU_TRY(cudaMemcpyAsync(&ix->max_bucket, ix->maxb.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     TRY(build_hash(ix, st));
     CU_TRY(cudaEventRecord(ix->bev[4], st));
     TRY(read_err_flag(ix, st, "index"));
@@ -647,9 +653,11 @@ int ensure_device(culsh_index* ix, cudaStream_t st) {
     CU_TRY(cudaMemsetAsync(ix->err.p, 0, sizeof(int), st));
     ix->h_boff.assign(L + 1, 0);
     int64_t maxB = 0;
+    ix->max_bucket = 0;
     for (int l = 0; l < L; ++l) {
         ix->h_boff[l + 1] = ix->h_boff[l] + ix->buckets[l];
         maxB = std::max<int64_t>(maxB, ix->buckets[l]);
+        for (uint32_t v : ix->h_sizes[l]) ix->max_bucket = std::max(ix->max_bucket, v);
     }
     const uint64_t totB = ix->h_boff[L];
     CU_TRY(ix->ids.reserve((size_t)L * N));
@@ -768,7 +776,7 @@ struct SearchPlan {
     float* vals;
     ProbeArgs pa;
     int probe_generic;
-    int use_ws, ws_grid;
+    int use_ws, ws_grid, use_dense, dense_grid;
     CandArgs ca;
     WsArgs wa;
     unsigned long long* stats;
@@ -938,6 +946,23 @@ int plan_search(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* 
         a.wt = tu.ws_wt;
         a.slots = tu.ws_slots;
         a.bf16 = bf16;
+        // Dense form: queries with at least dense_min non-unique candidates
+        // (max(32768, N/16), or CULSH_DENSE_MIN) take the bitmap kernel,
+        // launched only when some query could reach it (L*T*largest bucket)
+        // and the N-bit bitmap fits the shared memory of a block.
+        unsigned long long dmin = std::max<unsigned long long>(32768ull, (unsigned long long)ix->N / 16);
+        if (const char* e = getenv("CULSH_DENSE_MIN")) dmin = std::max(1ll, atoll(e));
+        const bool dense_fits = dense_smem_bytes(ix->N, D, K) + 8192 <= (size_t)s->smem_optin;
+        const bool dense_reachable = (unsigned long long)L * T * ix->max_bucket >= dmin;
+        P.use_dense = dense_fits && dense_reachable;
+        a.dense_min = P.use_dense ? dmin : ~0ull;
+        if (P.use_dense) {
+            CU_TRY(s->dense_q.reserve(Q));
+            a.dense_q = s->dense_q.p;
+            P.dense_grid = s->sms;
+        }
+        a.n_dense = reinterpret_cast<unsigned int*>(s->stats.p + 7);
+        a.dense_next = reinterpret_cast<unsigned int*>(s->stats.p + 7) + 1;
         if (bf16) {
             // |d~ - d| <= c1 d~ + c2 (2 rho b1 + rho^2 b2) with gamma_n = n u / (1 - n u),
             // n = ceil(D/8) + 6 roundings along any path, u = 2^-24:
@@ -976,12 +1001,13 @@ int enqueue_search(const SearchPlan& P, cudaStream_t st, bool capturing, int* la
     if (P.use_ws) {
         CU_TRY(launch_plan_items(P.wa, st));
         CU_TRY(launch_candidates_ws(P.wa, P.ws_grid, st));
+        if (P.use_dense) CU_TRY(launch_candidates_dense(P.wa, P.dense_grid, st));
     } else {
         CU_TRY(launch_candidates(P.ca, st));
     }
     CU_TRY(cudaEventRecordWithFlags(P.ev[3], st, evf));
     CU_TRY(cudaMemcpyAsync(P.h_stats, P.stats, 8 * 8, cudaMemcpyDeviceToHost, st));
-    *launches = P.use_ws ? 4 : 3;
+    *launches = P.use_ws ? (P.use_dense ? 5 : 4) : 3;
     return CULSH_OK;
 }
 
@@ -1111,6 +1137,7 @@ int finish_search(culsh_search* s, const SearchPlan& P, cudaStream_t st) {
     s->tot_unique = s->h_stats.p[0];
     s->tot_nonunique = s->h_stats.p[1];
     s->rechecked = P.use_ws && P.wa.bf16 && !s->ws_overflow ? (long long)s->h_stats.p[6] : 0;
+    s->dense_queries = P.use_ws && P.use_dense && !s->ws_overflow ? (int)(s->h_stats.p[7] & 0xffffffffu) : 0;
     return CULSH_OK;
 }
 
@@ -1523,6 +1550,7 @@ long long culsh_search_device_bytes(culsh_search* s) {
     add(s->item_p);
     add(s->part_d);
     add(s->part_i);
+    add(s->dense_q);
     return (long long)b;
 }
 
@@ -1533,7 +1561,7 @@ long long culsh_search_estimate_bytes(const culsh_index* ix, int Q, int K, int T
     const size_t per_item = k * 8 + 4 + 4 + 1;
     size_t cap = std::max<size_t>(2 * q, kWsPartialBytes / per_item);
     cap = std::min(cap, q * kWsPartitions);
-    b += 12 * q + cap * per_item;
+    b += 16 * q + cap * per_item;   // per-query plan arrays, dense-query list, partial lists
     return (long long)b;
 }
 
@@ -1562,6 +1590,7 @@ int culsh_search_release(culsh_search* s) {
     s->item_p.release();
     s->part_d.release();
     s->part_i.release();
+    s->dense_q.release();
     s->Q = 0;
     s->searched = false;
     s->qb_host_valid = false;
@@ -1803,6 +1832,7 @@ int culsh_search_profile_get(culsh_search* s, culsh_search_profile* out) {
     out->candidates_mode = s->ws_used ? (s->ws_overflow ? 2 : 1) : 0;
     out->graph_mode = s->graph_mode;
     out->rechecked = s->rechecked;
+    out->dense_queries = s->dense_queries;
     return CULSH_OK;
 }
 

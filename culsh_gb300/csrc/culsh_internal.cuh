@@ -189,7 +189,7 @@ cudaError_t launch_rl_count(const uint32_t* keys, int64_t N, int L, int KW, uint
 cudaError_t launch_rl_write(const uint32_t* keys, int64_t N, int L, int KW, const uint32_t* tile_off,
                             const uint64_t* boff, uint32_t* starts, uint32_t* ukeys, cudaStream_t st);
 cudaError_t launch_bucket_sizes(const uint64_t* boff, const uint32_t* starts, int64_t N, int L, int64_t maxB,
-                                uint32_t* sizes, cudaStream_t st);
+                                uint32_t* sizes, uint32_t* max_size, cudaStream_t st);
 cudaError_t launch_hash_build(const uint64_t* boff, const uint32_t* ukeys, int L, int M, int KW, int64_t maxB,
                               const uint16_t* foff, const uint8_t* fbits, const unsigned long long* rmul,
                               const uint64_t* hoff, const uint32_t* hmask, unsigned long long* hslots, int* err,
@@ -283,7 +283,14 @@ struct WsArgs {
     const uint8_t* xflag;              // [N] 1 exact in bf16, 2 always re-check, 0 bound applies
     float e_c1, e_c2;                  // error-bound factors (rounded up)
     unsigned long long* rechecked;     // candidates whose FP32 row pass 2 re-read
+    // Dense form: queries with at least dense_min non-unique candidates
+    unsigned long long dense_min;      // ~0ull: never
+    int* dense_q;                      // [Q] queries routed to the bitmap kernel
+    unsigned int* n_dense;
+    unsigned int* dense_next;          // claim counter of the bitmap kernel
 };
+size_t dense_smem_bytes(int64_t N, int D, int K);
+cudaError_t launch_candidates_dense(const WsArgs& a, int grid, cudaStream_t st);
 size_t ws_smem_bytes(int D, int K, int wt, int bf16, int slots);
 int ws_blocks_per_sm(int D, int K, int wt, int bf16, int slots);
 cudaError_t launch_bf16_rows(const float* X, int64_t N, int D, uint16_t* xb, uint8_t* flag, cudaStream_t st);

@@ -327,14 +327,19 @@ __global__ void k_rl_write(const uint32_t* __restrict__ keys, int64_t N, int L, 
 }
 
 __global__ void k_bucket_sizes(const uint64_t* __restrict__ boff, const uint32_t* __restrict__ starts, int64_t N,
-                               uint32_t* __restrict__ sizes) {
+                               uint32_t* __restrict__ sizes, uint32_t* __restrict__ max_size) {
     const int l = blockIdx.y;
     const int64_t j = (int64_t)blockIdx.x * NT + threadIdx.x;
     const int64_t B = (int64_t)(boff[l + 1] - boff[l]);
-    if (j >= B) return;
-    const uint64_t g = boff[l] + j;
-    const int64_t end = (j + 1 < B) ? (int64_t)starts[g + 1] : N;
-    sizes[g] = (uint32_t)(end - (int64_t)starts[g]);
+    uint32_t sz = 0;
+    if (j < B) {
+        const uint64_t g = boff[l] + j;
+        const int64_t end = (j + 1 < B) ? (int64_t)starts[g + 1] : N;
+        sz = (uint32_t)(end - (int64_t)starts[g]);
+        sizes[g] = sz;
+    }
+    const uint32_t wmax = __reduce_max_sync(0xffffffffu, sz);   // largest bucket, one atomic per warp
+    if ((threadIdx.x & 31) == 0 && wmax) atomicMax(max_size, wmax);
 }
 
 __global__ void k_hash_build(const uint64_t* __restrict__ boff, const uint32_t* __restrict__ ukeys, int M, int KW,
@@ -566,9 +571,9 @@ cudaError_t launch_rl_write(const uint32_t* keys, int64_t N, int L, int KW, cons
 }
 
 cudaError_t launch_bucket_sizes(const uint64_t* boff, const uint32_t* starts, int64_t N, int L, int64_t maxB,
-                                uint32_t* sizes, cudaStream_t st) {
+                                uint32_t* sizes, uint32_t* max_size, cudaStream_t st) {
     if (maxB <= 0) return cudaSuccess;
-    k_bucket_sizes<<<dim3(blocks_for(maxB), L), NT, 0, st>>>(boff, starts, N, sizes);
+    k_bucket_sizes<<<dim3(blocks_for(maxB), L), NT, 0, st>>>(boff, starts, N, sizes, max_size);
     return cudaGetLastError();
 }
 

@@ -73,6 +73,84 @@ __device__ __forceinline__ void set_insert(uint32_t* hset, uint32_t mask, uint32
     }
 }
 
+// Exact FP32 squared distances, in the reference lane order
+// (cuLSH_Kernels.cu:301-348), of list entries [0, cnt) into this warp's sorted
+// top-K list (wd, wi, n, thr_d, thr_i). Entry j is candidate ci = idx_of(j)
+// with point id id_at(ci); an entry whose exact distance is already known
+// (pre(ci, d) returns true) is not loaded. With D % 4 == 0 two lanes share a
+// candidate and each holds four of the eight lane partials from 16-byte
+// loads; otherwise eight lanes share one. Every lane reaches every shuffle.
+// All lanes of the warp call this with the same arguments.
+template <int WW, class IdxOf, class IdAt, class Pre>
+__device__ __forceinline__ void fp32_dist_pass(const float* __restrict__ X, int D, const float* qs, bool vec,
+                                               uint32_t cnt, IdxOf idx_of, IdAt id_at, Pre pre, float* wd,
+                                               uint32_t* wi, int K, int& n, float& thr_d, uint32_t& thr_i) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int per = vec ? 16 : 4;
+    for (uint32_t base = warp * per; base < cnt; base += WW * per) {
+        float dist = 0.f;
+        uint32_t id = 0;
+        bool own;
+        if (vec) {
+            const uint32_t j = base + (lane >> 1);
+            const int h = lane & 1;
+            const bool valid = j < cnt;
+            const uint32_t ci = valid ? idx_of(j) : 0u;
+            id = valid ? id_at(ci) : 0u;
+            float pd = 0.f;
+            const bool have = valid && pre(ci, pd);
+            const float* rowp = X + (int64_t)id * D;
+            float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+            if (valid && !have) {
+                for (int c = 4 * h; c < D; c += 8) {
+                    const float4 x = __ldg(reinterpret_cast<const float4*>(rowp + c));
+                    const float4 qv = *reinterpret_cast<const float4*>(qs + c);
+                    const float d0 = __fsub_rn(qv.x, x.x), d1 = __fsub_rn(qv.y, x.y);
+                    const float d2 = __fsub_rn(qv.z, x.z), d3 = __fsub_rn(qv.w, x.w);
+                    s0 = __fmaf_rn(d0, d0, s0);
+                    s1 = __fmaf_rn(d1, d1, s1);
+                    s2 = __fmaf_rn(d2, d2, s2);
+                    s3 = __fmaf_rn(d3, d3, s3);
+                }
+            }
+            const float o0 = __shfl_xor_sync(0xffffffffu, s0, 1), o1 = __shfl_xor_sync(0xffffffffu, s1, 1);
+            const float o2 = __shfl_xor_sync(0xffffffffu, s2, 1), o3 = __shfl_xor_sync(0xffffffffu, s3, 1);
+            const float t0 = __fadd_rn(s0, o0), t1 = __fadd_rn(s1, o1), t2 = __fadd_rn(s2, o2), t3 = __fadd_rn(s3, o3);
+            const float v = __fadd_rn(__fadd_rn(t0, t2), __fadd_rn(t1, t3));
+            dist = have ? pd : v;
+            own = valid && h == 0;
+        } else {
+            const uint32_t j = base + (lane >> 3);
+            const int r = lane & 7;
+            const bool valid = j < cnt;
+            const uint32_t ci = valid ? idx_of(j) : 0u;
+            id = valid ? id_at(ci) : 0u;
+            float pd = 0.f;
+            const bool have = valid && pre(ci, pd);
+            const float* rowp = X + (int64_t)id * D;
+            float sacc = 0.f;
+            if (valid && !have)
+                for (int c = r; c < D; c += 8) {
+                    const float df = __fsub_rn(qs[c], __ldg(rowp + c));
+                    sacc = __fmaf_rn(df, df, sacc);
+                }
+            const float t = __fadd_rn(sacc, __shfl_xor_sync(0xffffffffu, sacc, 4));
+            const float u = __fadd_rn(t, __shfl_xor_sync(0xffffffffu, t, 2));
+            const float v = __fadd_rn(u, __shfl_xor_sync(0xffffffffu, u, 1));
+            dist = have ? pd : v;
+            own = valid && r == 0;
+        }
+        uint32_t want = __ballot_sync(0xffffffffu, own && lessp(dist, id, thr_d, thr_i));
+        while (want) {
+            const int src = __ffs(want) - 1;
+            want &= want - 1;
+            const float cdv = __shfl_sync(0xffffffffu, dist, src);
+            const uint32_t cid = __shfl_sync(0xffffffffu, id, src);
+            if (lessp(cdv, cid, thr_d, thr_i)) warp_insert(wd, wi, n, K, cdv, cid, thr_d, thr_i);
+        }
+    }
+}
+
 // Visits every candidate id of query q: the ids of every matched bucket over
 // all L tables and T probes, duplicates included (the reference's candidate
 // lists, cuLSH_SearchTables.cu:321-343). The L*T bucket slots are read in

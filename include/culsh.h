@@ -192,6 +192,8 @@ typedef struct culsh_search_profile {
                             per query after a partition overflowed            */
     int graph_mode;      /* 0: direct launches; 1: graph captured; 2: replayed */
     long long rechecked; /* BF16 distance form: candidates re-read in FP32     */
+    int dense_queries;   /* queries deduplicated in an N-bit bitmap (candidate
+                            sets of at least max(32768, N/16) ids)             */
 } culsh_search_profile;
 int culsh_search_profile_get(culsh_search* s, culsh_search_profile* out);
 

@@ -328,8 +328,54 @@ def test_work_stealing_large_candidate_sets(culsh):
     assert st.getTotalCandidates_unique() == int(ref["unique"].sum())
     assert st.getTotalCandidates_nonUnique() == int(ref["nonunique"].sum())
     assert int(ref["unique"][:5].min()) > 60000 and int(ref["nonunique"][5:8].max()) == 0
+    # 269,900 non-unique candidates per query (>= 32,768): the bitmap kernel
+    assert st.profile()["dense_queries"] == 8
     st.set_tuning(distance_bf16=1)
     st.search(queries, dataset=X)
     np.testing.assert_array_equal(st.getKnnIds(), ref["knn_ids"])
     np.testing.assert_array_equal(st.getKnnDistances(), ref["knn_dists"])
-    assert st.profile()["rechecked"] < st.getTotalCandidates_unique() // 10
+    # the bitmap kernel computes FP32 distances; partitions stay for the rest
+    assert st.profile()["dense_queries"] == 8
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_dense_bitmap_candidates_kernel(culsh, name, monkeypatch):
+    """Every query with a candidate routed to the bitmap kernel (threshold
+    forced to 1): same ids, distances, buckets and counts as the oracle."""
+    monkeypatch.setenv("CULSH_DENSE_MIN", "1")
+    c = load_case(name)
+    ht = build_index(culsh, c)
+    st = culsh.SearchTables()
+    st.reset(ht, int(c["K"]), int(c["T"]))
+    st.search(c["queries"], dataset=c["X"])
+    check_search(st, c)
+    np.testing.assert_array_equal(st.getKnnDistances(), c["knn_dists"])
+    assert st.profile()["dense_queries"] == int((c["nonunique"] > 0).sum())
+
+
+@pytest.mark.parametrize("N,D,L,M,W,integer", [(6000, 700, 4, 10, 30.0, False), (5000, 64, 20, 16, 8.0, False),
+                                               (4000, 300, 18, 16, 400.0, True)])
+def test_streaming_tensor_core_projection(culsh, N, D, L, M, W, integer, monkeypatch):
+    """Projection matrices too large for shared memory (D > 256 or L*M > 256)
+    take the streaming tensor-core kernel (K slices of X and A, column
+    blocks); every code, bucket and id still matches the oracle. (The
+    tensor-core path is forced: for some of these shapes the predicted share
+    of codes to recompute would otherwise select the SIMT kernel.)"""
+    import oracle
+    monkeypatch.setenv("CULSH_PROJECT_TC", "1")
+    rng = np.random.default_rng(N + D + L)
+    if integer:
+        X = np.clip(np.rint(rng.normal(20, 30, (N, D))), 0, 255).astype(np.float32)
+    else:
+        X = rng.normal(0, 1, (N, D)).astype(np.float32)
+    A = rng.normal(0, 1, (L, M, D)).astype(np.float32)
+    b = rng.uniform(0, W, (L, M)).astype(np.float32)
+    ht = culsh.HashTables()
+    ht.reset(N, D, L, M, W, A=A, b=b)
+    ht.index(X)
+    assert ht.profile()["tensor_cores"] == 1
+    ref = oracle.build_index(X, A, b, W)
+    np.testing.assert_array_equal(ht.getBuckets(), ref.buckets)
+    for l in range(L):
+        np.testing.assert_array_equal(ht.getBuckets_codes(l), ref.codes(l), err_msg=f"table {l}")
+        np.testing.assert_array_equal(ht.getBuckets_totalIndices(l), ref.ids(l), err_msg=f"table {l}")
