@@ -162,6 +162,7 @@ struct culsh_index {
     DevBuf<int> ws_tcflags;
     double tc_predicted_open = 0.0;   // predicted share of codes the tensor-core bound leaves open
     DevBuf<uint32_t> maxb;
+    PinBuf<uint32_t> h_maxb;
     uint32_t max_bucket = 0;          // largest bucket of any table (gates the dense candidate kernel)
     DevBuf<unsigned long long> ws_relist;
     DevBuf<unsigned int> ws_relist_cnt;
@@ -596,10 +597,12 @@ int build_device(culsh_index* ix, const float* dX, cudaStream_t st, FILE* dbg) {
     CU_TRY(ix->maxb.reserve(1));
     CU_TRY(cudaMemsetAsync(ix->maxb.p, 0, sizeof(uint32_t), st));
     CU_TRY(launch_bucket_sizes(ix->boff.p, ix->starts.p, N, L, maxB, ix->sizes.p, ix->maxb.p, st));
-    CU_TRY(cudaMemcpyAsync(&ix->max_bucket, ix->maxb.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    CU_TRY(ix->h_maxb.reserve(1));   // pinned: the copy does not block the host mid-build
+    CU_TRY(cudaMemcpyAsync(ix->h_maxb.p, ix->maxb.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     TRY(build_hash(ix, st));
     CU_TRY(cudaEventRecord(ix->bev[4], st));
-    TRY(read_err_flag(ix, st, "index"));
+    TRY(read_err_flag(ix, st, "index"));   // synchronises the stream
+    ix->max_bucket = *ix->h_maxb.p;
     ix->indexed = ix->dev_valid = true;
     ix->host_valid = false;
     ix->built_once = true;
