@@ -220,6 +220,7 @@ struct culsh_search {
     int occ_val = 1;
     long long rechecked = 0;   // BF16 form: candidates re-read in FP32 by the last search
     int dense_queries = 0;     // queries of the last search that took the bitmap kernel
+    bool direct_host = false;  // host search read queries / wrote results in host memory directly
     SearchTune tune;
     bool use_graphs = true;
     cudaGraphExec_t gexec = nullptr;     // cached search graph and the plan it was captured from
@@ -1473,6 +1474,20 @@ static int precheck_search(culsh_search* s, int Q) {
     return CULSH_OK;
 }
 
+// Whether kernels may read pageable host memory (Grace-Blackwell: through
+// the host page tables over NVLink-C2C). CULSH_NO_DIRECT_HOST disables its use.
+static bool direct_host_access() {
+    static int v = -1;
+    if (v < 0) {
+        int dev = 0, a = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess)
+            a = 0;
+        v = a ? 1 : 0;
+    }
+    return v == 1 && getenv("CULSH_NO_DIRECT_HOST") == nullptr;
+}
+
 int culsh_search_run(culsh_search* s, const float* queries, int Q, const float* dataset, FILE* dbg) {
     TRY(precheck_search(s, Q));
     if (!queries) return fail(CULSH_ERR_INVALID_ARGUMENT, "null queries");
@@ -1491,16 +1506,26 @@ int culsh_search_run(culsh_search* s, const float* queries, int Q, const float* 
     }
     if (!ix->dev_x()) return fail(CULSH_ERR_INVALID_ARGUMENT, "null dataset and no dataset on the device");
     const int D = ix->D, K = s->K;
-    CU_TRY(s->dq.reserve((size_t)Q * D));
-    CU_TRY(s->oids.reserve((size_t)Q * K));
-    CU_TRY(s->od.reserve((size_t)Q * K));
     CU_TRY(s->h_ids.reserve((size_t)Q * K));
     CU_TRY(s->h_d.reserve((size_t)Q * K));
-    CU_TRY(cudaMemcpyAsync(s->dq.p, queries, sizeof(float) * (size_t)Q * D, cudaMemcpyHostToDevice, st));
     if (dbg) fprintf(dbg, "[SearchTables::search]\tPerforming searching. (Q, K, T) = (%d, %d, %d)\n", Q, K, s->T);
-    TRY(search_device(s, s->dq.p, Q, s->oids.p, s->od.p, st));
-    CU_TRY(cudaMemcpyAsync(s->h_ids.p, s->oids.p, 4 * (size_t)Q * K, cudaMemcpyDeviceToHost, st));
-    CU_TRY(cudaMemcpyAsync(s->h_d.p, s->od.p, 4 * (size_t)Q * K, cudaMemcpyDeviceToHost, st));
+    if (direct_host_access() && ((uintptr_t)queries & 15u) == 0) {
+        // The GPU reads the caller's (pageable) queries through the host page
+        // tables and writes the results into the pinned result buffers: no
+        // staging copies. Query rows are read with 16-byte loads, hence the
+        // alignment condition.
+        TRY(search_device(s, queries, Q, s->h_ids.p, s->h_d.p, st));
+        s->direct_host = true;
+    } else {
+        CU_TRY(s->dq.reserve((size_t)Q * D));
+        CU_TRY(s->oids.reserve((size_t)Q * K));
+        CU_TRY(s->od.reserve((size_t)Q * K));
+        CU_TRY(cudaMemcpyAsync(s->dq.p, queries, sizeof(float) * (size_t)Q * D, cudaMemcpyHostToDevice, st));
+        TRY(search_device(s, s->dq.p, Q, s->oids.p, s->od.p, st));
+        CU_TRY(cudaMemcpyAsync(s->h_ids.p, s->oids.p, 4 * (size_t)Q * K, cudaMemcpyDeviceToHost, st));
+        CU_TRY(cudaMemcpyAsync(s->h_d.p, s->od.p, 4 * (size_t)Q * K, cudaMemcpyDeviceToHost, st));
+        s->direct_host = false;
+    }
     CU_TRY(cudaEventRecord(s->ev[4], st));
     CU_TRY(cudaStreamSynchronize(st));
     s->host_copy_timed = true;

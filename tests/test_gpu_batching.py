@@ -209,3 +209,27 @@ def test_wide_rows_shared_memory_opt_in(culsh):
         st.search(queries, dataset=X)
         np.testing.assert_array_equal(st.getKnnIds(), ref["knn_ids"])
         np.testing.assert_array_equal(st.getKnnDistances(), ref["knn_dists"])
+
+
+@pytest.mark.parametrize("name", ["mix_d16_t8", "heavy", "odd_d13"])
+def test_host_search_direct_and_copy_paths(culsh, name, monkeypatch):
+    """The host search reads 16-byte-aligned queries directly from host memory
+    (where the device has pageable memory access) and otherwise stages them;
+    an unaligned query buffer always stages. All give the oracle's results."""
+    c = load_case(name)
+    ht = build_index(culsh, c)
+    st = culsh.SearchTables()
+    st.reset(ht, int(c["K"]), int(c["T"]))
+    D = c["queries"].shape[1]
+    buf = np.zeros(c["queries"].size + 1, np.float32)
+    unaligned = buf[1:].reshape(c["queries"].shape)   # 4-byte offset from a 16-byte boundary
+    unaligned[...] = c["queries"]
+    assert unaligned.ctypes.data % 16 == 4
+    for env in (None, "1"):
+        if env:
+            monkeypatch.setenv("CULSH_NO_DIRECT_HOST", env)
+        for q in (c["queries"], unaligned):
+            st.search(q, dataset=c["X"])
+            check_search(st, c)
+            np.testing.assert_array_equal(st.getKnnDistances(), c["knn_dists"])
+    assert D > 0
