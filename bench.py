@@ -537,9 +537,12 @@ def run_culsh(args):
         el_max = reduce_max(dist, el, dev)
         host_ids = st_h.getKnnIds()
         assert np.array_equal(host_ids, ids.cpu().numpy()), "host and device API results differ"
+        hp = st_h.profile()["host_path"]
+        how = {1: "staged through device copies",
+               2: "read and written by the kernels in host memory (pageable memory access)"}.get(hp, str(hp))
         e2e = {"value": aggregate_throughput(Q * args.steps, world, el_max), "unit": UNIT,
                "h2d_bytes_per_step": int(Qm.nbytes), "d2h_bytes_per_step": int(Q * K * 8),
-               "path": "culsh_search_run (C ABI, pageable host buffers)"}
+               "path": "culsh_search_run (C ABI, pageable host buffers)", "host_buffers": how}
         del st_h, ht_h
 
     rpoint = rpoint_int = None

@@ -56,7 +56,7 @@ class _Profile(ctypes.Structure):
     _fields_ = [("project_ms", ctypes.c_float), ("probe_ms", ctypes.c_float), ("candidates_ms", ctypes.c_float),
                 ("launches", ctypes.c_int), ("deferred_queries", ctypes.c_int), ("key_words", ctypes.c_int),
                 ("candidates_mode", ctypes.c_int), ("graph_mode", ctypes.c_int), ("rechecked", ctypes.c_longlong),
-                ("dense_queries", ctypes.c_int)]
+                ("dense_queries", ctypes.c_int), ("host_path", ctypes.c_int)]
 
 
 class _Tuning(ctypes.Structure):

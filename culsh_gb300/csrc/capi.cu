@@ -133,6 +133,9 @@ struct culsh_index {
     const float* x_src = nullptr;  // host pointer the copy was made from
     const float* x_borrow = nullptr;
     DevBuf<float> dA, db;
+    DevBuf<float> dAT;           // A transposed: D rows of lmp floats, columns past L*M zero
+    std::vector<float> at_host;  // host staging of dAT (kept alive for the asynchronous copy)
+    int lmp = 0;                 // L*M rounded up to a multiple of 4
     bool proj_on_dev = false;
     DevBuf<uint16_t> xb;    // bf16 copy of the device dataset (search precision form), built on first use
     DevBuf<uint8_t> xflag;  // per row: 1 exact in bf16, 2 always re-check in FP32, 0 bound applies
@@ -220,7 +223,7 @@ struct culsh_search {
     int occ_val = 1;
     long long rechecked = 0;   // BF16 form: candidates re-read in FP32 by the last search
     int dense_queries = 0;     // queries of the last search that took the bitmap kernel
-    bool direct_host = false;  // host search read queries / wrote results in host memory directly
+    int host_path = 0;  // last search: 0 device buffers, 1 staged host copies, 2 direct host access
     SearchTune tune;
     bool use_graphs = true;
     cudaGraphExec_t gexec = nullptr;     // cached search graph and the plan it was captured from
@@ -278,6 +281,14 @@ int upload_projection(culsh_index* ix, cudaStream_t st) {
     CU_TRY(ix->db.reserve(LM));
     CU_TRY(cudaMemcpyAsync(ix->dA.p, ix->A.data(), sizeof(float) * LM * ix->D, cudaMemcpyHostToDevice, st));
     CU_TRY(cudaMemcpyAsync(ix->db.p, ix->b.data(), sizeof(float) * LM, cudaMemcpyHostToDevice, st));
+    const int D = ix->D;
+    const int lmp = (int)((LM + 3) & ~(size_t)3);
+    ix->at_host.assign((size_t)lmp * D, 0.0f);
+    for (size_t c = 0; c < LM; ++c)
+        for (int d = 0; d < D; ++d) ix->at_host[(size_t)d * lmp + c] = ix->A[c * D + d];
+    CU_TRY(ix->dAT.reserve((size_t)lmp * D));
+    CU_TRY(cudaMemcpyAsync(ix->dAT.p, ix->at_host.data(), sizeof(float) * lmp * D, cudaMemcpyHostToDevice, st));
+    ix->lmp = lmp;
     ix->proj_on_dev = true;
     return CULSH_OK;
 }
@@ -526,8 +537,8 @@ int build_device(culsh_index* ix, const float* dX, cudaStream_t st, FILE* dbg) {
         const int gx = project_grid_x(N);
         CU_TRY(ix->ws_pmin.reserve((size_t)gx * LM));
         CU_TRY(ix->ws_pmax.reserve((size_t)gx * LM));
-        CU_TRY(launch_project_fp32(dX, N, D, ix->dA.p, ix->db.p, LM, ix->W, ix->ws_codes.p, nullptr, ix->ws_pmin.p,
-                                   ix->ws_pmax.p, ix->err.p, st));
+        CU_TRY(launch_project_fp32(dX, N, D, ix->dAT.p, ix->lmp, ix->db.p, LM, ix->W, ix->ws_codes.p, nullptr,
+                                   ix->ws_pmin.p, ix->ws_pmax.p, ix->err.p, st));
         CU_TRY(launch_minmax_reduce(ix->ws_pmin.p, ix->ws_pmax.p, gx, LM, ix->cmin.p, ix->cmax.p, st));
     }
     ix->h_cmin.resize(LM);
@@ -773,9 +784,9 @@ int env_int(const char* name, int lo, int hi, int dflt) {
 // the key of the cached CUDA graph.
 struct SearchPlan {
     const float* dQ;
-    int Q, D, LM, proj_tile;
+    int Q, D, LM, proj_tile, lmp;
     float W;
-    const float* A;
+    const float* AT;
     const float* b;
     float* vals;
     ProbeArgs pa;
@@ -823,7 +834,8 @@ int plan_search(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* 
     P.LM = LM;
     P.proj_tile = tu.proj_tile;
     P.W = ix->W;
-    P.A = ix->dA.p;
+    P.AT = ix->dAT.p;
+    P.lmp = ix->lmp;
     P.b = ix->db.p;
     P.vals = s->vals.p;
     P.pa.vals = s->vals.p;
@@ -997,8 +1009,8 @@ int enqueue_search(const SearchPlan& P, cudaStream_t st, bool capturing, int* la
     CU_TRY(cudaMemsetAsync(P.cnu, 0, 8 * (size_t)P.Q, st));
     CU_TRY(cudaMemsetAsync(P.stats, 0, 8 * 8, st));
     CU_TRY(cudaEventRecordWithFlags(P.ev[0], st, evf));
-    CU_TRY(launch_project_fp32(P.dQ, P.Q, P.D, P.A, P.b, P.LM, P.W, nullptr, P.vals, nullptr, nullptr, nullptr, st,
-                               P.proj_tile));
+    CU_TRY(launch_project_fp32(P.dQ, P.Q, P.D, P.AT, P.lmp, P.b, P.LM, P.W, nullptr, P.vals, nullptr, nullptr,
+                               nullptr, st, P.proj_tile));
     CU_TRY(cudaEventRecordWithFlags(P.ev[1], st, evf));
     CU_TRY(launch_probe(P.pa, st));
     CU_TRY(cudaEventRecordWithFlags(P.ev[2], st, evf));
@@ -1155,6 +1167,7 @@ int search_device(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float
         std::lock_guard<std::mutex> lk(alloc_capture_mutex());
         TRY(plan_search(s, dQ, Q, d_ids, d_d, st, &P));
         s->host_copy_timed = false;
+        s->host_path = 0;
         TRY(run_plan(s, P, st));
     }
     return finish_search(s, P, st);
@@ -1515,7 +1528,7 @@ int culsh_search_run(culsh_search* s, const float* queries, int Q, const float* 
         // staging copies. Query rows are read with 16-byte loads, hence the
         // alignment condition.
         TRY(search_device(s, queries, Q, s->h_ids.p, s->h_d.p, st));
-        s->direct_host = true;
+        s->host_path = 2;
     } else {
         CU_TRY(s->dq.reserve((size_t)Q * D));
         CU_TRY(s->oids.reserve((size_t)Q * K));
@@ -1524,7 +1537,7 @@ int culsh_search_run(culsh_search* s, const float* queries, int Q, const float* 
         TRY(search_device(s, s->dq.p, Q, s->oids.p, s->od.p, st));
         CU_TRY(cudaMemcpyAsync(s->h_ids.p, s->oids.p, 4 * (size_t)Q * K, cudaMemcpyDeviceToHost, st));
         CU_TRY(cudaMemcpyAsync(s->h_d.p, s->od.p, 4 * (size_t)Q * K, cudaMemcpyDeviceToHost, st));
-        s->direct_host = false;
+        s->host_path = 1;
     }
     CU_TRY(cudaEventRecord(s->ev[4], st));
     CU_TRY(cudaStreamSynchronize(st));
@@ -1861,6 +1874,7 @@ int culsh_search_profile_get(culsh_search* s, culsh_search_profile* out) {
     out->graph_mode = s->graph_mode;
     out->rechecked = s->rechecked;
     out->dense_queries = s->dense_queries;
+    out->host_path = s->host_path;
     return CULSH_OK;
 }
 
@@ -1960,8 +1974,8 @@ extern "C" int culsh_search_run_device_noalloc(culsh_search* s, const float* d_q
 
     CU_TRY(cudaMemsetAsync(cnu, 0, 8 * (size_t)Q, st));
     CU_TRY(cudaMemsetAsync(stats, 0, 8 * 4, st));
-    CU_TRY(launch_project_fp32(d_queries, Q, D, ix->dA.p, ix->db.p, L * M, ix->W, nullptr, vals, nullptr, nullptr,
-                               nullptr, st));
+    CU_TRY(launch_project_fp32(d_queries, Q, D, ix->dAT.p, ix->lmp, ix->db.p, L * M, ix->W, nullptr, vals, nullptr,
+                               nullptr, nullptr, st));
     ProbeArgs pa;
     pa.vals = vals;
     pa.Q = Q;

@@ -118,8 +118,10 @@ struct LookupView {
 // codes != nullptr: floored codes [LM][n_pts] + per-block min/max partials
 // [grid_x][LM]; vals != nullptr: unfloored values [LM][n_pts].
 // tile picks the query-value tiling (0: 64x128, 1: 32x128, 2: 128x64 points x columns).
-cudaError_t launch_project_fp32(const float* X, int64_t n_pts, int D, const float* A, const float* b, int LM,
-                                float W, int32_t* codes, float* vals, int32_t* pmin, int32_t* pmax, int* err,
+// AT: the projection matrix transposed, D rows of lmp floats (lmp = LM rounded
+// up to a multiple of 4, columns past LM zero, 16-byte aligned).
+cudaError_t launch_project_fp32(const float* X, int64_t n_pts, int D, const float* AT, int lmp, const float* b,
+                                int LM, float W, int32_t* codes, float* vals, int32_t* pmin, int32_t* pmax, int* err,
                                 cudaStream_t st, int tile = 0);
 int project_grid_x(int64_t n_pts);
 cudaError_t launch_minmax_reduce(const int32_t* pmin, const int32_t* pmax, int nparts, int LM, int32_t* cmin,

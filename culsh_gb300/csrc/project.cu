@@ -23,29 +23,99 @@ constexpr int NT = 256;   // threads: 16 (points) x 16 (columns), each PT x CT o
 
 // Block tile BN = 16*PT points x BC = 16*CT columns, BK dimensions per
 // shared-memory stage. Index builds use PT = 8, CT = 4, BK = 16; query batches
-// use PT = 4, CT = 8, BK = 64 by default (fewer barriers and shared-memory
+// use PT = 4, CT = 8, BK = 32 by default (fewer barriers and shared-memory
 // loads per FMA, enough blocks for ten thousand queries), PT = 2 for small
 // batches or PT = 8, CT = 4, BK = 32 for large ones, as the search tuner picks.
+//
+// Thread (tx, ty) owns points 32*(i/2) + 2*tx + (i%2), i < PT, so that a
+// half-warp's float2 reads of the X tile cover 128 contiguous bytes (no bank
+// conflicts), and columns ty*CT .. ty*CT+CT-1. The projection matrix is read
+// transposed (AT[d][c], rows of lmp >= LM floats, columns past LM zero) with
+// coalesced float4 loads. The next stage's tiles are loaded into registers
+// while the current one is multiplied.
 template <bool kCodes, int PT, int CT, int BK>
 __global__ void __launch_bounds__(NT) k_project(const float* __restrict__ X, int64_t n_pts, int D,
-                                                const float* __restrict__ A, const float* __restrict__ b, int LM,
-                                                float W, int32_t* __restrict__ codes, float* __restrict__ vals,
-                                                int32_t* __restrict__ pmin, int32_t* __restrict__ pmax,
-                                                int* __restrict__ err) {
+                                                const float* __restrict__ AT, int lmp, const float* __restrict__ b,
+                                                int LM, float W, int32_t* __restrict__ codes,
+                                                float* __restrict__ vals, int32_t* __restrict__ pmin,
+                                                int32_t* __restrict__ pmax, int* __restrict__ err) {
     constexpr int BN = 16 * PT;
     constexpr int BC = 16 * CT;
-    constexpr int kTileBytes = BK * (BN + BC) * 4;
+    constexpr int XP = BN + 2;   // padded X row: the transposing stores conflict at most 4 ways
+    constexpr int XS = BN * BK / NT;        // X floats per thread per stage
+    constexpr int AV = BC * BK / 4 / NT;    // AT float4 per thread per stage
+    static_assert(PT % 2 == 0 && XS % 4 == 0 && AV >= 1 && BC * BK == AV * 4 * NT, "tile shape");
+    static_assert(BK % 16 == 0, "As must start 16-byte aligned");
+    constexpr int kTileBytes = BK * (XP + BC) * 4;
     constexpr int kStageBytes = BC * (BN + 1) * 4;
-    constexpr bool kUnion = kTileBytes >= kStageBytes;   // epilogue staging reuses the tiles
-    __shared__ __align__(16) unsigned char smem[kUnion ? kTileBytes : kTileBytes + kStageBytes];
-    float (*Xs)[BN] = reinterpret_cast<float (*)[BN]>(smem);
-    float (*As)[BC] = reinterpret_cast<float (*)[BC]>(smem + BK * BN * 4);
-    uint32_t (*Cs)[BN + 1] = reinterpret_cast<uint32_t (*)[BN + 1]>(smem + (kUnion ? 0 : kTileBytes));
+    // The epilogue's staging reuses the tiles (the main loop ends on a barrier).
+    __shared__ __align__(16) unsigned char smem[kTileBytes > kStageBytes ? kTileBytes : kStageBytes];
+    float (*Xs)[XP] = reinterpret_cast<float (*)[XP]>(smem);
+    float (*As)[BC] = reinterpret_cast<float (*)[BC]>(smem + BK * XP * 4);
+    uint32_t (*Cs)[BN + 1] = reinterpret_cast<uint32_t (*)[BN + 1]>(smem);
 
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     const int64_t n0 = (int64_t)blockIdx.x * BN;
     const int c0 = blockIdx.y * BC;
     const bool vec = (D & 3) == 0;
+
+    float xr[XS];
+    float4 ar[AV];
+    // Global -> registers. Vector path: BK/4 consecutive threads read one
+    // point's BK dimensions; scalar path (D % 4 != 0): BK threads do. Zero
+    // fill past D adds +-0 to a chain, which leaves it unchanged.
+    auto gload = [&](int d0) {
+        if (vec) {
+#pragma unroll
+            for (int r = 0; r < XS / 4; ++r) {
+                const int f = tid + NT * r, dq = f % (BK / 4), p = f / (BK / 4);
+                const int64_t gn = n0 + p;
+                const int gd = d0 + dq * 4;
+                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (gn < n_pts && gd < D) v = __ldg(reinterpret_cast<const float4*>(X + gn * D + gd));
+                xr[4 * r + 0] = v.x;
+                xr[4 * r + 1] = v.y;
+                xr[4 * r + 2] = v.z;
+                xr[4 * r + 3] = v.w;
+            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < XS; ++r) {
+                const int f = tid + NT * r, dd = f % BK, p = f / BK;
+                const int64_t gn = n0 + p;
+                const int gd = d0 + dd;
+                xr[r] = (gn < n_pts && gd < D) ? __ldg(X + gn * D + gd) : 0.0f;
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < AV; ++r) {
+            const int f = tid + NT * r, cq = f % (BC / 4), dd = f / (BC / 4);
+            const int gc = c0 + cq * 4, gd = d0 + dd;
+            ar[r] = (gc < lmp && gd < D) ? __ldg(reinterpret_cast<const float4*>(AT + (int64_t)gd * lmp + gc))
+                                         : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    };
+    auto sstore = [&]() {
+        if (vec) {
+#pragma unroll
+            for (int r = 0; r < XS / 4; ++r) {
+                const int f = tid + NT * r, dq = f % (BK / 4), p = f / (BK / 4);
+#pragma unroll
+                for (int e = 0; e < 4; ++e) Xs[dq * 4 + e][p] = xr[4 * r + e];
+            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < XS; ++r) {
+                const int f = tid + NT * r, dd = f % BK, p = f / BK;
+                Xs[dd][p] = xr[r];
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < AV; ++r) {
+            const int f = tid + NT * r, cq = f % (BC / 4), dd = f / (BC / 4);
+            *reinterpret_cast<float4*>(&As[dd][cq * 4]) = ar[r];
+        }
+    };
 
     float acc[PT][CT];
 #pragma unroll
@@ -53,45 +123,17 @@ __global__ void __launch_bounds__(NT) k_project(const float* __restrict__ X, int
 #pragma unroll
         for (int j = 0; j < CT; ++j) acc[i][j] = 0.0f;
 
+    gload(0);
     for (int d0 = 0; d0 < D; d0 += BK) {
-        // X tile: BN points x BK dims, transposed into Xs[dim][point]. Zero
-        // fill past D adds +-0 to a chain, which leaves it unchanged.
-        if (vec) {
-#pragma unroll
-            for (int r = 0; r < (BN * BK / 4 + NT - 1) / NT; ++r) {
-                const int f = tid + NT * r, p = f % BN, dq = f / BN;
-                if (f >= BN * BK / 4) break;
-                const int64_t gn = n0 + p;
-                const int gd = d0 + dq * 4;
-                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (gn < n_pts && gd < D) v = __ldg(reinterpret_cast<const float4*>(X + gn * D + gd));
-                Xs[dq * 4 + 0][p] = v.x;
-                Xs[dq * 4 + 1][p] = v.y;
-                Xs[dq * 4 + 2][p] = v.z;
-                Xs[dq * 4 + 3][p] = v.w;
-            }
-        } else {
-#pragma unroll
-            for (int r = 0; r < BN * BK / NT; ++r) {
-                const int f = tid + NT * r, p = f % BN, dd = f / BN;
-                const int64_t gn = n0 + p;
-                const int gd = d0 + dd;
-                Xs[dd][p] = (gn < n_pts && gd < D) ? __ldg(X + gn * D + gd) : 0.0f;
-            }
-        }
-#pragma unroll
-        for (int r = 0; r < BC * BK / NT; ++r) {
-            const int f = tid + NT * r, c = f % BC, dd = f / BC;
-            const int gc = c0 + c, gd = d0 + dd;
-            As[dd][c] = (gc < LM && gd < D) ? __ldg(A + (int64_t)gc * D + gd) : 0.0f;
-        }
+        sstore();
         __syncthreads();
+        if (d0 + BK < D) gload(d0 + BK);
 #pragma unroll 8
         for (int k = 0; k < BK; ++k) {
             float xv[PT];
 #pragma unroll
             for (int i = 0; i < PT; i += 2) {
-                const float2 x2 = *reinterpret_cast<const float2*>(&Xs[k][tx * PT + i]);
+                const float2 x2 = *reinterpret_cast<const float2*>(&Xs[k][16 * i + 2 * tx]);
                 xv[i] = x2.x;
                 xv[i + 1] = x2.y;
             }
@@ -122,6 +164,7 @@ __global__ void __launch_bounds__(NT) k_project(const float* __restrict__ X, int
         int32_t lo = INT_MAX, hi = INT_MIN;
 #pragma unroll
         for (int i = 0; i < PT; ++i) {
+            const int pi = 16 * (i & ~1) + 2 * tx + (i & 1);
             const float v = __fdiv_rn(__fsub_rn(acc[i][j], bc), W);
             uint32_t bits;
             if (kCodes) {
@@ -134,7 +177,7 @@ __global__ void __launch_bounds__(NT) k_project(const float* __restrict__ X, int
                 } else {
                     code = (int32_t)f;
                 }
-                if (n0 + tx * PT + i < n_pts && c < LM) {
+                if (n0 + pi < n_pts && c < LM) {
                     lo = min(lo, code);
                     hi = max(hi, code);
                 }
@@ -142,7 +185,7 @@ __global__ void __launch_bounds__(NT) k_project(const float* __restrict__ X, int
             } else {
                 bits = __float_as_uint(v);
             }
-            Cs[ty * CT + j][tx * PT + i] = bits;
+            Cs[ty * CT + j][pi] = bits;
         }
         if (kCodes) {
 #pragma unroll
@@ -212,22 +255,23 @@ __global__ void k_minmax_reduce(const int32_t* __restrict__ pmin, const int32_t*
 // 64-point tiles so that ten thousand queries still fill every SM.
 int project_grid_x(int64_t n_pts) { return (int)((n_pts + 127) / 128); }
 
-cudaError_t launch_project_fp32(const float* X, int64_t n_pts, int D, const float* A, const float* b, int LM,
-                                float W, int32_t* codes, float* vals, int32_t* pmin, int32_t* pmax, int* err,
+cudaError_t launch_project_fp32(const float* X, int64_t n_pts, int D, const float* AT, int lmp, const float* b,
+                                int LM, float W, int32_t* codes, float* vals, int32_t* pmin, int32_t* pmax, int* err,
                                 cudaStream_t st, int tile) {
     if (n_pts <= 0) return cudaSuccess;
+    if (lmp < LM || (lmp & 3) || ((uintptr_t)AT & 15)) return cudaErrorInvalidValue;
     if (codes) {
         k_project<true, 8, 4, 16><<<dim3(project_grid_x(n_pts), (LM + 63) / 64), NT, 0, st>>>(
-            X, n_pts, D, A, b, LM, W, codes, nullptr, pmin, pmax, err);
+            X, n_pts, D, AT, lmp, b, LM, W, codes, nullptr, pmin, pmax, err);
     } else if (tile == 1) {
         k_project<false, 2, 8, 64><<<dim3((unsigned)((n_pts + 31) / 32), (LM + 127) / 128), NT, 0, st>>>(
-            X, n_pts, D, A, b, LM, W, nullptr, vals, nullptr, nullptr, err);
+            X, n_pts, D, AT, lmp, b, LM, W, nullptr, vals, nullptr, nullptr, err);
     } else if (tile == 2) {
         k_project<false, 8, 4, 32><<<dim3((unsigned)((n_pts + 127) / 128), (LM + 63) / 64), NT, 0, st>>>(
-            X, n_pts, D, A, b, LM, W, nullptr, vals, nullptr, nullptr, err);
+            X, n_pts, D, AT, lmp, b, LM, W, nullptr, vals, nullptr, nullptr, err);
     } else {
-        k_project<false, 4, 8, 64><<<dim3((unsigned)((n_pts + 63) / 64), (LM + 127) / 128), NT, 0, st>>>(
-            X, n_pts, D, A, b, LM, W, nullptr, vals, nullptr, nullptr, err);
+        k_project<false, 4, 8, 32><<<dim3((unsigned)((n_pts + 63) / 64), (LM + 127) / 128), NT, 0, st>>>(
+            X, n_pts, D, AT, lmp, b, LM, W, nullptr, vals, nullptr, nullptr, err);
     }
     return cudaGetLastError();
 }

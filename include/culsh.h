@@ -194,6 +194,11 @@ typedef struct culsh_search_profile {
     long long rechecked; /* BF16 distance form: candidates re-read in FP32     */
     int dense_queries;   /* queries deduplicated in an N-bit bitmap (candidate
                             sets of at least max(32768, N/16) ids)             */
+    int host_path;       /* 0: device buffers (culsh_search_run_device*);
+                            1: host buffers staged through device copies;
+                            2: host buffers read and written by the kernels
+                            directly (device with pageable memory access,
+                            16-byte aligned queries)                          */
 } culsh_search_profile;
 int culsh_search_profile_get(culsh_search* s, culsh_search_profile* out);
 

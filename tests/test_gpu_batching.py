@@ -232,4 +232,9 @@ def test_host_search_direct_and_copy_paths(culsh, name, monkeypatch):
             st.search(q, dataset=c["X"])
             check_search(st, c)
             np.testing.assert_array_equal(st.getKnnDistances(), c["knn_dists"])
+            path = st.profile()["host_path"]
+            if env is None and q is c["queries"]:
+                assert path in (1, 2)   # 2 where the device reads pageable memory (Grace-Blackwell)
+            else:
+                assert path == 1
     assert D > 0
