@@ -78,7 +78,27 @@ def build(verbose: bool = False, force: bool = False) -> str:
         if verbose:
             print(" ".join(cmd), flush=True)
         subprocess.run(cmd, check=True)
+    build_cli(verbose)
     return LIB
+
+
+CLI_SRC = os.path.join(HERE, "culsh_main.cpp")
+CLI = os.path.join(HERE, "culsh_main")
+
+
+def build_cli(verbose: bool = False) -> str:
+    """The command-line program (culsh_main.cpp), a host C++ program over the
+    drop-in header, linked against libculsh.so next to it."""
+    if os.path.exists(CLI) and os.path.getmtime(CLI) >= max(
+            os.path.getmtime(CLI_SRC), os.path.getmtime(LIB), os.path.getmtime(os.path.join(INCLUDE, "cuLSH.h"))):
+        return CLI
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-I", INCLUDE, CLI_SRC, "-o", CLI, "-L", HERE, "-lculsh",
+           "-Wl,-rpath,$ORIGIN"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    subprocess.run(cmd, check=True)
+    return CLI
 
 
 if __name__ == "__main__":

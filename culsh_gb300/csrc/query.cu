@@ -19,6 +19,7 @@
 #include <atomic>
 #include <cfloat>
 #include <cstdlib>
+#include <utility>
 
 #include "culsh_internal.cuh"
 #include "topk_common.cuh"
@@ -325,6 +326,96 @@ __device__ void heap_order_strided(V val, int8_t* perm, int M2, int maxT) {
     }
 }
 
+// Batcher's odd-even merge-sort network for N keys (any N), built at compile
+// time: comparator i orders keys a[i] < b[i]. N = 8, 12, 16 give 19, 42, 63
+// comparators.
+template <int N>
+struct SortNet {
+    int a[64], b[64], n;
+    constexpr SortNet() : a{}, b{}, n(0) {
+        for (int p = 1; p < N; p <<= 1)
+            for (int k = p; k >= 1; k >>= 1)
+                for (int j = k % p; j + k < N; j += 2 * k)
+                    for (int i = 0; i < k && i < N - j - k; ++i)
+                        if ((i + j) / (2 * p) == (i + j + k) / (2 * p)) {
+                            a[n] = i + j;
+                            b[n] = i + j + k;
+                            ++n;
+                        }
+    }
+};
+template <int N>
+constexpr SortNet<N> kSortNet{};
+
+template <int A, int B, int N>
+__device__ __forceinline__ void compare_swap(float (&v)[N], uint32_t (&pl)[N]) {
+    const bool sw = v[B] < v[A];
+    const float lo = sw ? v[B] : v[A], hi = sw ? v[A] : v[B];
+    const uint32_t plo = sw ? pl[B] : pl[A], phi = sw ? pl[A] : pl[B];
+    v[A] = lo;
+    v[B] = hi;
+    pl[A] = plo;
+    pl[B] = phi;
+}
+
+template <int N, size_t... I>
+__device__ __forceinline__ void sort_network(float (&v)[N], uint32_t (&pl)[N], std::index_sequence<I...>) {
+    (compare_swap<kSortNet<N>.a[I], kSortNet<N>.b[I]>(v, pl), ...);
+}
+
+// Orders the 2M deltas of one (table, query) pair in registers for M <= MM:
+// the downs are sorted by a network (payload: column), each down's place in
+// the merged sequence is its rank plus the number of ups below it, and the
+// ups fill the remaining places in ascending order (ups fall as downs rise).
+// Writes enc[] (sorted delta -> column | up << 7) and returns whether all 2M
+// values are distinct and strictly ascending; otherwise the caller takes the
+// reference's heap procedure.
+template <int MM, class SV>
+__device__ __forceinline__ bool order_deltas_net(const float* dn, uint8_t* enc, int M, SV sv) {
+    float v[MM];
+    uint32_t col[MM];
+#pragma unroll
+    for (int k = 0; k < MM; ++k) {
+        v[k] = k < M ? dn[k * PF] : 2.0f;   // padding sorts last
+        col[k] = (uint32_t)k;
+    }
+    sort_network<MM>(v, col, std::make_index_sequence<kSortNet<MM>.n>{});
+    float u[MM];
+#pragma unroll
+    for (int k = 0; k < MM; ++k) u[k] = __fsub_rn(1.0f, v[k]);   // padding: -1, below every value
+    uint32_t taken = 0;
+#pragma unroll
+    for (int k = 0; k < MM; ++k) {
+        if (k < M) {
+            int below = 0;
+#pragma unroll
+            for (int k2 = 0; k2 < MM; ++k2) below += u[k2] < v[k];
+            const int pos = k + below - (MM - M);
+            taken |= 1u << pos;
+            enc[pos * PF] = (uint8_t)col[k];
+        }
+    }
+#pragma unroll
+    for (int k = MM - 1; k >= 0; --k) {
+        if (k < M) {
+            const int pos = __ffs((int)~taken) - 1;
+            taken |= 1u << pos;
+            enc[pos * PF] = (uint8_t)(col[k] | 0x80u);
+        }
+    }
+    bool ok = true;
+    float prev = sv(0);
+#pragma unroll
+    for (int o = 1; o < 2 * MM; ++o) {
+        if (o < 2 * M) {
+            const float x = sv(o);
+            ok &= prev < x;
+            prev = x;
+        }
+    }
+    return ok;
+}
+
 // Per-thread shared-memory slice of the fast kernel, in bytes per thread.
 template <typename MaskT>
 __host__ __device__ constexpr size_t probe_fast_bytes_per_thread(int M, int T) {
@@ -332,7 +423,9 @@ __host__ __device__ constexpr size_t probe_fast_bytes_per_thread(int M, int T) {
 }
 
 // PCH: probes whose group loads are in flight together (tuned: 1, 2 or 4).
-template <typename MaskT, int PCH>
+// MM > 0: M <= MM, deltas ordered in registers (order_deltas_net); MM = 0:
+// ranking and merge over the shared-memory slice.
+template <typename MaskT, int PCH, int MM>
 __global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
     extern __shared__ __align__(16) unsigned char psm[];
     const LookupView& lv = a.lv;
@@ -393,7 +486,19 @@ __global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
         c.h0 += (uint64_t)(h - lo) * __ldg(c.rmul + m);
     }
 
-    if (T > 1) {
+    if (T > 1 && MM > 0) {
+        if (distinct) distinct = order_deltas_net<(MM > 0 ? MM : 1)>(dn, enc, M, sv);
+        if (!distinct) {
+            int8_t* perm = reinterpret_cast<int8_t*>(enc);
+            heap_order_strided(dv, perm, M2, M2);
+            for (int i = 0; i < M2; ++i) {
+                const int pm = perm[i * PF];
+                enc[i * PF] = (uint8_t)((pm % M) | (pm >= M ? 0x80 : 0));
+            }
+        }
+        comb[0] = 1;
+        cd[0] = sv(0);
+    } else if (T > 1) {
         // Rank the downs (ties or NaN fall back to the heap procedure).
         for (int i = 0; i < M && distinct; ++i) {
             const float di = dn[i * PF];
@@ -529,29 +634,34 @@ __global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
     if (cnu) atomicAdd(a.cnu + q, cnu);
 }
 
-template <typename MaskT, int PCH>
+template <typename MaskT, int PCH, int MM>
 cudaError_t launch_probe_fast_v(const ProbeArgs& a, cudaStream_t st) {
     const size_t smem = (size_t)PF * probe_fast_bytes_per_thread<MaskT>(a.lv.M, a.T);
     static std::atomic<size_t> cap{0};   // dynamic shared memory this kernel is opted into
-    const cudaError_t e = opt_in_smem(k_probe_fast<MaskT, PCH>, smem, cap);
+    const cudaError_t e = opt_in_smem(k_probe_fast<MaskT, PCH, MM>, smem, cap);
     if (e != cudaSuccess) return e;
     const int64_t n = (int64_t)a.lv.L * a.Q;
-    k_probe_fast<MaskT, PCH><<<(unsigned)((n + PF - 1) / PF), PF, smem, st>>>(a);
+    k_probe_fast<MaskT, PCH, MM><<<(unsigned)((n + PF - 1) / PF), PF, smem, st>>>(a);
     return cudaGetLastError();
 }
 
-template <typename MaskT>
+template <typename MaskT, int MM>
 cudaError_t launch_probe_fast_t(const ProbeArgs& a, cudaStream_t st) {
     switch (a.pch) {
-        case 1: return launch_probe_fast_v<MaskT, 1>(a, st);
-        case 4: return launch_probe_fast_v<MaskT, 4>(a, st);
-        default: return launch_probe_fast_v<MaskT, 2>(a, st);
+        case 1: return launch_probe_fast_v<MaskT, 1, MM>(a, st);
+        case 4: return launch_probe_fast_v<MaskT, 4, MM>(a, st);
+        default: return launch_probe_fast_v<MaskT, 2, MM>(a, st);
     }
 }
 
-// 32-bit masks when the 2M sorted deltas fit (M <= 16).
+// 32-bit masks when the 2M sorted deltas fit (M <= 16), with the deltas
+// ordered in registers for M padded to 8, 12 or 16.
 cudaError_t launch_probe_fast(const ProbeArgs& a, cudaStream_t st) {
-    return a.lv.M <= 16 ? launch_probe_fast_t<uint32_t>(a, st) : launch_probe_fast_t<uint64_t>(a, st);
+    const int M = a.lv.M;
+    if (M <= 8) return launch_probe_fast_t<uint32_t, 8>(a, st);
+    if (M <= 12) return launch_probe_fast_t<uint32_t, 12>(a, st);
+    if (M <= 16) return launch_probe_fast_t<uint32_t, 16>(a, st);
+    return launch_probe_fast_t<uint64_t, 0>(a, st);
 }
 
 __global__ void __launch_bounds__(CT) k_candidates(CandArgs a) {

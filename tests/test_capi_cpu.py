@@ -215,3 +215,29 @@ def build_dropin(culsh, tmp_path):
 def test_dropin_header_compiles_and_links(culsh, tmp_path):
     exe = build_dropin(culsh, tmp_path)
     assert exe.exists()
+
+
+def test_cli_arguments_and_missing_file(culsh):
+    """The command-line program keeps the reference demo's contract
+    (cuLSH_main.cu:23-32): a usage message and status 0 without exactly nine
+    arguments, status 1 for a file that cannot be opened or read. None of
+    these paths touches the GPU."""
+    from culsh_gb300 import _build
+    cli = _build.build_cli()
+    r = subprocess.run([cli], capture_output=True, text=True)
+    assert r.returncode == 0 and "while 9 are required" in r.stdout
+    assert "[filename] [D] [N] [L] [M] [W] [Q] [K] [T]" in r.stdout
+    r = subprocess.run([cli, "/nonexistent/data.bin", "4", "10", "1", "2", "1.0", "2", "1", "1"],
+                       capture_output=True, text=True)
+    assert r.returncode == 1 and "Could not open file" in r.stdout
+
+
+def test_cli_short_file_and_bad_sizes(culsh, tmp_path):
+    from culsh_gb300 import _build
+    cli = _build.build_cli()
+    f = tmp_path / "short.bin"
+    np.zeros(10, np.float32).tofile(f)
+    r = subprocess.run([cli, str(f), "4", "10", "1", "2", "1.0", "2", "1", "1"], capture_output=True, text=True)
+    assert r.returncode == 1 and "Could not load data matrix" in r.stdout
+    r = subprocess.run([cli, str(f), "4", "2", "1", "2", "1.0", "3", "1", "1"], capture_output=True, text=True)
+    assert r.returncode == 1 and "Invalid sizes" in r.stdout

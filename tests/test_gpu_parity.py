@@ -252,6 +252,53 @@ def test_search_general_probe_kernel(culsh, name, monkeypatch):
     check_search(st, c)
 
 
+@pytest.mark.parametrize("M,T,ties", [(9, 16, False), (12, 16, False), (12, 16, True), (16, 24, False),
+                                       (16, 16, True), (5, 9, True)])
+def test_probe_order_register_network(culsh, M, T, ties):
+    """For M <= 16 the fast kernel orders the 2M deltas in registers (sorting
+    network + merge by counting) and takes the reference's heap procedure
+    whenever two deltas tie. Query buckets (the probe order of every table)
+    and kNN ids match the oracle. The tie cases mix queries with integer
+    projections and W = 4 or 8 (downs are multiples of 1/W, so M > W downs
+    must tie, and downs of 1/2 tie with ups) with noisy queries whose deltas
+    are all distinct."""
+    import oracle
+    rng = np.random.default_rng(100 * M + T)
+    N, D, L = 3000, 16, 3
+    if ties:
+        X = rng.integers(-1, 2, (N, D)).astype(np.float32)
+        A = rng.integers(-1, 2, (L, M, D)).astype(np.float32)
+        b = np.zeros((L, M), np.float32)
+        W = 8.0 if M % 2 == 0 else 4.0   # more downs than values k/W: ties in every exact query
+        Qm = np.concatenate([X[rng.integers(0, N, 60)],
+                             X[rng.integers(0, N, 60)] + rng.normal(0, 0.4, (60, D)).astype(np.float32)])
+    else:
+        centers = rng.normal(0, 3, (12, D)).astype(np.float32)
+        X = centers[rng.integers(0, 12, N)] + rng.normal(0, 0.3, (N, D)).astype(np.float32)
+        A = rng.normal(0, 1, (L, M, D)).astype(np.float32)
+        W = 4.0
+        b = rng.uniform(0, W, (L, M)).astype(np.float32)
+        Qm = centers[rng.integers(0, 12, 120)] + rng.normal(0, 0.3, (120, D)).astype(np.float32)
+    Qm = np.ascontiguousarray(Qm, np.float32)
+    K = 10
+    ht = culsh.HashTables()
+    ht.reset(N, D, L, M, W, A=A, b=b)
+    ht.index(X)
+    st = culsh.SearchTables()
+    st.reset(ht, K, T)
+    st.search(Qm, dataset=X)
+    ref = oracle.search(oracle.build_index(X, A, b, W), X, Qm, K, T)
+    Q = Qm.shape[0]
+    hits = 0
+    for l in range(L):
+        qb = st.getQueryBuckets(l)
+        np.testing.assert_array_equal(qb, ref["qbuckets"][l].reshape(Q, T), err_msg=f"table {l}")
+        hits += int((qb[:, 1:] >= 0).sum())
+    assert hits > Q   # the comparison covers many non-home probes that found a bucket
+    np.testing.assert_array_equal(st.getKnnIds(), ref["knn_ids"])
+    np.testing.assert_array_equal(st.getKnnDistances(), ref["knn_dists"])
+
+
 @pytest.mark.parametrize("name", golden_cases())
 def test_index_simt_projection(culsh, name, monkeypatch):
     """The SIMT projection kernel (the form every shape supports) builds the
@@ -379,3 +426,38 @@ def test_streaming_tensor_core_projection(culsh, N, D, L, M, W, integer, monkeyp
     for l in range(L):
         np.testing.assert_array_equal(ht.getBuckets_codes(l), ref.codes(l), err_msg=f"table {l}")
         np.testing.assert_array_equal(ht.getBuckets_totalIndices(l), ref.ids(l), err_msg=f"table {l}")
+
+
+def test_cli_index_and_search(culsh, tmp_path):
+    """The command-line program (the reference demo's nine arguments) builds
+    an index with random projections and searches the first Q points. The
+    index it saves matches, byte for byte, the oracle's index built with the
+    A and b stored in that file, and its printed selectivity is the oracle's."""
+    import re
+    import oracle
+    from culsh_gb300 import _build
+    cli = _build.build_cli()
+    rng = np.random.default_rng(77)
+    N, D, L, M, W, Q, K, T = 5000, 24, 5, 6, 5.0, 300, 10, 8
+    centers = rng.normal(0, 6, (50, D))
+    X = (centers[rng.integers(0, 50, N)] + rng.normal(0, 1, (N, D))).astype(np.float32)
+    data = tmp_path / "data.bin"
+    X.tofile(data)
+    saved = tmp_path / "cli.index"
+    env = dict(os.environ, CULSH_SAVE_INDEX=str(saved))
+    r = subprocess.run([cli, str(data), str(D), str(N), str(L), str(M), str(W), str(Q), str(K), str(T)],
+                       capture_output=True, text=True, env=env)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "seconds to index" in r.stdout and "seconds to search" in r.stdout
+    ht = culsh.HashTables()
+    ht.reset(str(saved))
+    A = np.stack([ht.getA(l) for l in range(L)])
+    b = np.stack([ht.getb(l) for l in range(L)])
+    ref = oracle.build_index(X, A, b, W)
+    ref_file = tmp_path / "oracle.index"
+    ref.save(str(ref_file))
+    assert saved.read_bytes() == ref_file.read_bytes()
+    want = oracle.search(ref, X, X[:Q], K, T)
+    sel = float(re.search(r"Selectivity = ([0-9.]+)%", r.stdout).group(1))
+    assert sel == pytest.approx(float(want["unique"].sum()) / N / Q, abs=6e-4)
+    assert want["unique"].sum() > 0
