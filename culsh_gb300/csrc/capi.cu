@@ -155,6 +155,10 @@ struct culsh_index {
     DevBuf<uint64_t> boff, hoff;
     DevBuf<uint32_t> hmask;
     DevBuf<unsigned long long> hslots;
+    std::vector<uint64_t> h_fl_off;   // key filters (see filter_mix)
+    std::vector<uint32_t> h_fl_mask;
+    DevBuf<uint64_t> fl_off;
+    DevBuf<uint32_t> fl_mask, filt;
     DevBuf<float> dcodes;
     DevBuf<int> err;
 
@@ -194,6 +198,7 @@ struct SearchTune {
     int ws_chunk = 1024;   // non-unique candidates per id partition
     int dist_bf16 = 0;     // 1: BF16 candidate distances + certified FP32 rerank (work-stealing form)
     int ws_slots = 4096;   // shared hash-set slots per work item (4096 or 8192)
+    int probe_split = 0;   // 1: enumeration kernel, then one lookup thread per probe (M <= 16)
 };
 constexpr size_t kPlanBytes = 1024;   // room for the graph key (checked below)
 
@@ -209,6 +214,9 @@ struct culsh_search {
     bool host_copy_timed = false;
     DevBuf<float> dq, vals, od;
     DevBuf<int32_t> qb, oids;
+    DevBuf<unsigned long long> ph;   // split probe lookups: hash, mask, pair context
+    DevBuf<uint32_t> pmask;
+    DevBuf<uint4> pctx;
     DevBuf<unsigned long long> cnu, cu, stats;
     DevBuf<int> deferred;
     DevBuf<uint32_t> arena;
@@ -379,8 +387,24 @@ int build_hash(culsh_index* ix, cudaStream_t st) {
     CU_TRY(cudaMemcpyAsync(ix->hoff.p, ix->h_hoff.data(), 8 * (L + 1), cudaMemcpyHostToDevice, st));
     CU_TRY(cudaMemcpyAsync(ix->hmask.p, ix->h_hmask.data(), 4 * L, cudaMemcpyHostToDevice, st));
     CU_TRY(cudaMemsetAsync(ix->hslots.p, 0xFF, 8 * ix->h_hoff[L], st));
+    // Filter words per table: a power of two holding 8 to 16 bits per key.
+    ix->h_fl_off.assign(L + 1, 0);
+    std::vector<uint32_t>& flm = ix->h_fl_mask;
+    flm.assign(L, 0);
+    for (int l = 0; l < L; ++l) {
+        const uint64_t B = ix->h_boff[l + 1] - ix->h_boff[l];
+        const uint64_t words = next_pow2(std::max<uint64_t>((B * kFilterBitsPerKey + 31) / 32, 1));
+        flm[l] = (uint32_t)(words - 1);
+        ix->h_fl_off[l + 1] = ix->h_fl_off[l] + words;
+    }
+    CU_TRY(ix->fl_off.reserve(L + 1));
+    CU_TRY(ix->fl_mask.reserve(L));
+    CU_TRY(ix->filt.reserve(ix->h_fl_off[L]));
+    CU_TRY(cudaMemcpyAsync(ix->fl_off.p, ix->h_fl_off.data(), 8 * (L + 1), cudaMemcpyHostToDevice, st));
+    CU_TRY(cudaMemcpyAsync(ix->fl_mask.p, flm.data(), 4 * L, cudaMemcpyHostToDevice, st));
+    CU_TRY(cudaMemsetAsync(ix->filt.p, 0, 4 * ix->h_fl_off[L], st));
     CU_TRY(launch_hash_build(ix->boff.p, ix->ukeys.p, L, ix->M, ix->KW, maxB, ix->foff.p, ix->fbits.p, ix->rmul.p,
-                             ix->hoff.p, ix->hmask.p, ix->hslots.p,
+                             ix->hoff.p, ix->hmask.p, ix->hslots.p, ix->filt.p, ix->fl_off.p, ix->fl_mask.p,
                              ix->err.p, st));
     return CULSH_OK;
 }
@@ -734,6 +758,9 @@ LookupView lookup_view(const culsh_index* ix) {
     lv.hslots = ix->hslots.p;
     lv.hoff = ix->hoff.p;
     lv.hmask = ix->hmask.p;
+    lv.filt = ix->filt.p;
+    lv.fl_off = ix->fl_off.p;
+    lv.fl_mask = ix->fl_mask.p;
     lv.funit = ix->funit.p;
     lv.rmul = ix->rmul.p;
     return lv;
@@ -792,7 +819,7 @@ struct SearchPlan {
     ProbeArgs pa;
     int probe_generic;
     int use_ws, ws_grid, use_dense, dense_grid;
-    CandArgs ca;
+    CandArgs ca{};
     WsArgs wa;
     unsigned long long* stats;
     unsigned long long* h_stats;
@@ -847,6 +874,20 @@ int plan_search(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* 
     P.pa.small_codes = small_codes(ix);
     P.pa.pch = tu.probe_pch;
     P.probe_generic = getenv("CULSH_PROBE_GENERIC") != nullptr;
+    {
+        // CULSH_PROBE_SPLIT=0/1 overrides the tuning (the tests run both).
+        const char* e = getenv("CULSH_PROBE_SPLIT");
+        const bool split = (e ? atoi(e) != 0 : tu.probe_split != 0) && M <= 16;
+        if (split) {
+            CU_TRY(s->ph.reserve((size_t)L * Q * T));
+            CU_TRY(s->pmask.reserve((size_t)L * Q * T));
+            CU_TRY(s->pctx.reserve(3 * (size_t)L * Q));
+            P.pa.split = 1;
+            P.pa.ph = s->ph.p;
+            P.pa.pmask = s->pmask.p;
+            P.pa.pctx = s->pctx.p;
+        }
+    }
     CandArgs& ca = P.ca;
     ca.X = dX;
     ca.N = ix->N;
@@ -1023,7 +1064,7 @@ int enqueue_search(const SearchPlan& P, cudaStream_t st, bool capturing, int* la
     }
     CU_TRY(cudaEventRecordWithFlags(P.ev[3], st, evf));
     CU_TRY(cudaMemcpyAsync(P.h_stats, P.stats, 8 * 8, cudaMemcpyDeviceToHost, st));
-    *launches = P.use_ws ? (P.use_dense ? 5 : 4) : 3;
+    *launches = (P.use_ws ? (P.use_dense ? 4 : 3) : 2) + probe_launches(P.pa);
     return CULSH_OK;
 }
 
@@ -1577,6 +1618,9 @@ long long culsh_search_device_bytes(culsh_search* s) {
     add(s->vals);
     add(s->od);
     add(s->qb);
+    add(s->ph);
+    add(s->pmask);
+    add(s->pctx);
     add(s->oids);
     add(s->cnu);
     add(s->cu);
@@ -1603,6 +1647,7 @@ long long culsh_search_estimate_bytes(const culsh_index* ix, int Q, int K, int T
     size_t cap = std::max<size_t>(2 * q, kWsPartialBytes / per_item);
     cap = std::min(cap, q * kWsPartitions);
     b += 16 * q + cap * per_item;   // per-query plan arrays, dense-query list, partial lists
+    if (M <= 16) b += 12 * L * q * (size_t)T + 48 * L * q;   // split probe lookups
     return (long long)b;
 }
 
@@ -1617,6 +1662,9 @@ int culsh_search_release(culsh_search* s) {
     s->vals.release();
     s->od.release();
     s->qb.release();
+    s->ph.release();
+    s->pmask.release();
+    s->pctx.release();
     s->oids.release();
     s->cnu.release();
     s->cu.release();
@@ -1647,6 +1695,7 @@ static void tune_to_c(const SearchTune& t, culsh_tuning* o) {
     o->ws_chunk = t.ws_chunk;
     o->distance_bf16 = t.dist_bf16;
     o->ws_set_slots = t.ws_slots;
+    o->probe_split = t.probe_split;
 }
 
 int culsh_search_get_tuning(culsh_search* s, culsh_tuning* out) {
@@ -1664,7 +1713,8 @@ int culsh_search_set_tuning(culsh_search* s, const culsh_tuning* in) {
                     (in->ws_threads == 64 || in->ws_threads == 128 || in->ws_threads == 256) &&
                     in->ws_blocks_per_sm >= 0 && in->ws_blocks_per_sm <= 64 && in->ws_chunk >= 64 &&
                     in->ws_chunk <= 65536 && (in->distance_bf16 == 0 || in->distance_bf16 == 1) &&
-                    (in->ws_set_slots == 4096 || in->ws_set_slots == 8192);
+                    (in->ws_set_slots == 4096 || in->ws_set_slots == 8192) &&
+                    (in->probe_split == 0 || in->probe_split == 1);
     if (!ok) return fail(CULSH_ERR_INVALID_ARGUMENT, "tuning value out of range");
     s->tune.proj_tile = in->proj_tile;
     s->tune.probe_pch = in->probe_batch;
@@ -1674,6 +1724,7 @@ int culsh_search_set_tuning(culsh_search* s, const culsh_tuning* in) {
     s->tune.ws_chunk = in->ws_chunk;
     s->tune.dist_bf16 = in->distance_bf16;
     s->tune.ws_slots = in->ws_set_slots;
+    s->tune.probe_split = in->probe_split;
     return CULSH_OK;
 }
 
@@ -1748,11 +1799,13 @@ int culsh_search_autotune(culsh_search* s, const float* d_queries, int Q, int* d
             best.proj_tile = tile;
         }
     }
-    // probe batch depth
-    const int pchs[3] = {1, 2, 4};
-    for (int i = 0; i < 3; ++i) {
+    // probe form: fused with batch depth 1, 2 or 4, or split lookups (M <= 16)
+    const int pchs[4] = {1, 2, 4, 0};
+    const int nforms = s->ix->M <= 16 ? 4 : 3;
+    for (int i = 0; i < nforms; ++i) {
         s->tune = best;
-        s->tune.probe_pch = pchs[i];
+        s->tune.probe_split = pchs[i] == 0;
+        if (pchs[i]) s->tune.probe_pch = pchs[i];
         const int rc = measure(stage);
         if (rc != CULSH_OK) {
             s->tune = start;
@@ -1760,7 +1813,8 @@ int culsh_search_autotune(culsh_search* s, const float* d_queries, int Q, int* d
         }
         if (i == 0 || stage[1] < best_t) {
             best_t = stage[1];
-            best.probe_pch = pchs[i];
+            best.probe_split = pchs[i] == 0;
+            if (pchs[i]) best.probe_pch = pchs[i];
         }
     }
     // candidate stage
@@ -1976,7 +2030,7 @@ extern "C" int culsh_search_run_device_noalloc(culsh_search* s, const float* d_q
     CU_TRY(cudaMemsetAsync(stats, 0, 8 * 4, st));
     CU_TRY(launch_project_fp32(d_queries, Q, D, ix->dAT.p, ix->lmp, ix->db.p, L * M, ix->W, nullptr, vals, nullptr,
                                nullptr, nullptr, st));
-    ProbeArgs pa;
+    ProbeArgs pa{};
     pa.vals = vals;
     pa.Q = Q;
     pa.T = T;
@@ -1986,7 +2040,7 @@ extern "C" int culsh_search_run_device_noalloc(culsh_search* s, const float* d_q
     pa.small_codes = small_codes(ix);
     pa.pch = 2;
     CU_TRY(launch_probe(pa, st));
-    CandArgs ca;
+    CandArgs ca{};
     ca.X = ix->dev_x();
     ca.N = ix->N;
     ca.D = D;

@@ -77,6 +77,19 @@ __host__ __device__ __forceinline__ uint64_t field_mult(int c) {
 }
 __host__ __device__ __forceinline__ uint64_t hash_finish(uint64_t h) { return mix64(h ^ kHashSeed); }
 
+// Key filter beside each table's hash (a blocked Bloom filter, two bits in
+// one 32-bit word, 8 to 16 bits per key): the word index and the two bits
+// come from the high half of a 64-bit product of the finished hash, so they
+// are independent of the group (low bits) and the fingerprint (top 16 bits).
+// A key that is in the table always finds both of its bits set.
+__host__ __device__ __forceinline__ uint32_t filter_mix(uint64_t hh) {
+    return (uint32_t)((hh * 0xD6E8FEB86659FD93ull) >> 32);
+}
+__host__ __device__ __forceinline__ uint32_t filter_bits(uint32_t fx) {
+    return (1u << (fx >> 27)) | (1u << ((fx >> 22) & 31u));
+}
+constexpr int kFilterBitsPerKey = 8;
+
 // Place a field of `bits` bits (<= 32) at bit offset `off` of a little-endian
 // multi-word key.
 __host__ __device__ __forceinline__ void key_put(uint32_t* key, int off, int bits, uint32_t val) {
@@ -109,6 +122,9 @@ struct LookupView {
     const uint32_t* hmask;
     const unsigned long long* funit;   // [L*M][2]: 2^foff as (low, high) 64-bit words
     const unsigned long long* rmul;    // [L*M]: field multipliers of the lookup hash
+    const uint32_t* filt;              // key filters, table l at words [fl_off[l], fl_off[l+1])
+    const uint64_t* fl_off;
+    const uint32_t* fl_mask;           // [L]: words in table l's filter - 1 (a power of two - 1)
 };
 
 // ---------------------------------------------------------------------------
@@ -194,7 +210,8 @@ cudaError_t launch_bucket_sizes(const uint64_t* boff, const uint32_t* starts, in
                                 uint32_t* sizes, uint32_t* max_size, cudaStream_t st);
 cudaError_t launch_hash_build(const uint64_t* boff, const uint32_t* ukeys, int L, int M, int KW, int64_t maxB,
                               const uint16_t* foff, const uint8_t* fbits, const unsigned long long* rmul,
-                              const uint64_t* hoff, const uint32_t* hmask, unsigned long long* hslots, int* err,
+                              const uint64_t* hoff, const uint32_t* hmask, unsigned long long* hslots,
+                              uint32_t* filt, const uint64_t* fl_off, const uint32_t* fl_mask, int* err,
                               cudaStream_t st);
 // Bucket codes [M][B_l] per table (float, the reference's layout) decoded from ukeys.
 cudaError_t launch_decode_codes(const uint64_t* boff, const uint32_t* ukeys, int L, int M, int KW, int64_t maxB,
@@ -220,8 +237,16 @@ struct ProbeArgs {
     unsigned long long* cnu;   // [Q] non-unique candidate counts (accumulated)
     int small_codes;           // every |cmin|, |cmax| < 2^24 - 2 (set by the host)
     int pch;                   // fast kernel: probes whose group loads overlap (1, 2, 4)
+    // Split lookups (M <= 16, fast kernel): the enumeration kernel stores each
+    // valid probe's finished hash and mask and marks its query bucket -2;
+    // one thread per probe then checks the key filter and walks the hash.
+    int split;
+    unsigned long long* ph;    // [L][T][Q] finished hash of each pending probe
+    uint32_t* pmask;           // [L][T][Q] its mask over the sorted deltas
+    uint4* pctx;               // [L*Q][3] home key (128 bits), sorted deltas (32 bytes)
 };
 cudaError_t launch_probe(const ProbeArgs& a, cudaStream_t st);
+int probe_launches(const ProbeArgs& a);   // kernels launch_probe launches
 
 struct CandArgs {
     const float* X;

@@ -425,7 +425,7 @@ __host__ __device__ constexpr size_t probe_fast_bytes_per_thread(int M, int T) {
 // PCH: probes whose group loads are in flight together (tuned: 1, 2 or 4).
 // MM > 0: M <= MM, deltas ordered in registers (order_deltas_net); MM = 0:
 // ranking and merge over the shared-memory slice.
-template <typename MaskT, int PCH, int MM>
+template <typename MaskT, int PCH, int MM, bool kSplit>
 __global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
     extern __shared__ __align__(16) unsigned char psm[];
     const LookupView& lv = a.lv;
@@ -543,16 +543,85 @@ __global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
         cd[0] = sv(0);
     }
 
-    // Probes: enumerate (cuLSH_Kernels.cu:216-255) PCH at a time, issue the
-    // group loads of the batch together, then resolve each probe: walk its
-    // group's fingerprints (registers) until an empty slot, verifying the
-    // stored key on a fingerprint match.
+    int32_t* qb = a.qbuckets + (int64_t)l * Q * T + (int64_t)q * T;
+    int size = 1;
+    // One enumeration step (cuLSH_Kernels.cu:216-255): probe t > 0 is the
+    // candidate of smallest delta sum (the first of equal sums), which is
+    // then shifted in place and expanded into a new candidate.
+    auto next_probe = [&]() -> MaskT {
+        float mn = FLT_MAX;
+        int mi = 0;
+        for (int i = 0; i < size; ++i) {
+            const float x = cd[i * PF];
+            if (x < mn) {
+                mi = i;
+                mn = x;
+            }
+        }
+        const MaskT probe = comb[mi * PF];
+        const int top = highest_bit(probe);
+        if (top < M2 - 1) {
+            const MaskT p1 = probe | ((MaskT)1 << (top + 1));
+            const float m1 = __fadd_rn(mn, sv(top + 1));
+            comb[mi * PF] = p1;
+            cd[mi * PF] = m1;
+            comb[size * PF] = p1 - ((MaskT)1 << top);
+            cd[size * PF] = __fsub_rn(m1, sv(top));
+            ++size;
+        }
+        return probe;
+    };
+    if constexpr (kSplit) {
+        // Pair context for the lookup kernel: home key and sorted deltas.
+        uint32_t ew[8];
+#pragma unroll
+        for (int w = 0; w < 8; ++w) ew[w] = 0;
+        if (T > 1) {
+#pragma unroll
+            for (int i = 0; i < 32; ++i)
+                if (i < M2) ew[i >> 2] |= (uint32_t)enc[i * PF] << (8 * (i & 3));
+        }
+        uint4* cx = a.pctx + idx * 3;
+        cx[0] = make_uint4((uint32_t)c.hkey, (uint32_t)(c.hkey >> 32), (uint32_t)(c.hkey >> 64),
+                           (uint32_t)(c.hkey >> 96));
+        cx[1] = make_uint4(ew[0], ew[1], ew[2], ew[3]);
+        cx[2] = make_uint4(ew[4], ew[5], ew[6], ew[7]);
+        // Hash and mask of probe t at [l][t][q] (a warp's stores coalesce);
+        // the query buckets are staged four at a time for 16-byte stores.
+        const int64_t base = (int64_t)l * T * Q + q;
+        const bool vec = (T & 3) == 0;
+        int s0 = -1, s1 = -1, s2 = -1, s3 = -1;
+        for (int t = 0; t < T; ++t) {
+            const MaskT probe = t > 0 ? next_probe() : (MaskT)0;
+            uint64_t hh;
+            const bool ok = probe_hash(c, probe, hh);
+            if (ok) {
+                a.ph[base + (int64_t)t * Q] = hh;
+                a.pmask[base + (int64_t)t * Q] = (uint32_t)probe;
+            }
+            const int v = ok ? -2 : -1;
+            if (vec) {
+                const int r = t & 3;
+                s0 = r == 0 ? v : s0;
+                s1 = r == 1 ? v : s1;
+                s2 = r == 2 ? v : s2;
+                s3 = r == 3 ? v : s3;
+                if (r == 3) *reinterpret_cast<int4*>(qb + t - 3) = make_int4(s0, s1, s2, s3);
+            } else {
+                qb[t] = v;
+            }
+        }
+        return;
+    }
+
+    // Probes: enumerate PCH at a time, issue the group loads of the batch
+    // together, then resolve each probe: walk its group's fingerprints
+    // (registers) until an empty slot, verifying the stored key on a
+    // fingerprint match.
     const uint32_t gmask = __ldg(lv.hmask + l);
     const unsigned long long* slots = lv.hslots + __ldg(lv.hoff + l);
     const uint64_t bo = __ldg(lv.boff + l);
-    int32_t* qb = a.qbuckets + (int64_t)l * Q * T + (int64_t)q * T;
     unsigned long long cnu = 0;
-    int size = 1;
     for (int t0 = 0; t0 < T; t0 += PCH) {
         MaskT pm[PCH];
         unsigned long long fw[PCH];   // fingerprint word of each probe's group
@@ -564,29 +633,7 @@ __global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
             fw[j] = ~0ull;
             hsv[j] = fpv[j] = 0;
             if (t < T) {
-                MaskT probe = 0;
-                if (t > 0) {
-                    float mn = FLT_MAX;
-                    int mi = 0;
-                    for (int i = 0; i < size; ++i) {
-                        const float x = cd[i * PF];
-                        if (x < mn) {
-                            mi = i;
-                            mn = x;
-                        }
-                    }
-                    probe = comb[mi * PF];
-                    const int top = highest_bit(probe);
-                    if (top < M2 - 1) {
-                        const MaskT p1 = probe | ((MaskT)1 << (top + 1));
-                        const float m1 = __fadd_rn(mn, sv(top + 1));
-                        comb[mi * PF] = p1;
-                        cd[mi * PF] = m1;
-                        comb[size * PF] = p1 - ((MaskT)1 << top);
-                        cd[size * PF] = __fsub_rn(m1, sv(top));
-                        ++size;
-                    }
-                }
+                const MaskT probe = t > 0 ? next_probe() : (MaskT)0;
                 pm[j] = probe;
                 uint64_t hh;
                 if (probe_hash(c, probe, hh)) {
@@ -634,34 +681,152 @@ __global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
     if (cnu) atomicAdd(a.cnu + q, cnu);
 }
 
-template <typename MaskT, int PCH, int MM>
+// Lookups of the split form. A thread takes four probe slots t = 4g .. 4g+3
+// of one (table, query) pair, queries fastest across threads, so that the
+// hash and mask reads coalesce and four filter loads are in flight at once.
+// Slots the enumeration marked -2 hold a valid probe: the key filter rules
+// most absent keys out with one 4-byte load; otherwise the group walk of
+// k_probe_fast runs, and a fingerprint match is verified against the key
+// rebuilt from the pair's home key and sorted deltas (as probe_key does).
+constexpr int kResolveSlots = 4;
+
+__device__ __forceinline__ int32_t resolve_slot(const ProbeArgs& a, int l, int q, uint64_t hh, uint32_t pmask) {
+    const LookupView& lv = a.lv;
+    const int M = lv.M, KW = lv.KW;
+    const uint32_t gmask = __ldg(lv.hmask + l);
+    const unsigned long long* slots = lv.hslots + __ldg(lv.hoff + l);
+    const uint64_t bo = __ldg(lv.boff + l);
+    const uint32_t fp = slot_fp(hh);
+    uint32_t h = (uint32_t)hh & gmask;
+    bool have_key = false;
+    u128 key = 0;
+    for (uint32_t p = 0; p <= gmask; ++p) {
+        const unsigned long long* grp = slots + (uint64_t)h * kGroupWords;
+        const unsigned long long w = __ldg(grp);
+        for (int e = 0; e < kGroupSlots; ++e) {
+            const uint32_t f = (uint32_t)(w >> (16 * e)) & 0xFFFFu;
+            if (f == kEmptyFp) return -1;
+            if (f != fp) continue;
+            if (!have_key) {
+                const uint4* cx = a.pctx + ((int64_t)l * a.Q + q) * 3;
+                const uint4 k0 = cx[0], e0 = cx[1], e1 = cx[2];
+                uint32_t up = 0, dn = 0;
+                for (uint32_t b = pmask; b; b &= b - 1) {
+                    const int bit = lowest_bit(b);
+                    const int wi = bit >> 2;
+                    const uint32_t word = wi == 0 ? e0.x : wi == 1 ? e0.y : wi == 2 ? e0.z : wi == 3 ? e0.w
+                                        : wi == 4 ? e1.x : wi == 5 ? e1.y : wi == 6 ? e1.z : e1.w;
+                    const uint32_t en = (word >> (8 * (bit & 3))) & 0xFFu;
+                    if (en & 0x80u) up |= 1u << (en & 0x3fu);
+                    else dn |= 1u << (en & 0x3fu);
+                }
+                key = ((u128)k0.w << 96) | ((u128)k0.z << 64) | ((u128)k0.y << 32) | (u128)k0.x;
+                const unsigned long long* funit = lv.funit + 2 * (int64_t)l * M;
+                for (uint32_t b = up & ~dn; b; b &= b - 1) key += unit_of(funit, lowest_bit(b));
+                for (uint32_t b = dn & ~up; b; b &= b - 1) key -= unit_of(funit, lowest_bit(b));
+                have_key = true;
+            }
+            const uint32_t bj = __ldg(reinterpret_cast<const uint32_t*>(grp + 1) + e);
+            if (key_matches(lv.ukeys + (bo + bj) * KW, key, KW)) return (int32_t)bj;
+        }
+        h = (h + 1) & gmask;
+    }
+    return -1;
+}
+
+__global__ void __launch_bounds__(256, 4) k_probe_resolve(ProbeArgs a) {
+    const LookupView& lv = a.lv;
+    const int Q = a.Q, T = a.T;
+    const int G = (T + kResolveSlots - 1) / kResolveSlots;
+    const int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x;
+    if (i >= (int64_t)lv.L * G * Q) return;
+    const int q = (int)(i % Q);
+    const int64_t lg = i / Q;
+    const int l = (int)(lg / G), t0 = (int)(lg - (int64_t)l * G) * kResolveSlots;
+    int32_t* qb = a.qbuckets + ((int64_t)l * Q + q) * T + t0;
+    const bool vec = (T & 3) == 0;
+    int v[kResolveSlots];
+    if (vec) {
+        const int4 x = *reinterpret_cast<const int4*>(qb);
+        v[0] = x.x;
+        v[1] = x.y;
+        v[2] = x.z;
+        v[3] = x.w;
+    } else {
+#pragma unroll
+        for (int k = 0; k < kResolveSlots; ++k) v[k] = t0 + k < T ? qb[k] : -1;
+    }
+    if (v[0] != -2 && v[1] != -2 && v[2] != -2 && v[3] != -2) return;
+    const int64_t base = (int64_t)l * T * Q + (int64_t)t0 * Q + q;
+    uint64_t hh[kResolveSlots];
+    uint32_t fw[kResolveSlots], need[kResolveSlots];
+#pragma unroll
+    for (int k = 0; k < kResolveSlots; ++k) hh[k] = v[k] == -2 ? a.ph[base + (int64_t)k * Q] : 0;
+    const uint32_t* filt = lv.filt ? lv.filt + __ldg(lv.fl_off + l) : nullptr;
+    const uint32_t fmask = lv.filt ? __ldg(lv.fl_mask + l) : 0;
+#pragma unroll
+    for (int k = 0; k < kResolveSlots; ++k) {
+        const uint32_t fx = filter_mix(hh[k]);
+        need[k] = filter_bits(fx);
+        fw[k] = (v[k] == -2 && filt) ? __ldg(filt + (fx & fmask)) : ~0u;
+    }
+    unsigned long long added = 0;
+#pragma unroll
+    for (int k = 0; k < kResolveSlots; ++k) {
+        if (v[k] != -2) continue;
+        int32_t res = -1;
+        if ((fw[k] & need[k]) == need[k]) res = resolve_slot(a, l, q, hh[k], a.pmask[base + (int64_t)k * Q]);
+        v[k] = res;
+        if (res >= 0) added += __ldg(lv.sizes + __ldg(lv.boff + l) + res);
+    }
+    if (vec) {
+        *reinterpret_cast<int4*>(qb) = make_int4(v[0], v[1], v[2], v[3]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < kResolveSlots; ++k)
+            if (t0 + k < T) qb[k] = v[k];
+    }
+    if (added) atomicAdd(a.cnu + q, added);
+}
+
+template <typename MaskT, int PCH, int MM, bool kSplit>
 cudaError_t launch_probe_fast_v(const ProbeArgs& a, cudaStream_t st) {
     const size_t smem = (size_t)PF * probe_fast_bytes_per_thread<MaskT>(a.lv.M, a.T);
     static std::atomic<size_t> cap{0};   // dynamic shared memory this kernel is opted into
-    const cudaError_t e = opt_in_smem(k_probe_fast<MaskT, PCH, MM>, smem, cap);
+    const cudaError_t e = opt_in_smem(k_probe_fast<MaskT, PCH, MM, kSplit>, smem, cap);
     if (e != cudaSuccess) return e;
     const int64_t n = (int64_t)a.lv.L * a.Q;
-    k_probe_fast<MaskT, PCH, MM><<<(unsigned)((n + PF - 1) / PF), PF, smem, st>>>(a);
+    k_probe_fast<MaskT, PCH, MM, kSplit><<<(unsigned)((n + PF - 1) / PF), PF, smem, st>>>(a);
+    if (kSplit) {
+        const int64_t threads = n * ((a.T + kResolveSlots - 1) / kResolveSlots);
+        k_probe_resolve<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(a);
+    }
     return cudaGetLastError();
 }
 
 template <typename MaskT, int MM>
 cudaError_t launch_probe_fast_t(const ProbeArgs& a, cudaStream_t st) {
+    if constexpr (sizeof(MaskT) == 4) {
+        if (a.split) return launch_probe_fast_v<MaskT, 1, MM, true>(a, st);
+    }
     switch (a.pch) {
-        case 1: return launch_probe_fast_v<MaskT, 1, MM>(a, st);
-        case 4: return launch_probe_fast_v<MaskT, 4, MM>(a, st);
-        default: return launch_probe_fast_v<MaskT, 2, MM>(a, st);
+        case 1: return launch_probe_fast_v<MaskT, 1, MM, false>(a, st);
+        case 4: return launch_probe_fast_v<MaskT, 4, MM, false>(a, st);
+        default: return launch_probe_fast_v<MaskT, 2, MM, false>(a, st);
     }
 }
 
 // 32-bit masks when the 2M sorted deltas fit (M <= 16), with the deltas
-// ordered in registers for M padded to 8, 12 or 16.
+// ordered in registers for M padded to 8, 12 or 16; the split form exists
+// for these. 64-bit masks (M <= 32) use the shared-memory ordering.
 cudaError_t launch_probe_fast(const ProbeArgs& a, cudaStream_t st) {
     const int M = a.lv.M;
     if (M <= 8) return launch_probe_fast_t<uint32_t, 8>(a, st);
     if (M <= 12) return launch_probe_fast_t<uint32_t, 12>(a, st);
     if (M <= 16) return launch_probe_fast_t<uint32_t, 16>(a, st);
-    return launch_probe_fast_t<uint64_t, 0>(a, st);
+    ProbeArgs b = a;
+    b.split = 0;
+    return launch_probe_fast_t<uint64_t, 0>(b, st);
 }
 
 __global__ void __launch_bounds__(CT) k_candidates(CandArgs a) {
@@ -818,18 +983,26 @@ __global__ void __launch_bounds__(CT) k_candidates(CandArgs a) {
 
 }  // namespace
 
+// Whether the fast kernel serves these arguments. It keeps per-thread state
+// in shared memory: used while a block's slice stays within 100 KB (two
+// blocks per SM), i.e. T <= 64 for M <= 16. CULSH_PROBE_GENERIC forces the
+// general kernel (the tests run both).
+static bool probe_fast_eligible(const ProbeArgs& a) {
+    const bool generic_only = getenv("CULSH_PROBE_GENERIC") != nullptr;
+    const size_t fast_bytes = (size_t)PF * (a.lv.M <= 16 ? probe_fast_bytes_per_thread<uint32_t>(a.lv.M, a.T)
+                                                         : probe_fast_bytes_per_thread<uint64_t>(a.lv.M, a.T));
+    return !generic_only && a.small_codes && a.lv.KW <= 4 && a.T <= 64 && a.lv.M <= 32 && fast_bytes <= 100 * 1024;
+}
+
+int probe_launches(const ProbeArgs& a) {
+    if ((int64_t)a.lv.L * a.Q <= 0) return 0;
+    return probe_fast_eligible(a) && a.split && a.lv.M <= 16 ? 2 : 1;
+}
+
 cudaError_t launch_probe(const ProbeArgs& a, cudaStream_t st) {
     const int64_t n = (int64_t)a.lv.L * a.Q;
     if (n <= 0) return cudaSuccess;
-    // CULSH_PROBE_GENERIC forces the general kernel (the tests run both).
-    const bool generic_only = getenv("CULSH_PROBE_GENERIC") != nullptr;
-    // The fast kernel keeps per-thread state in shared memory: used while a
-    // block's slice stays within 100 KB (two blocks per SM), i.e. T <= 64
-    // for M <= 16.
-    const size_t fast_bytes = (size_t)PF * (a.lv.M <= 16 ? probe_fast_bytes_per_thread<uint32_t>(a.lv.M, a.T)
-                                                         : probe_fast_bytes_per_thread<uint64_t>(a.lv.M, a.T));
-    if (!generic_only && a.small_codes && a.lv.KW <= 4 && a.T <= 64 && a.lv.M <= 32 && fast_bytes <= 100 * 1024)
-        return launch_probe_fast(a, st);
+    if (probe_fast_eligible(a)) return launch_probe_fast(a, st);
     k_probe<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(a);
     return cudaGetLastError();
 }

@@ -345,7 +345,9 @@ __global__ void k_bucket_sizes(const uint64_t* __restrict__ boff, const uint32_t
 __global__ void k_hash_build(const uint64_t* __restrict__ boff, const uint32_t* __restrict__ ukeys, int M, int KW,
                              const uint16_t* __restrict__ foff, const uint8_t* __restrict__ fbits,
                              const unsigned long long* __restrict__ rmul, const uint64_t* __restrict__ hoff,
-                             const uint32_t* __restrict__ hmask, unsigned long long* __restrict__ hslots, int* err) {
+                             const uint32_t* __restrict__ hmask, unsigned long long* __restrict__ hslots,
+                             uint32_t* __restrict__ filt, const uint64_t* __restrict__ fl_off,
+                             const uint32_t* __restrict__ fl_mask, int* err) {
     const int l = blockIdx.y;
     const int64_t j = (int64_t)blockIdx.x * NT + threadIdx.x;
     const int64_t B = (int64_t)(boff[l + 1] - boff[l]);
@@ -362,6 +364,10 @@ __global__ void k_hash_build(const uint64_t* __restrict__ boff, const uint32_t* 
     const uint64_t hh = hash_finish(hs);
     const uint32_t h = (uint32_t)hh;
     const uint32_t fp = slot_fp(hh);
+    if (filt) {
+        const uint32_t fx = filter_mix(hh);
+        atomicOr(filt + fl_off[l] + (fx & fl_mask[l]), filter_bits(fx));
+    }
     unsigned long long* slots = hslots + hoff[l];
     // Claim the first empty slot in probe order (a group's slots in order,
     // then the next group), then store the bucket index beside it. Lookups
@@ -579,11 +585,12 @@ cudaError_t launch_bucket_sizes(const uint64_t* boff, const uint32_t* starts, in
 
 cudaError_t launch_hash_build(const uint64_t* boff, const uint32_t* ukeys, int L, int M, int KW, int64_t maxB,
                               const uint16_t* foff, const uint8_t* fbits, const unsigned long long* rmul,
-                              const uint64_t* hoff, const uint32_t* hmask, unsigned long long* hslots, int* err,
+                              const uint64_t* hoff, const uint32_t* hmask, unsigned long long* hslots,
+                              uint32_t* filt, const uint64_t* fl_off, const uint32_t* fl_mask, int* err,
                               cudaStream_t st) {
     if (maxB <= 0) return cudaSuccess;
     k_hash_build<<<dim3(blocks_for(maxB), L), NT, 0, st>>>(boff, ukeys, M, KW, foff, fbits, rmul, hoff, hmask,
-                                                          hslots, err);
+                                                          hslots, filt, fl_off, fl_mask, err);
     return cudaGetLastError();
 }
 

@@ -146,6 +146,8 @@ typedef struct culsh_tuning {
     int ws_set_slots;     /* work-stealing shared hash set per item: 4096 or 8192 slots */
     float search_ms;      /* culsh_search_autotune: median device ms of the choice       */
     int configs_tried;    /* culsh_search_autotune: configurations timed                 */
+    int probe_split;      /* 1 (M <= 16): enumerate every probe first, then look each up
+                             in its own thread behind a key filter (same results as 0) */
 } culsh_tuning;
 
 /* Times the search over the tuning space on the caller's queries (device

@@ -75,11 +75,16 @@ def test_every_tuning_configuration(culsh, name):
     ht = build_index(culsh, c)
     st = culsh.SearchTables()
     st.reset(ht, int(c["K"]), int(c["T"]))
+    M = c["A"].shape[1]
     for tile, pch in itertools.product((0, 1, 2), (1, 2, 4)):
-        st.set_tuning(proj_tile=tile, probe_batch=pch)
-        st.search(c["queries"], dataset=c["X"])
-        check_search(st, c)
-    st.set_tuning(proj_tile=0, probe_batch=2, candidates_mode=0)
+        launches = []
+        for split in (0, 1):
+            st.set_tuning(proj_tile=tile, probe_batch=pch, probe_split=split)
+            st.search(c["queries"], dataset=c["X"])
+            check_search(st, c)
+            launches.append(st.profile()["launches"])
+        assert launches[1] == launches[0] + (M <= 16)   # the split form's lookup kernel
+    st.set_tuning(proj_tile=0, probe_batch=2, probe_split=0, candidates_mode=0)
     st.search(c["queries"], dataset=c["X"])
     check_search(st, c)
     assert st.profile()["candidates_mode"] == 0
@@ -148,7 +153,7 @@ def test_bf16_form_extreme_magnitudes_and_ties(culsh):
 def test_tuning_rejects_out_of_range(culsh):
     st = culsh.SearchTables()
     for bad in ({"probe_batch": 3}, {"proj_tile": 5}, {"ws_threads": 96}, {"ws_chunk": 8}, {"candidates_mode": 2},
-                {"distance_bf16": 2}, {"ws_set_slots": 5000}):
+                {"distance_bf16": 2}, {"ws_set_slots": 5000}, {"probe_split": 2}):
         with pytest.raises(culsh.CulshError) as ei:
             st.set_tuning(**bad)
         assert ei.value.code == culsh.ERR_INVALID_ARGUMENT
@@ -172,6 +177,7 @@ def test_autotune_keeps_results(culsh):
     assert tune["ws_set_slots"] in (4096, 8192)
     assert tune["distance_bf16"] in (0, 1)
     assert tune["probe_batch"] in (1, 2, 4) and tune["ws_threads"] in (64, 128, 256)
+    assert tune["probe_split"] in (0, 1)
     assert st.get_tuning()["probe_batch"] == tune["probe_batch"]
     torch.cuda.synchronize()
     np.testing.assert_array_equal(ids.cpu().numpy(), c["knn_ids"])

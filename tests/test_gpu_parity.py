@@ -252,17 +252,34 @@ def test_search_general_probe_kernel(culsh, name, monkeypatch):
     check_search(st, c)
 
 
+@pytest.mark.parametrize("name", golden_cases())
+def test_search_split_probe_lookups(culsh, name, monkeypatch):
+    """Split lookups (every probe enumerated first, then one lookup thread per
+    probe behind the key filter) give exactly the fused kernel's results:
+    query buckets, non-unique counts, ids and distances."""
+    monkeypatch.setenv("CULSH_PROBE_SPLIT", "1")
+    c = load_case(name)
+    ht = build_index(culsh, c)
+    st = culsh.SearchTables()
+    st.reset(ht, int(c["K"]), int(c["T"]))
+    st.search(c["queries"], dataset=c["X"])
+    check_search(st, c)
+    np.testing.assert_array_equal(st.getKnnDistances(), c["knn_dists"])
+
+
+@pytest.mark.parametrize("split", ["0", "1"])
 @pytest.mark.parametrize("M,T,ties", [(9, 16, False), (12, 16, False), (12, 16, True), (16, 24, False),
                                        (16, 16, True), (5, 9, True)])
-def test_probe_order_register_network(culsh, M, T, ties):
+def test_probe_order_register_network(culsh, M, T, ties, split, monkeypatch):
     """For M <= 16 the fast kernel orders the 2M deltas in registers (sorting
     network + merge by counting) and takes the reference's heap procedure
     whenever two deltas tie. Query buckets (the probe order of every table)
     and kNN ids match the oracle. The tie cases mix queries with integer
     projections and W = 4 or 8 (downs are multiples of 1/W, so M > W downs
     must tie, and downs of 1/2 tie with ups) with noisy queries whose deltas
-    are all distinct."""
+    are all distinct. Both probe forms (fused and split lookups) run."""
     import oracle
+    monkeypatch.setenv("CULSH_PROBE_SPLIT", split)
     rng = np.random.default_rng(100 * M + T)
     N, D, L = 3000, 16, 3
     if ties:
