@@ -1564,11 +1564,14 @@ int culsh_search_run(culsh_search* s, const float* queries, int Q, const float* 
     CU_TRY(s->h_d.reserve((size_t)Q * K));
     if (dbg) fprintf(dbg, "[SearchTables::search]\tPerforming searching. (Q, K, T) = (%d, %d, %d)\n", Q, K, s->T);
     if (direct_host_access() && ((uintptr_t)queries & 15u) == 0) {
-        // The GPU reads the caller's (pageable) queries through the host page
-        // tables and writes the results into the pinned result buffers: no
-        // staging copies. Query rows are read with 16-byte loads, hence the
-        // alignment condition.
-        TRY(search_device(s, queries, Q, s->h_ids.p, s->h_d.p, st));
+        // One kernel reads the caller's (pageable) queries through the host
+        // page tables into the device query buffer (one pass, 16-byte loads,
+        // hence the alignment condition), and the search writes its results
+        // into the pinned result buffers: no staging copies, and the graph
+        // key does not depend on the caller's buffer.
+        CU_TRY(s->dq.reserve((size_t)Q * D));
+        CU_TRY(launch_copy_f32(queries, s->dq.p, (int64_t)Q * D, st));
+        TRY(search_device(s, s->dq.p, Q, s->h_ids.p, s->h_d.p, st));
         s->host_path = 2;
     } else {
         CU_TRY(s->dq.reserve((size_t)Q * D));

@@ -140,6 +140,9 @@ cudaError_t launch_project_fp32(const float* X, int64_t n_pts, int D, const floa
                                 int LM, float W, int32_t* codes, float* vals, int32_t* pmin, int32_t* pmax, int* err,
                                 cudaStream_t st, int tile = 0);
 int project_grid_x(int64_t n_pts);
+// n floats, 16-byte aligned source and destination (src may be host memory
+// the device reads directly).
+cudaError_t launch_copy_f32(const float* src, float* dst, int64_t n, cudaStream_t st);
 cudaError_t launch_minmax_reduce(const int32_t* pmin, const int32_t* pmax, int nparts, int LM, int32_t* cmin,
                                  int32_t* cmax, cudaStream_t st);
 

@@ -11,6 +11,7 @@
 // multiply-add chain over d = 0..D-1 in ascending order (register-tiled, the
 // tiling never reorders a chain), so codes are bit-exact against the CPU
 // oracle. The FP32 FMA pipe bounds this kernel (2*N*D*L*M flops).
+#include <algorithm>
 #include <cfloat>
 #include <climits>
 
@@ -279,6 +280,30 @@ cudaError_t launch_project_fp32(const float* X, int64_t n_pts, int D, const floa
 cudaError_t launch_minmax_reduce(const int32_t* pmin, const int32_t* pmax, int nparts, int LM, int32_t* cmin,
                                  int32_t* cmax, cudaStream_t st) {
     k_minmax_reduce<<<LM, 256, 0, st>>>(pmin, pmax, nparts, LM, cmin, cmax);
+    return cudaGetLastError();
+}
+
+// Copies n floats from src (16-byte aligned; host memory the device can read,
+// or device memory) to dst with 16-byte loads: one pass over the source.
+__global__ void k_copy_f32(const float* __restrict__ src, float* __restrict__ dst, int64_t n) {
+    const int64_t n4 = n >> 2;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const float4* s4 = reinterpret_cast<const float4*>(src);
+    float4* d4 = reinterpret_cast<float4*>(dst);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) d4[i] = s4[i];
+    const int64_t tail = (n4 << 2) + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tail < n) dst[tail] = src[tail];
+}
+
+cudaError_t launch_copy_f32(const float* src, float* dst, int64_t n, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    if (((uintptr_t)src & 15) || ((uintptr_t)dst & 15)) return cudaErrorInvalidValue;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t want = ((n >> 2) + 255) / 256;
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)std::max(sms, 1) * 8));
+    k_copy_f32<<<blocks, 256, 0, st>>>(src, dst, n);
     return cudaGetLastError();
 }
 
