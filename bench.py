@@ -512,9 +512,17 @@ def run_culsh(args):
     peak, peak_kind = hbm_peak()
     achieved = sb[dom] / (med[dom] / 1e3) / 1e9
     kernel_name = {"project": "k_project", "probe": "k_probe", "candidates": "k_candidates"}[dom]
+    kernel_label = kernel_name
+    if dom == "probe":
+        # the probe stage is one fused kernel or, in the split form (M <= 16),
+        # the enumeration kernel plus the lookup kernel
+        env = os.environ.get("CULSH_PROBE_SPLIT")
+        split = (env != "0" if env is not None else bool(st.get_tuning().get("probe_split", 0))) and M <= 16
+        kernel_name = "k_probe_split" if split else "k_probe_fused"
+        kernel_label = "k_probe_fast (enumeration) + k_probe_resolve" if split else "k_probe_fast"
     roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 5), "traffic": ncu_traffic(kernel_name, name),
-                "kernel": kernel_name, "algorithmic_bytes": sb[dom], "peak_source": f"{peak_kind} hbm_gbs",
+                "kernel": kernel_label, "algorithmic_bytes": sb[dom], "peak_source": f"{peak_kind} hbm_gbs",
                 "stage_ms_median": {k: round(v, 4) for k, v in med.items()}}
 
     # End to end through the reference-facing C ABI with host buffers.

@@ -734,7 +734,7 @@ __device__ __forceinline__ int32_t resolve_slot(const ProbeArgs& a, int l, int q
     return -1;
 }
 
-__global__ void __launch_bounds__(256, 4) k_probe_resolve(ProbeArgs a) {
+__global__ void __launch_bounds__(256, 5) k_probe_resolve(const __grid_constant__ ProbeArgs a) {
     const LookupView& lv = a.lv;
     const int Q = a.Q, T = a.T;
     const int G = (T + kResolveSlots - 1) / kResolveSlots;
@@ -758,26 +758,28 @@ __global__ void __launch_bounds__(256, 4) k_probe_resolve(ProbeArgs a) {
     }
     if (v[0] != -2 && v[1] != -2 && v[2] != -2 && v[3] != -2) return;
     const int64_t base = (int64_t)l * T * Q + (int64_t)t0 * Q + q;
-    uint64_t hh[kResolveSlots];
-    uint32_t fw[kResolveSlots], need[kResolveSlots];
-#pragma unroll
-    for (int k = 0; k < kResolveSlots; ++k) hh[k] = v[k] == -2 ? a.ph[base + (int64_t)k * Q] : 0;
+    // Filter words of the pending slots, all four loads in flight together.
     const uint32_t* filt = lv.filt ? lv.filt + __ldg(lv.fl_off + l) : nullptr;
     const uint32_t fmask = lv.filt ? __ldg(lv.fl_mask + l) : 0;
+    uint32_t fw[kResolveSlots], need[kResolveSlots];
 #pragma unroll
     for (int k = 0; k < kResolveSlots; ++k) {
-        const uint32_t fx = filter_mix(hh[k]);
-        need[k] = filter_bits(fx);
-        fw[k] = (v[k] == -2 && filt) ? __ldg(filt + (fx & fmask)) : ~0u;
+        need[k] = 0;
+        fw[k] = 0;
+        if (v[k] == -2) {
+            const uint32_t fx = filter_mix(a.ph[base + (int64_t)k * Q]);
+            need[k] = filter_bits(fx);
+            fw[k] = filt ? __ldg(filt + (fx & fmask)) : ~0u;
+        }
     }
-    unsigned long long added = 0;
+    // Slots the filter rules out are misses; the rest (a few percent when
+    // most probes miss) are resolved one at a time after the common store.
+    uint32_t pass = 0;
 #pragma unroll
     for (int k = 0; k < kResolveSlots; ++k) {
         if (v[k] != -2) continue;
-        int32_t res = -1;
-        if ((fw[k] & need[k]) == need[k]) res = resolve_slot(a, l, q, hh[k], a.pmask[base + (int64_t)k * Q]);
-        v[k] = res;
-        if (res >= 0) added += __ldg(lv.sizes + __ldg(lv.boff + l) + res);
+        if ((fw[k] & need[k]) == need[k]) pass |= 1u << k;
+        else v[k] = -1;
     }
     if (vec) {
         *reinterpret_cast<int4*>(qb) = make_int4(v[0], v[1], v[2], v[3]);
@@ -785,6 +787,16 @@ __global__ void __launch_bounds__(256, 4) k_probe_resolve(ProbeArgs a) {
 #pragma unroll
         for (int k = 0; k < kResolveSlots; ++k)
             if (t0 + k < T) qb[k] = v[k];
+    }
+    if (!pass) return;
+    unsigned long long added = 0;
+    const uint64_t bo = __ldg(lv.boff + l);
+#pragma unroll 1
+    for (; pass; pass &= pass - 1) {
+        const int k = lowest_bit(pass);
+        const int32_t res = resolve_slot(a, l, q, a.ph[base + (int64_t)k * Q], a.pmask[base + (int64_t)k * Q]);
+        qb[k] = res;
+        if (res >= 0) added += __ldg(lv.sizes + bo + res);
     }
     if (added) atomicAdd(a.cnu + q, added);
 }
