@@ -416,6 +416,24 @@ __device__ __forceinline__ bool order_deltas_net(const float* dn, uint8_t* enc, 
     return ok;
 }
 
+// The reference's heap procedure over a pair's 2M deltas, for the rare pairs
+// whose deltas tie (or are NaN). Out of line: inlined, its loops enlarge the
+// probe kernel and slow every pair. dn: the pair's downs (strided slice);
+// enc: receives sorted delta -> column | up << 7.
+__device__ __noinline__ void order_deltas_heap(const float* dn, uint8_t* enc, int M) {
+    auto dv = [&](int i) {
+        const float d = dn[(i < M ? i : i - M) * PF];
+        return i < M ? d : __fsub_rn(1.0f, d);
+    };
+    const int M2 = 2 * M;
+    int8_t* perm = reinterpret_cast<int8_t*>(enc);
+    heap_order_strided(dv, perm, M2, M2);
+    for (int i = 0; i < M2; ++i) {
+        const int pm = perm[i * PF];
+        enc[i * PF] = (uint8_t)((pm % M) | (pm >= M ? 0x80 : 0));
+    }
+}
+
 // Per-thread shared-memory slice of the fast kernel, in bytes per thread.
 template <typename MaskT>
 __host__ __device__ constexpr size_t probe_fast_bytes_per_thread(int M, int T) {
@@ -426,7 +444,7 @@ __host__ __device__ constexpr size_t probe_fast_bytes_per_thread(int M, int T) {
 // MM > 0: M <= MM, deltas ordered in registers (order_deltas_net); MM = 0:
 // ranking and merge over the shared-memory slice.
 template <typename MaskT, int PCH, int MM, bool kSplit>
-__global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
+__global__ void __launch_bounds__(PF, kSplit ? 8 : 6) k_probe_fast(ProbeArgs a) {
     extern __shared__ __align__(16) unsigned char psm[];
     const LookupView& lv = a.lv;
     const int Q = a.Q, T = a.T, L = lv.L, M = lv.M, KW = lv.KW;
@@ -488,14 +506,7 @@ __global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
 
     if (T > 1 && MM > 0) {
         if (distinct) distinct = order_deltas_net<(MM > 0 ? MM : 1)>(dn, enc, M, sv);
-        if (!distinct) {
-            int8_t* perm = reinterpret_cast<int8_t*>(enc);
-            heap_order_strided(dv, perm, M2, M2);
-            for (int i = 0; i < M2; ++i) {
-                const int pm = perm[i * PF];
-                enc[i * PF] = (uint8_t)((pm % M) | (pm >= M ? 0x80 : 0));
-            }
-        }
+        if (!distinct) order_deltas_heap(dn, enc, M);
         comb[0] = 1;
         cd[0] = sv(0);
     } else if (T > 1) {
@@ -531,14 +542,7 @@ __global__ void __launch_bounds__(PF, 6) k_probe_fast(ProbeArgs a) {
                 else --iu;
             }
         }
-        if (!distinct) {
-            int8_t* perm = reinterpret_cast<int8_t*>(enc);
-            heap_order_strided(dv, perm, M2, M2);
-            for (int i = 0; i < M2; ++i) {
-                const int pm = perm[i * PF];
-                enc[i * PF] = (uint8_t)((pm % M) | (pm >= M ? 0x80 : 0));
-            }
-        }
+        if (!distinct) order_deltas_heap(dn, enc, M);
         comb[0] = 1;
         cd[0] = sv(0);
     }
