@@ -350,7 +350,19 @@ def recall_point(culsh, torch, dev, steps, warmup, autotune=True):
     if autotune:   # untimed; the tuner may pick either distance form, both are timed below
         tuned = st.autotune(qt.data_ptr(), Q, ids.data_ptr(), dists.data_ptr(), sp)
     for name, bf in (("fp32", 0), ("bf16_rerank", 1)):
-        st.set_tuning(candidates_mode=1, distance_bf16=bf)
+        # each form at its own best set size, partition size and item order
+        # (untimed selection among a few; the tuner's choice is one of them)
+        best = None
+        for sl, ch in ((4096, 2048), (8192, 4096), (16384, 8192)):
+            for order in (0, 1):
+                st.set_tuning(candidates_mode=1, distance_bf16=bf, ws_set_slots=sl, ws_chunk=ch, ws_order=order)
+                t = []
+                for _ in range(3):
+                    st.search_device(qt.data_ptr(), Q, ids.data_ptr(), dists.data_ptr(), sp)
+                    t.append(st.profile()["candidates_ms"])
+                if best is None or statistics.median(t) < best[0]:
+                    best = (statistics.median(t), sl, ch, order)
+        st.set_tuning(candidates_mode=1, distance_bf16=bf, ws_set_slots=best[1], ws_chunk=best[2], ws_order=best[3])
         for _ in range(warmup):
             st.search_device(qt.data_ptr(), Q, ids.data_ptr(), dists.data_ptr(), sp)
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
@@ -369,6 +381,7 @@ def recall_point(culsh, torch, dev, steps, warmup, autotune=True):
             ref = out
         pr = st.profile()
         forms[name] = {"qps": round(Q / (ms / 1e3), 1), "ms_per_step": round(ms, 3),
+                       "set_slots": best[1], "chunk": best[2], "order": best[3],
                        "candidates_ms": round(statistics.median(cand), 3), "rechecked_fp32": int(pr["rechecked"]),
                        "identical_to_fp32": bool(np.array_equal(out, ref))}
     uniq = st.getTotalCandidates_unique() / Q

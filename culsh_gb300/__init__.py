@@ -63,7 +63,7 @@ class _Tuning(ctypes.Structure):
     _fields_ = [("proj_tile", ctypes.c_int), ("probe_batch", ctypes.c_int), ("candidates_mode", ctypes.c_int),
                 ("ws_threads", ctypes.c_int), ("ws_blocks_per_sm", ctypes.c_int), ("ws_chunk", ctypes.c_int),
                 ("distance_bf16", ctypes.c_int), ("ws_set_slots", ctypes.c_int), ("search_ms", ctypes.c_float),
-                ("configs_tried", ctypes.c_int), ("probe_split", ctypes.c_int)]
+                ("configs_tried", ctypes.c_int), ("probe_split", ctypes.c_int), ("ws_order", ctypes.c_int)]
 
 
 class _IndexProfile(ctypes.Structure):
@@ -334,7 +334,7 @@ class SearchTables:
     def set_tuning(self, **kw):
         """Sets tuning fields (proj_tile, probe_batch, probe_split,
         candidates_mode, ws_threads, ws_blocks_per_sm, ws_chunk,
-        distance_bf16, ws_set_slots); others keep their value."""
+        distance_bf16, ws_set_slots, ws_order); others keep their value."""
         t = _Tuning()
         _check(lib().culsh_search_get_tuning(self._h, ctypes.byref(t)))
         for k, v in kw.items():

@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(PT_PLAN) k_plan_items(WsArgs a) {
     __shared__ uint8_t s_empty[PT_PLAN];
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int q0 = blockIdx.x * PT_PLAN;
-    const int q = q0 + tid;
+    const int q = q0 + tid < a.Q ? (a.order ? (int)a.order[q0 + tid] : q0 + tid) : a.Q;
     uint32_t P = 0;
     bool dense = false;
     if (q < a.Q) {
@@ -96,16 +96,79 @@ __global__ void __launch_bounds__(PT_PLAN) k_plan_items(WsArgs a) {
     for (int i = tid; i < nq * K; i += PT_PLAN) {
         const int ql = i / K;
         if (s_empty[ql]) {
-            a.out_ids[(int64_t)q0 * K + i] = -1;
-            a.out_d[(int64_t)q0 * K + i] = FLT_MAX;
+            const int64_t qq = a.order ? (int64_t)a.order[q0 + ql] : (int64_t)(q0 + ql);
+            const int64_t o = qq * K + (i - ql * K);
+            a.out_ids[o] = -1;
+            a.out_d[o] = FLT_MAX;
         }
     }
 }
 
+// Locality order of the queries: a counting sort into kOrderBins bins of the
+// home bucket of table 0 (bucket indices follow the lexicographic order of
+// the codes, so nearby bins hold nearby points); queries without a home
+// bucket go to the last bin. Order within a bin is arbitrary.
+__device__ __forceinline__ uint32_t order_bin(const WsArgs& a, int q) {
+    const int32_t b = a.qbuckets[(int64_t)q * a.T];   // table 0, probe 0
+    const uint64_t b0 = a.boff[1] - a.boff[0];
+    return b < 0 || b0 == 0 ? (uint32_t)kOrderBins : (uint32_t)((uint64_t)b * kOrderBins / b0);
+}
+
+__global__ void k_order_hist(WsArgs a) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < a.Q) atomicAdd(a.order_bins + order_bin(a, q), 1u);
+}
+
+// Exclusive scan of kOrderBins + 1 counters in one block of 1024 threads.
+__global__ void __launch_bounds__(1024) k_order_scan(WsArgs a) {
+    constexpr int PER = (kOrderBins + 1 + 1023) / 1024;
+    __shared__ uint32_t warp_sum[32];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    uint32_t v[PER], tot = 0;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int i = tid * PER + k;
+        v[k] = i <= kOrderBins ? a.order_bins[i] : 0u;
+        tot += v[k];
+    }
+    uint32_t x = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sum[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t s = warp_sum[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        warp_sum[lane] = s - warp_sum[lane];
+    }
+    __syncthreads();
+    uint32_t run = warp_sum[w] + x - tot;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int i = tid * PER + k;
+        if (i <= kOrderBins) a.order_bins[i] = run;
+        run += v[k];
+    }
+}
+
+__global__ void k_order_scatter(WsArgs a) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < a.Q) a.order[atomicAdd(a.order_bins + order_bin(a, q), 1u)] = (uint32_t)q;
+}
+
 // WT threads per item: WT / 32 warps each keep a sorted top-K list over a
 // strided share of the item's candidates (tuned: 64, 128 or 256).
-// W_SLOTS: shared hash-set slots per item (4096 or 8192, tuned); an item
-// holds at most W_CAP = W_SLOTS / 2 distinct ids.
+// W_SLOTS: shared hash-set slots per item (4096, 8192 or 16384, tuned); an
+// item holds at most W_CAP = W_SLOTS / 2 distinct ids. Every item of a query
+// scans the query's whole id list and keeps its partition, so larger sets
+// (fewer, larger partitions) scan less at the cost of occupancy.
 template <int WT, bool kBF16, int W_SLOTS>
 __global__ void __launch_bounds__(WT) k_candidates_ws(WsArgs a) {
     constexpr int WW = WT / 32;
@@ -509,6 +572,17 @@ size_t ws_smem_bytes(int D, int K, int wt, int bf16, int slots) {
            (size_t)(wt / 32) * K * (sizeof(float) + sizeof(uint32_t)) + (bf16 ? 2 * sizeof(float) * cap : 0);
 }
 
+cudaError_t launch_order_queries(const WsArgs& a, cudaStream_t st) {
+    if (a.Q <= 0 || !a.order) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(a.order_bins, 0, sizeof(uint32_t) * (kOrderBins + 1), st);
+    if (e != cudaSuccess) return e;
+    const unsigned g = (unsigned)((a.Q + 255) / 256);
+    k_order_hist<<<g, 256, 0, st>>>(a);
+    k_order_scan<<<1, 1024, 0, st>>>(a);
+    k_order_scatter<<<g, 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_plan_items(const WsArgs& a, cudaStream_t st) {
     if (a.Q <= 0) return cudaSuccess;
     k_plan_items<<<(a.Q + PT_PLAN - 1) / PT_PLAN, PT_PLAN, 0, st>>>(a);
@@ -586,11 +660,14 @@ __global__ void k_bf16_rows(const float* __restrict__ X, int64_t N, int D, uint1
 }  // namespace
 
 cudaError_t launch_candidates_ws(const WsArgs& a, int grid, cudaStream_t st) {
+    if (a.slots == 16384)
+        return a.bf16 ? launch_ws_w<true, 16384>(a, grid, st) : launch_ws_w<false, 16384>(a, grid, st);
     if (a.slots == 8192) return a.bf16 ? launch_ws_w<true, 8192>(a, grid, st) : launch_ws_w<false, 8192>(a, grid, st);
     return a.bf16 ? launch_ws_w<true, 4096>(a, grid, st) : launch_ws_w<false, 4096>(a, grid, st);
 }
 
 int ws_blocks_per_sm(int D, int K, int wt, int bf16, int slots) {
+    if (slots == 16384) return bf16 ? ws_bps_w<true, 16384>(D, K, wt) : ws_bps_w<false, 16384>(D, K, wt);
     if (slots == 8192) return bf16 ? ws_bps_w<true, 8192>(D, K, wt) : ws_bps_w<false, 8192>(D, K, wt);
     return bf16 ? ws_bps_w<true, 4096>(D, K, wt) : ws_bps_w<false, 4096>(D, K, wt);
 }

@@ -197,8 +197,9 @@ struct SearchTune {
     int ws_bps = 0;        // resident work-stealing CTAs per SM (0: occupancy limit)
     int ws_chunk = 1024;   // non-unique candidates per id partition
     int dist_bf16 = 0;     // 1: BF16 candidate distances + certified FP32 rerank (work-stealing form)
-    int ws_slots = 4096;   // shared hash-set slots per work item (4096 or 8192)
+    int ws_slots = 4096;   // shared hash-set slots per work item (4096, 8192 or 16384)
     int probe_split = 0;   // 1: enumeration kernel, then one lookup thread per probe (M <= 16)
+    int ws_order = 0;      // 1: plan queries in the locality order of their home bucket (work-stealing form)
 };
 constexpr size_t kPlanBytes = 1024;   // room for the graph key (checked below)
 
@@ -222,6 +223,7 @@ struct culsh_search {
     DevBuf<uint32_t> arena;
     // work-stealing candidate stage
     DevBuf<int> q_items, q_off, item_q, part_n, dense_q;
+    DevBuf<uint32_t> qorder, qorder_bins;
     DevBuf<unsigned int> q_done;
     DevBuf<uint8_t> item_p;
     DevBuf<float> part_d;
@@ -1020,6 +1022,12 @@ int plan_search(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* 
         }
         a.n_dense = reinterpret_cast<unsigned int*>(s->stats.p + 7);
         a.dense_next = reinterpret_cast<unsigned int*>(s->stats.p + 7) + 1;
+        if (tu.ws_order) {
+            CU_TRY(s->qorder.reserve(Q));
+            CU_TRY(s->qorder_bins.reserve(kOrderBins + 1));
+            a.order = s->qorder.p;
+            a.order_bins = s->qorder_bins.p;
+        }
         if (bf16) {
             // |d~ - d| <= c1 d~ + c2 (2 rho b1 + rho^2 b2) with gamma_n = n u / (1 - n u),
             // n = ceil(D/8) + 6 roundings along any path, u = 2^-24:
@@ -1056,6 +1064,7 @@ int enqueue_search(const SearchPlan& P, cudaStream_t st, bool capturing, int* la
     CU_TRY(launch_probe(P.pa, st));
     CU_TRY(cudaEventRecordWithFlags(P.ev[2], st, evf));
     if (P.use_ws) {
+        if (P.wa.order) CU_TRY(launch_order_queries(P.wa, st));
         CU_TRY(launch_plan_items(P.wa, st));
         CU_TRY(launch_candidates_ws(P.wa, P.ws_grid, st));
         if (P.use_dense) CU_TRY(launch_candidates_dense(P.wa, P.dense_grid, st));
@@ -1064,7 +1073,7 @@ int enqueue_search(const SearchPlan& P, cudaStream_t st, bool capturing, int* la
     }
     CU_TRY(cudaEventRecordWithFlags(P.ev[3], st, evf));
     CU_TRY(cudaMemcpyAsync(P.h_stats, P.stats, 8 * 8, cudaMemcpyDeviceToHost, st));
-    *launches = (P.use_ws ? (P.use_dense ? 4 : 3) : 2) + probe_launches(P.pa);
+    *launches = (P.use_ws ? (P.use_dense ? 4 : 3) + (P.wa.order ? 3 : 0) : 2) + probe_launches(P.pa);
     return CULSH_OK;
 }
 
@@ -1639,6 +1648,8 @@ long long culsh_search_device_bytes(culsh_search* s) {
     add(s->part_d);
     add(s->part_i);
     add(s->dense_q);
+    add(s->qorder);
+    add(s->qorder_bins);
     return (long long)b;
 }
 
@@ -1650,6 +1661,7 @@ long long culsh_search_estimate_bytes(const culsh_index* ix, int Q, int K, int T
     size_t cap = std::max<size_t>(2 * q, kWsPartialBytes / per_item);
     cap = std::min(cap, q * kWsPartitions);
     b += 16 * q + cap * per_item;   // per-query plan arrays, dense-query list, partial lists
+    b += 4 * q + 4 * (kOrderBins + 1);   // locality order
     if (M <= 16) b += 12 * L * q * (size_t)T + 48 * L * q;   // split probe lookups
     return (long long)b;
 }
@@ -1683,6 +1695,8 @@ int culsh_search_release(culsh_search* s) {
     s->part_d.release();
     s->part_i.release();
     s->dense_q.release();
+    s->qorder.release();
+    s->qorder_bins.release();
     s->Q = 0;
     s->searched = false;
     s->qb_host_valid = false;
@@ -1699,6 +1713,7 @@ static void tune_to_c(const SearchTune& t, culsh_tuning* o) {
     o->distance_bf16 = t.dist_bf16;
     o->ws_set_slots = t.ws_slots;
     o->probe_split = t.probe_split;
+    o->ws_order = t.ws_order;
 }
 
 int culsh_search_get_tuning(culsh_search* s, culsh_tuning* out) {
@@ -1716,8 +1731,8 @@ int culsh_search_set_tuning(culsh_search* s, const culsh_tuning* in) {
                     (in->ws_threads == 64 || in->ws_threads == 128 || in->ws_threads == 256) &&
                     in->ws_blocks_per_sm >= 0 && in->ws_blocks_per_sm <= 64 && in->ws_chunk >= 64 &&
                     in->ws_chunk <= 65536 && (in->distance_bf16 == 0 || in->distance_bf16 == 1) &&
-                    (in->ws_set_slots == 4096 || in->ws_set_slots == 8192) &&
-                    (in->probe_split == 0 || in->probe_split == 1);
+                    (in->ws_set_slots == 4096 || in->ws_set_slots == 8192 || in->ws_set_slots == 16384) &&
+                    (in->probe_split == 0 || in->probe_split == 1) && (in->ws_order == 0 || in->ws_order == 1);
     if (!ok) return fail(CULSH_ERR_INVALID_ARGUMENT, "tuning value out of range");
     s->tune.proj_tile = in->proj_tile;
     s->tune.probe_pch = in->probe_batch;
@@ -1728,6 +1743,7 @@ int culsh_search_set_tuning(culsh_search* s, const culsh_tuning* in) {
     s->tune.dist_bf16 = in->distance_bf16;
     s->tune.ws_slots = in->ws_set_slots;
     s->tune.probe_split = in->probe_split;
+    s->tune.ws_order = in->ws_order;
     return CULSH_OK;
 }
 
@@ -1737,10 +1753,11 @@ int culsh_search_set_graphs(culsh_search* s, int enabled) {
     return CULSH_OK;
 }
 
-// Coordinate search: the projection tiling by its stage time, the probe batch
-// depth by its stage time, then the candidate stage over its kernel form,
-// item width, partition size and residency. Each configuration is searched
-// once untimed and three times timed (median of each stage, device events).
+// Coordinate search: the projection tiling by its stage time, the probe form
+// by its stage time, then the candidate stage over its kernel form, item
+// width, set size and partition size, distance form and locality order
+// jointly, then the residency. Each configuration is searched once untimed
+// and three times timed (median of each stage, device events).
 int culsh_search_autotune(culsh_search* s, const float* d_queries, int Q, int* d_ids, float* d_dists, void* stream,
                           culsh_tuning* out) {
     TRY(precheck_search(s, Q));
@@ -1829,19 +1846,22 @@ int culsh_search_autotune(culsh_search* s, const float* d_queries, int Q, int* d
         // (set slots, partition size): a partition of `chunk` non-unique
         // candidates always fits a set of 2 * chunk slots
         const int wts[3] = {64, 128, 256};
-        const int sets[5][2] = {{4096, 1024}, {4096, 2048}, {8192, 1024}, {8192, 2048}, {8192, 4096}};
-        for (int f = 0; f < 2; ++f)
-            for (int a = 0; a < 3; ++a)
-                for (int b = 0; b < 5; ++b) {
-                    SearchTune u = best;
-                    u.cand_ws = 1;
-                    u.ws_wt = wts[a];
-                    u.ws_slots = sets[b][0];
-                    u.ws_chunk = sets[b][1];
-                    u.ws_bps = 0;
-                    u.dist_bf16 = f;
-                    cands.push_back(u);
-                }
+        const int sets[7][2] = {{4096, 1024}, {4096, 2048}, {8192, 1024}, {8192, 2048},
+                                {8192, 4096}, {16384, 4096}, {16384, 8192}};
+        for (int o = 0; o < 2; ++o)
+            for (int f = 0; f < 2; ++f)
+                for (int a = 0; a < 3; ++a)
+                    for (int b = 0; b < 7; ++b) {
+                        SearchTune u = best;
+                        u.cand_ws = 1;
+                        u.ws_wt = wts[a];
+                        u.ws_slots = sets[b][0];
+                        u.ws_chunk = sets[b][1];
+                        u.ws_bps = 0;
+                        u.dist_bf16 = f;
+                        u.ws_order = o;
+                        cands.push_back(u);
+                    }
     }
     bool first = true;
     for (const SearchTune& t : cands) {
@@ -1868,7 +1888,10 @@ int culsh_search_autotune(culsh_search* s, const float* d_queries, int Q, int* d
                 s->tune = start;
                 return rc;
             }
-            if (stage[2] < best_t) best = t;
+            if (stage[2] < best_t) {
+                best = t;
+                best_t = stage[2];
+            }
         }
     }
     s->tune = best;

@@ -318,7 +318,14 @@ struct WsArgs {
     int* dense_q;                      // [Q] queries routed to the bitmap kernel
     unsigned int* n_dense;
     unsigned int* dense_next;          // claim counter of the bitmap kernel
+    // Locality order (tuned): queries planned in the order of their home
+    // bucket in table 0 (launch_order_queries), so that items of queries
+    // with shared candidates run close together and share rows in L2.
+    uint32_t* order;                   // [Q] queries in that order; nullptr: index order
+    uint32_t* order_bins;              // [kOrderBins + 1] counting-sort bins
 };
+constexpr int kOrderBins = 4096;
+cudaError_t launch_order_queries(const WsArgs& a, cudaStream_t st);   // 3 kernels + 1 memset
 size_t dense_smem_bytes(int64_t N, int D, int K);
 cudaError_t launch_candidates_dense(const WsArgs& a, int grid, cudaStream_t st);
 size_t ws_smem_bytes(int D, int K, int wt, int bf16, int slots);

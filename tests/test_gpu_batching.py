@@ -88,9 +88,10 @@ def test_every_tuning_configuration(culsh, name):
     st.search(c["queries"], dataset=c["X"])
     check_search(st, c)
     assert st.profile()["candidates_mode"] == 0
-    for wt, chunk, bps, bf, sl in itertools.product((64, 128, 256), (64, 1024, 4096), (0, 1), (0, 1), (4096, 8192)):
+    for wt, chunk, bps, bf, sl in itertools.product((64, 128, 256), (64, 1024, 4096), (0, 1), (0, 1),
+                                                     (4096, 8192, 16384)):
         st.set_tuning(candidates_mode=1, ws_threads=wt, ws_chunk=chunk, ws_blocks_per_sm=bps, distance_bf16=bf,
-                      ws_set_slots=sl)
+                      ws_set_slots=sl, ws_order=(bps + bf + (sl == 8192) + (wt == 128)) % 2)
         st.search(c["queries"], dataset=c["X"])
         check_search(st, c)
         np.testing.assert_array_equal(st.getKnnDistances(), c["knn_dists"])
@@ -153,7 +154,7 @@ def test_bf16_form_extreme_magnitudes_and_ties(culsh):
 def test_tuning_rejects_out_of_range(culsh):
     st = culsh.SearchTables()
     for bad in ({"probe_batch": 3}, {"proj_tile": 5}, {"ws_threads": 96}, {"ws_chunk": 8}, {"candidates_mode": 2},
-                {"distance_bf16": 2}, {"ws_set_slots": 5000}, {"probe_split": 2}):
+                {"distance_bf16": 2}, {"ws_set_slots": 5000}, {"probe_split": 2}, {"ws_order": 3}):
         with pytest.raises(culsh.CulshError) as ei:
             st.set_tuning(**bad)
         assert ei.value.code == culsh.ERR_INVALID_ARGUMENT
@@ -173,11 +174,11 @@ def test_autotune_keeps_results(culsh):
     st.reset(ht, K, T)
     side = torch.cuda.Stream()
     tune = st.autotune(q.data_ptr(), q.shape[0], ids.data_ptr(), d.data_ptr(), side.cuda_stream)
-    assert tune["configs_tried"] >= 37 and tune["search_ms"] > 0
-    assert tune["ws_set_slots"] in (4096, 8192)
+    assert tune["configs_tried"] >= 90 and tune["search_ms"] > 0
+    assert tune["ws_set_slots"] in (4096, 8192, 16384)
     assert tune["distance_bf16"] in (0, 1)
     assert tune["probe_batch"] in (1, 2, 4) and tune["ws_threads"] in (64, 128, 256)
-    assert tune["probe_split"] in (0, 1)
+    assert tune["probe_split"] in (0, 1) and tune["ws_order"] in (0, 1)
     assert st.get_tuning()["probe_batch"] == tune["probe_batch"]
     torch.cuda.synchronize()
     np.testing.assert_array_equal(ids.cpu().numpy(), c["knn_ids"])
