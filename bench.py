@@ -61,6 +61,8 @@ def parse_args(argv=None):
     p.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per serving rate")
     p.add_argument("--no-recall-point", action="store_true",
                    help="skip the recall@10 >= 0.90 operating point (clustered 1M x 128, W chosen for recall)")
+    p.add_argument("--tuning", default=None,
+                   help="with --recall-point-only: fixed search tuning key=value,... (no tuner, no per-form choice)")
     p.add_argument("--recall-point-only", action="store_true",
                    help="run only the recall operating point and print its JSON (profiling)")
     return p.parse_args(argv)
@@ -320,7 +322,17 @@ def serve_run(culsh, ht, pool, rate, seconds, Ks, Ts, seed, slots=4):
             "peak_device_mb": round(st["peak_device_bytes"] / 2**20, 1), "failed": int(st["failed"]) + len(errors)}
 
 
-def recall_point(culsh, torch, dev, steps, warmup, autotune=True):
+def parse_tuning(spec):
+    """'ws_threads=256,ws_order=1' -> {'ws_threads': 256, 'ws_order': 1}"""
+    out = {}
+    for kv in (spec or "").split(","):
+        if kv.strip():
+            k, v = kv.split("=")
+            out[k.strip()] = int(v)
+    return out
+
+
+def recall_point(culsh, torch, dev, steps, warmup, autotune=True, fixed=None):
     """Search throughput where LSH reaches recall@10 >= 0.90: the Gaussian-
     mixture generator (100 centres ~N(0,10^2), unit noise) at 1M x 128, L=8,
     M=8, T=16, K=10, with W=32 (the named W=4 leaves every held-out query
@@ -347,20 +359,26 @@ def recall_point(culsh, torch, dev, steps, warmup, autotune=True):
     forms = {}
     ref = None
     tuned = None
-    if autotune:   # untimed; the tuner may pick either distance form, both are timed below
+    if autotune and not fixed:   # untimed; the tuner may pick either distance form, both are timed below
         tuned = st.autotune(qt.data_ptr(), Q, ids.data_ptr(), dists.data_ptr(), sp)
+    if fixed:
+        st.set_tuning(**fixed)
+        tuned = st.get_tuning()
     for name, bf in (("fp32", 0), ("bf16_rerank", 1)):
+        if fixed and "distance_bf16" in fixed and fixed["distance_bf16"] != bf:
+            continue
         # each form at its own best set size, partition size and item order
         # (untimed selection among a few; the tuner's choice is one of them)
-        best = None
-        for sl, ch in ((4096, 2048), (8192, 4096), (16384, 8192)):
+        t0 = st.get_tuning()
+        best = (0.0, t0["ws_set_slots"], t0["ws_chunk"], t0["ws_order"])
+        for sl, ch in (() if fixed else ((4096, 2048), (8192, 4096), (16384, 8192))):
             for order in (0, 1):
                 st.set_tuning(candidates_mode=1, distance_bf16=bf, ws_set_slots=sl, ws_chunk=ch, ws_order=order)
                 t = []
                 for _ in range(3):
                     st.search_device(qt.data_ptr(), Q, ids.data_ptr(), dists.data_ptr(), sp)
                     t.append(st.profile()["candidates_ms"])
-                if best is None or statistics.median(t) < best[0]:
+                if best[0] == 0.0 or statistics.median(t) < best[0]:
                     best = (statistics.median(t), sl, ch, order)
         st.set_tuning(candidates_mode=1, distance_bf16=bf, ws_set_slots=best[1], ws_chunk=best[2], ws_order=best[3])
         for _ in range(warmup):
@@ -627,7 +645,8 @@ def main(argv=None):
         dev = torch.device("cuda", 0)
         torch.cuda.set_device(dev)
         print(json.dumps({"recall_point": recall_point(culsh, torch, dev, args.steps, args.warmup,
-                                                       autotune=not args.no_autotune)}), flush=True)
+                                                       autotune=not args.no_autotune,
+                                                       fixed=parse_tuning(args.tuning))}), flush=True)
         return 0
     return run_culsh(args)
 

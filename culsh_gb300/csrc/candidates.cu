@@ -164,7 +164,8 @@ __global__ void k_order_scatter(WsArgs a) {
 }
 
 // WT threads per item: WT / 32 warps each keep a sorted top-K list over a
-// strided share of the item's candidates (tuned: 64, 128 or 256).
+// strided share of the item's candidates (tuned: 64, 128, 256 or 512; wide
+// items keep more row gathers in flight per block of shared memory).
 // W_SLOTS: shared hash-set slots per item (4096, 8192 or 16384, tuned); an
 // item holds at most W_CAP = W_SLOTS / 2 distinct ids. Every item of a query
 // scans the query's whole id list and keeps its partition, so larger sets
@@ -262,6 +263,7 @@ __global__ void __launch_bounds__(WT) k_candidates_ws(WsArgs a) {
                     const uint16_t* rowp = a.xb + (int64_t)id * D;
                     float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
                     if (valid) {
+#pragma unroll 8
                         for (int c = 4 * h; c < D; c += 8) {
                             const uint2 raw = __ldg(reinterpret_cast<const uint2*>(rowp + c));
                             const float x0 = __uint_as_float(raw.x << 16), x1 = __uint_as_float(raw.x & 0xFFFF0000u);
@@ -299,6 +301,7 @@ __global__ void __launch_bounds__(WT) k_candidates_ws(WsArgs a) {
                     const uint16_t* rowp = a.xb + (int64_t)id * D;
                     float sacc = 0.f;
                     if (valid)
+#pragma unroll 4
                         for (int c = r; c < D; c += 8) {
                             const float x = __uint_as_float((uint32_t)__ldg(rowp + c) << 16);
                             const float df = __fsub_rn(qs[c], x);
@@ -620,6 +623,7 @@ cudaError_t launch_ws_w(const WsArgs& a, int grid, cudaStream_t st) {
     switch (a.wt) {
         case 64: return launch_ws_v<64, kBF16, SL>(a, grid, st);
         case 256: return launch_ws_v<256, kBF16, SL>(a, grid, st);
+        case 512: return launch_ws_v<512, kBF16, SL>(a, grid, st);
         default: return launch_ws_v<128, kBF16, SL>(a, grid, st);
     }
 }
@@ -629,6 +633,7 @@ int ws_bps_w(int D, int K, int wt) {
     switch (wt) {
         case 64: return ws_bps_v<64, kBF16, SL>(D, K);
         case 256: return ws_bps_v<256, kBF16, SL>(D, K);
+        case 512: return ws_bps_v<512, kBF16, SL>(D, K);
         default: return ws_bps_v<128, kBF16, SL>(D, K);
     }
 }

@@ -193,7 +193,7 @@ struct SearchTune {
     int proj_tile = 0;     // query projection tiling (launch_project_fp32)
     int probe_pch = 2;     // probes whose hash-group loads overlap (1, 2, 4)
     int cand_ws = 1;       // 1: work-stealing candidate kernel, 0: one block per query
-    int ws_wt = 128;       // threads per work item (64, 128, 256)
+    int ws_wt = 128;       // threads per work item (64, 128, 256, 512)
     int ws_bps = 0;        // resident work-stealing CTAs per SM (0: occupancy limit)
     int ws_chunk = 1024;   // non-unique candidates per id partition
     int dist_bf16 = 0;     // 1: BF16 candidate distances + certified FP32 rerank (work-stealing form)
@@ -1728,7 +1728,8 @@ int culsh_search_set_tuning(culsh_search* s, const culsh_tuning* in) {
     const bool ok = in->proj_tile >= 0 && in->proj_tile <= 2 &&
                     (in->probe_batch == 1 || in->probe_batch == 2 || in->probe_batch == 4) &&
                     (in->candidates_mode == 0 || in->candidates_mode == 1) &&
-                    (in->ws_threads == 64 || in->ws_threads == 128 || in->ws_threads == 256) &&
+                    (in->ws_threads == 64 || in->ws_threads == 128 || in->ws_threads == 256 ||
+                     in->ws_threads == 512) &&
                     in->ws_blocks_per_sm >= 0 && in->ws_blocks_per_sm <= 64 && in->ws_chunk >= 64 &&
                     in->ws_chunk <= 65536 && (in->distance_bf16 == 0 || in->distance_bf16 == 1) &&
                     (in->ws_set_slots == 4096 || in->ws_set_slots == 8192 || in->ws_set_slots == 16384) &&
@@ -1845,12 +1846,12 @@ int culsh_search_autotune(culsh_search* s, const float* d_queries, int Q, int* d
         cands.push_back(t);
         // (set slots, partition size): a partition of `chunk` non-unique
         // candidates always fits a set of 2 * chunk slots
-        const int wts[3] = {64, 128, 256};
+        const int wts[4] = {64, 128, 256, 512};
         const int sets[7][2] = {{4096, 1024}, {4096, 2048}, {8192, 1024}, {8192, 2048},
                                 {8192, 4096}, {16384, 4096}, {16384, 8192}};
         for (int o = 0; o < 2; ++o)
             for (int f = 0; f < 2; ++f)
-                for (int a = 0; a < 3; ++a)
+                for (int a = 0; a < 4; ++a)
                     for (int b = 0; b < 7; ++b) {
                         SearchTune u = best;
                         u.cand_ws = 1;

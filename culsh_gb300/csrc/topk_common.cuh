@@ -102,6 +102,7 @@ __device__ __forceinline__ void fp32_dist_pass(const float* __restrict__ X, int 
             const float* rowp = X + (int64_t)id * D;
             float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
             if (valid && !have) {
+#pragma unroll 8
                 for (int c = 4 * h; c < D; c += 8) {
                     const float4 x = __ldg(reinterpret_cast<const float4*>(rowp + c));
                     const float4 qv = *reinterpret_cast<const float4*>(qs + c);
@@ -130,6 +131,7 @@ __device__ __forceinline__ void fp32_dist_pass(const float* __restrict__ X, int 
             const float* rowp = X + (int64_t)id * D;
             float sacc = 0.f;
             if (valid && !have)
+#pragma unroll 4
                 for (int c = r; c < D; c += 8) {
                     const float df = __fsub_rn(qs[c], __ldg(rowp + c));
                     sacc = __fmaf_rn(df, df, sacc);

@@ -137,7 +137,7 @@ typedef struct culsh_tuning {
     int proj_tile;        /* query projection tiling: 0 (64x128), 1 (32x128), 2 (128x64) */
     int probe_batch;      /* multiprobe hash-group loads in flight per thread: 1, 2, 4   */
     int candidates_mode;  /* 0: one block per query; 1: persistent work-stealing grid   */
-    int ws_threads;       /* work-stealing threads per item: 64, 128, 256               */
+    int ws_threads;       /* work-stealing threads per item: 64, 128, 256, 512          */
     int ws_blocks_per_sm; /* resident work-stealing CTAs per SM, 0 = occupancy limit     */
     int ws_chunk;         /* non-unique candidates per id partition (64 .. 65536)        */
     int distance_bf16;    /* 1: candidate distances from a bf16 copy of the dataset, then

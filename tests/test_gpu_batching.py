@@ -88,7 +88,7 @@ def test_every_tuning_configuration(culsh, name):
     st.search(c["queries"], dataset=c["X"])
     check_search(st, c)
     assert st.profile()["candidates_mode"] == 0
-    for wt, chunk, bps, bf, sl in itertools.product((64, 128, 256), (64, 1024, 4096), (0, 1), (0, 1),
+    for wt, chunk, bps, bf, sl in itertools.product((64, 128, 256, 512), (64, 1024, 4096), (0, 1), (0, 1),
                                                      (4096, 8192, 16384)):
         st.set_tuning(candidates_mode=1, ws_threads=wt, ws_chunk=chunk, ws_blocks_per_sm=bps, distance_bf16=bf,
                       ws_set_slots=sl, ws_order=(bps + bf + (sl == 8192) + (wt == 128)) % 2)
@@ -174,10 +174,10 @@ def test_autotune_keeps_results(culsh):
     st.reset(ht, K, T)
     side = torch.cuda.Stream()
     tune = st.autotune(q.data_ptr(), q.shape[0], ids.data_ptr(), d.data_ptr(), side.cuda_stream)
-    assert tune["configs_tried"] >= 90 and tune["search_ms"] > 0
+    assert tune["configs_tried"] >= 118 and tune["search_ms"] > 0
     assert tune["ws_set_slots"] in (4096, 8192, 16384)
     assert tune["distance_bf16"] in (0, 1)
-    assert tune["probe_batch"] in (1, 2, 4) and tune["ws_threads"] in (64, 128, 256)
+    assert tune["probe_batch"] in (1, 2, 4) and tune["ws_threads"] in (64, 128, 256, 512)
     assert tune["probe_split"] in (0, 1) and tune["ws_order"] in (0, 1)
     assert st.get_tuning()["probe_batch"] == tune["probe_batch"]
     torch.cuda.synchronize()
