@@ -284,26 +284,35 @@ cudaError_t launch_minmax_reduce(const int32_t* pmin, const int32_t* pmax, int n
 }
 
 // Copies n floats from src (16-byte aligned; host memory the device can read,
-// or device memory) to dst with 16-byte loads: one pass over the source.
-__global__ void k_copy_f32(const float* __restrict__ src, float* __restrict__ dst, int64_t n) {
+// or device memory) to dst with 16-byte loads: one pass over the source. Each
+// thread issues kCopyVec independent loads before its stores, so that reads
+// over the host link (microseconds of latency) overlap.
+constexpr int kCopyVec = 8;
+
+__global__ void __launch_bounds__(256) k_copy_f32(const float* __restrict__ src, float* __restrict__ dst, int64_t n) {
     const int64_t n4 = n >> 2;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const float4* s4 = reinterpret_cast<const float4*>(src);
     float4* d4 = reinterpret_cast<float4*>(dst);
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) d4[i] = s4[i];
-    const int64_t tail = (n4 << 2) + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (tail < n) dst[tail] = src[tail];
+    const int64_t base = (int64_t)blockIdx.x * (256 * kCopyVec) + threadIdx.x;
+    float4 v[kCopyVec];
+#pragma unroll
+    for (int k = 0; k < kCopyVec; ++k) {
+        const int64_t i = base + (int64_t)k * 256;
+        if (i < n4) v[k] = s4[i];
+    }
+#pragma unroll
+    for (int k = 0; k < kCopyVec; ++k) {
+        const int64_t i = base + (int64_t)k * 256;
+        if (i < n4) d4[i] = v[k];
+    }
+    if (blockIdx.x == 0 && threadIdx.x < (n & 3)) dst[(n4 << 2) + threadIdx.x] = src[(n4 << 2) + threadIdx.x];
 }
 
 cudaError_t launch_copy_f32(const float* src, float* dst, int64_t n, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     if (((uintptr_t)src & 15) || ((uintptr_t)dst & 15)) return cudaErrorInvalidValue;
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int64_t want = ((n >> 2) + 255) / 256;
-    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)std::max(sms, 1) * 8));
-    k_copy_f32<<<blocks, 256, 0, st>>>(src, dst, n);
+    const int64_t blocks = ((n >> 2) + 256 * kCopyVec - 1) / (256 * kCopyVec);
+    k_copy_f32<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, st>>>(src, dst, n);
     return cudaGetLastError();
 }
 
