@@ -434,10 +434,24 @@ __device__ __noinline__ void order_deltas_heap(const float* dn, uint8_t* enc, in
     }
 }
 
+// Entries kept in the enumeration's candidate list. Picked sums never
+// decrease (an expansion adds a delta, a shift trades a delta for a later,
+// larger one), so a candidate with r candidates before it in pick order
+// (sum, then insertion order) is picked r + 1 steps later at the earliest;
+// once the list holds more than ceil(T/2) + 1, its last one can no longer be
+// among the remaining picks and is dropped (the others keep their order, so
+// ties still go to the earlier candidate). Only for T > 16, where the list
+// sets the shared memory per thread and hence the occupancy.
+__host__ __device__ constexpr int probe_cand_cap(int T) { return T > 16 ? (T + 1) / 2 + 1 : T; }
+// Slots of the list: one more than the cap while capping, for the entry
+// appended before the drop; T otherwise (the list never exceeds T - 1 + 1).
+__host__ __device__ constexpr int probe_cand_slots(int T) { return T > 16 ? probe_cand_cap(T) + 1 : T; }
+
 // Per-thread shared-memory slice of the fast kernel, in bytes per thread.
 template <typename MaskT>
 __host__ __device__ constexpr size_t probe_fast_bytes_per_thread(int M, int T) {
-    return sizeof(MaskT) * (size_t)T + sizeof(float) * (size_t)(M + T) + (size_t)(2 * M + M);
+    return sizeof(MaskT) * (size_t)probe_cand_slots(T) + sizeof(float) * (size_t)(M + probe_cand_slots(T)) +
+           (size_t)(2 * M + M);
 }
 
 // PCH: probes whose group loads are in flight together (tuned: 1, 2 or 4).
@@ -451,15 +465,17 @@ __global__ void __launch_bounds__(PF, kSplit ? 8 : 6) k_probe_fast(ProbeArgs a) 
     const int tid = threadIdx.x;
     const int M2 = 2 * M;
     // Strided per-thread slices (element i of a thread at [i * PF + tid]):
-    // comb[T] (MaskT), dn[M], cd[T] (f32), enc[2M] (sorted delta -> column |
-    // up << 7), ord[M] (u8). Each slice is placed from the block's base; the
-    // thread offset is added last, in units of the slice's own element type.
+    // comb[S] (MaskT), dn[M], cd[S] (f32), enc[2M] (sorted delta -> column
+    // | up << 7), ord[M] (u8), S = probe_cand_slots(T). Each slice is placed
+    // from the block's base; the thread offset is added last, in units of the
+    // slice's own element type.
+    const int CAP = probe_cand_cap(T), SLOTS = probe_cand_slots(T);
     size_t off = 0;
     MaskT* comb = reinterpret_cast<MaskT*>(psm + off) + tid;
-    off += sizeof(MaskT) * (size_t)T * PF;
+    off += sizeof(MaskT) * (size_t)SLOTS * PF;
     float* dn = reinterpret_cast<float*>(psm + off) + tid;
     float* cd = reinterpret_cast<float*>(psm + off) + M * PF + tid;
-    off += sizeof(float) * (size_t)(M + T) * PF;
+    off += sizeof(float) * (size_t)(M + SLOTS) * PF;
     uint8_t* enc = psm + off + tid;
     uint8_t* ord = psm + off + M2 * PF + tid;
     // value of delta i (i < M: down of column i; else up of column i - M,
@@ -572,6 +588,22 @@ __global__ void __launch_bounds__(PF, kSplit ? 8 : 6) k_probe_fast(ProbeArgs a) 
             comb[size * PF] = p1 - ((MaskT)1 << top);
             cd[size * PF] = __fsub_rn(m1, sv(top));
             ++size;
+            if (size > CAP) {   // drop the last candidate in pick order (see probe_cand_cap)
+                float mx = -FLT_MAX;
+                int mj = 0;
+                for (int i = 0; i < size; ++i) {
+                    const float x = cd[i * PF];
+                    if (x >= mx) {
+                        mx = x;
+                        mj = i;
+                    }
+                }
+                for (int i = mj; i + 1 < size; ++i) {
+                    comb[i * PF] = comb[(i + 1) * PF];
+                    cd[i * PF] = cd[(i + 1) * PF];
+                }
+                --size;
+            }
         }
         return probe;
     };

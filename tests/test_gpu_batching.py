@@ -245,3 +245,34 @@ def test_host_search_direct_and_copy_paths(culsh, name, monkeypatch):
             else:
                 assert path == 1
     assert D > 0
+
+
+def test_clustered_queries_every_item_shape_and_order(culsh):
+    """Clustered data where queries of one cluster share most of their
+    candidates (up to ~9,400 non-unique, ~6,300 unique per query): every item
+    width, set size with partition size, locality order and distance form
+    gives the oracle's ids and distances."""
+    import oracle
+    rng = np.random.default_rng(2026)
+    N, D, L, M, W, Q, K, T = 30000, 32, 4, 4, 24.0, 400, 10, 16
+    centers = rng.normal(0, 6, (30, D))
+    X = (centers[rng.integers(0, 30, N)] + rng.normal(0, 1, (N, D))).astype(np.float32)
+    Qm = (centers[rng.integers(0, 30, Q)] + rng.normal(0, 1, (Q, D))).astype(np.float32)
+    A = rng.normal(0, 1, (L, M, D)).astype(np.float32)
+    b = rng.uniform(0, W, (L, M)).astype(np.float32)
+    ref = oracle.search(oracle.build_index(X, A, b, W), X, Qm, K, T)
+    assert int(ref["nonunique"].max()) > 8192
+    ht = culsh.HashTables()
+    ht.reset(N, D, L, M, W, A=A, b=b)
+    ht.index(X)
+    st = culsh.SearchTables()
+    st.reset(ht, K, T)
+    for wt, (sl, ch), order, bf in itertools.product((128, 512), ((4096, 2048), (8192, 4096), (16384, 8192)),
+                                                     (0, 1), (0, 1)):
+        st.set_tuning(candidates_mode=1, ws_threads=wt, ws_set_slots=sl, ws_chunk=ch, ws_order=order,
+                      distance_bf16=bf)
+        st.search(Qm, dataset=X)
+        np.testing.assert_array_equal(st.getKnnIds(), ref["knn_ids"], err_msg=f"{wt} {sl} {ch} {order} {bf}")
+        np.testing.assert_array_equal(st.getKnnDistances(), ref["knn_dists"])
+        assert st.getTotalCandidates_unique() == int(ref["unique"].sum())
+        assert st.profile()["candidates_mode"] == 1

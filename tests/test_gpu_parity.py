@@ -269,7 +269,8 @@ def test_search_split_probe_lookups(culsh, name, monkeypatch):
 
 @pytest.mark.parametrize("split", ["0", "1"])
 @pytest.mark.parametrize("M,T,ties", [(9, 16, False), (12, 16, False), (12, 16, True), (16, 24, False),
-                                       (16, 16, True), (5, 9, True)])
+                                       (16, 16, True), (5, 9, True), (10, 32, False), (16, 64, False),
+                                       (12, 48, True), (16, 40, True)])
 def test_probe_order_register_network(culsh, M, T, ties, split, monkeypatch):
     """For M <= 16 the fast kernel orders the 2M deltas in registers (sorting
     network + merge by counting) and takes the reference's heap procedure
@@ -277,7 +278,8 @@ def test_probe_order_register_network(culsh, M, T, ties, split, monkeypatch):
     and kNN ids match the oracle. The tie cases mix queries with integer
     projections and W = 4 or 8 (downs are multiples of 1/W, so M > W downs
     must tie, and downs of 1/2 tie with ups) with noisy queries whose deltas
-    are all distinct. Both probe forms (fused and split lookups) run."""
+    are all distinct. Both probe forms (fused and split lookups) run. T > 16
+    also exercises the capped candidate list of the enumeration."""
     import oracle
     monkeypatch.setenv("CULSH_PROBE_SPLIT", split)
     rng = np.random.default_rng(100 * M + T)
