@@ -236,6 +236,8 @@ struct culsh_search {
     int host_path = 0;  // last search: 0 device buffers, 1 staged host copies, 2 direct host access
     SearchTune tune;
     bool use_graphs = true;
+    bool stage_events = true;        // record the four stage events (culsh_search_set_profiling)
+    bool last_stage_events = true;   // whether the last search recorded them
     cudaGraphExec_t gexec = nullptr;     // cached search graph and the plan it was captured from
     unsigned char gplan[kPlanBytes] = {};
     int glaunches = 0, graph_mode = 0;
@@ -827,6 +829,7 @@ struct SearchPlan {
     unsigned long long* h_stats;
     unsigned long long* cnu;
     cudaEvent_t ev[4];
+    int stage_events;   // 0: no stage events in the graph (they cost a few microseconds each)
 };
 
 static_assert(sizeof(SearchPlan) <= kPlanBytes, "graph key buffer too small");
@@ -1046,6 +1049,7 @@ int plan_search(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* 
     P.h_stats = s->h_stats.p;
     P.cnu = s->cnu.p;
     for (int i = 0; i < 4; ++i) P.ev[i] = s->ev[i];
+    P.stage_events = s->stage_events ? 1 : 0;
     return CULSH_OK;
 }
 
@@ -1057,12 +1061,12 @@ int enqueue_search(const SearchPlan& P, cudaStream_t st, bool capturing, int* la
     const unsigned int evf = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
     CU_TRY(cudaMemsetAsync(P.cnu, 0, 8 * (size_t)P.Q, st));
     CU_TRY(cudaMemsetAsync(P.stats, 0, 8 * 8, st));
-    CU_TRY(cudaEventRecordWithFlags(P.ev[0], st, evf));
+    if (P.stage_events) CU_TRY(cudaEventRecordWithFlags(P.ev[0], st, evf));
     CU_TRY(launch_project_fp32(P.dQ, P.Q, P.D, P.AT, P.lmp, P.b, P.LM, P.W, nullptr, P.vals, nullptr, nullptr,
                                nullptr, st, P.proj_tile));
-    CU_TRY(cudaEventRecordWithFlags(P.ev[1], st, evf));
+    if (P.stage_events) CU_TRY(cudaEventRecordWithFlags(P.ev[1], st, evf));
     CU_TRY(launch_probe(P.pa, st));
-    CU_TRY(cudaEventRecordWithFlags(P.ev[2], st, evf));
+    if (P.stage_events) CU_TRY(cudaEventRecordWithFlags(P.ev[2], st, evf));
     if (P.use_ws) {
         if (P.wa.order) CU_TRY(launch_order_queries(P.wa, st));
         CU_TRY(launch_plan_items(P.wa, st));
@@ -1071,7 +1075,7 @@ int enqueue_search(const SearchPlan& P, cudaStream_t st, bool capturing, int* la
     } else {
         CU_TRY(launch_candidates(P.ca, st));
     }
-    CU_TRY(cudaEventRecordWithFlags(P.ev[3], st, evf));
+    if (P.stage_events) CU_TRY(cudaEventRecordWithFlags(P.ev[3], st, evf));
     CU_TRY(cudaMemcpyAsync(P.h_stats, P.stats, 8 * 8, cudaMemcpyDeviceToHost, st));
     *launches = (P.use_ws ? (P.use_dense ? 4 : 3) + (P.wa.order ? 3 : 0) : 2) + probe_launches(P.pa);
     return CULSH_OK;
@@ -1216,6 +1220,7 @@ int search_device(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float
     {
         std::lock_guard<std::mutex> lk(alloc_capture_mutex());
         TRY(plan_search(s, dQ, Q, d_ids, d_d, st, &P));
+        s->last_stage_events = P.stage_events != 0;
         s->host_copy_timed = false;
         s->host_path = 0;
         TRY(run_plan(s, P, st));
@@ -1592,13 +1597,15 @@ int culsh_search_run(culsh_search* s, const float* queries, int Q, const float* 
         CU_TRY(cudaMemcpyAsync(s->h_d.p, s->od.p, 4 * (size_t)Q * K, cudaMemcpyDeviceToHost, st));
         s->host_path = 1;
     }
-    CU_TRY(cudaEventRecord(s->ev[4], st));
+    if (s->last_stage_events) CU_TRY(cudaEventRecord(s->ev[4], st));
     CU_TRY(cudaStreamSynchronize(st));
     s->host_copy_timed = true;
     float ms[3] = {0, 0, 0};
-    cudaEventElapsedTime(&ms[0], s->ev[0], s->ev[2]);
-    cudaEventElapsedTime(&ms[1], s->ev[2], s->ev[3]);
-    cudaEventElapsedTime(&ms[2], s->ev[3], s->ev[4]);
+    if (s->last_stage_events) {
+        cudaEventElapsedTime(&ms[0], s->ev[0], s->ev[2]);
+        cudaEventElapsedTime(&ms[1], s->ev[2], s->ev[3]);
+        cudaEventElapsedTime(&ms[2], s->ev[3], s->ev[4]);
+    }
     s->times = culsh_times{ms[0] / 1e3f, 0.f, 0.f, 0.f, ms[1] / 1e3f, ms[2] / 1e3f};
     s->Q = Q;
     s->searched = true;
@@ -1754,6 +1761,12 @@ int culsh_search_set_graphs(culsh_search* s, int enabled) {
     return CULSH_OK;
 }
 
+int culsh_search_set_profiling(culsh_search* s, int stage_times) {
+    if (!s) return fail(CULSH_ERR_INVALID_ARGUMENT, "null search");
+    s->stage_events = stage_times != 0;
+    return CULSH_OK;
+}
+
 // Coordinate search: the projection tiling by its stage time, the probe form
 // by its stage time, then the candidate stage over its kernel form, item
 // width, set size and partition size, distance form and locality order
@@ -1768,6 +1781,13 @@ int culsh_search_autotune(culsh_search* s, const float* d_queries, int Q, int* d
     s->searched = false;
     s->qb_host_valid = false;
     TRY(ensure_device(s->ix, st));
+    // the tuner times stages: stage events on while it runs, as before after
+    struct EventsOn {
+        culsh_search* s;
+        bool was;
+        ~EventsOn() { s->stage_events = was; }
+    } events_on{s, s->stage_events};
+    s->stage_events = true;
     const size_t nout = (size_t)Q * s->K;
     std::vector<int> ref_ids(nout), got_ids(nout);
     std::vector<float> ref_d(nout), got_d(nout);
@@ -1944,10 +1964,13 @@ int culsh_search_profile_get(culsh_search* s, culsh_search_profile* out) {
     if (!s || !out) return fail(CULSH_ERR_INVALID_ARGUMENT, "null argument");
     *out = culsh_search_profile{};
     if (!s->ev[0] || s->Q <= 0) return fail(CULSH_ERR_STATE, "no search has run");
-    CU_TRY(cudaEventSynchronize(s->ev[3]));
-    CU_TRY(cudaEventElapsedTime(&out->project_ms, s->ev[0], s->ev[1]));
-    CU_TRY(cudaEventElapsedTime(&out->probe_ms, s->ev[1], s->ev[2]));
-    CU_TRY(cudaEventElapsedTime(&out->candidates_ms, s->ev[2], s->ev[3]));
+    out->stage_times = s->last_stage_events ? 1 : 0;
+    if (s->last_stage_events) {
+        CU_TRY(cudaEventSynchronize(s->ev[3]));
+        CU_TRY(cudaEventElapsedTime(&out->project_ms, s->ev[0], s->ev[1]));
+        CU_TRY(cudaEventElapsedTime(&out->probe_ms, s->ev[1], s->ev[2]));
+        CU_TRY(cudaEventElapsedTime(&out->candidates_ms, s->ev[2], s->ev[3]));
+    }
     out->launches = s->launches;
     out->deferred_queries = s->deferred_queries;
     out->key_words = s->ix ? s->ix->KW : 0;

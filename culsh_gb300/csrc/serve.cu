@@ -381,6 +381,7 @@ int culsh_server_create(culsh_server** out, culsh_index* ix, const culsh_server_
             return culsh::set_last_error(CULSH_ERR_CUDA, "serving: slot creation failed");
         }
         culsh_search_set_graphs(sl->s, v->graphs);
+        culsh_search_set_profiling(sl->s, 0);   // latency is measured per request on the host
         v->slots.push_back(std::move(sl));
     }
     culsh_server* p = v.release();

@@ -162,6 +162,12 @@ int culsh_search_autotune(culsh_search* s, const float* d_queries, int Q, int* d
 int culsh_search_get_tuning(culsh_search* s, culsh_tuning* out);
 int culsh_search_set_tuning(culsh_search* s, const culsh_tuning* in);   /* CULSH_ERR_INVALID_ARGUMENT when out of range */
 int culsh_search_set_graphs(culsh_search* s, int enabled);               /* default 1 */
+/* Stage timing (default 1): four events in each search (the per-stage times
+ * of culsh_search_profile_get and culsh_search_get_times). Each costs a few
+ * microseconds of device time in the graph; 0 leaves them out, and the stage
+ * times then read 0 (profile.stage_times = 0). The autotuner turns them on
+ * while it runs. */
+int culsh_search_set_profiling(culsh_search* s, int stage_times);
 
 /* Device memory of a search object (no counterpart in the reference; the
  * serving loop's admission uses them). device_bytes: bytes its buffers hold
@@ -204,6 +210,8 @@ typedef struct culsh_search_profile {
                             2: host buffers read and written by the kernels
                             directly (device with pageable memory access,
                             16-byte aligned queries)                          */
+    int stage_times;     /* 1: the stage times above were measured; 0: stage
+                            events off (culsh_search_set_profiling)          */
 } culsh_search_profile;
 int culsh_search_profile_get(culsh_search* s, culsh_search_profile* out);
 

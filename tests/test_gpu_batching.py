@@ -276,3 +276,29 @@ def test_clustered_queries_every_item_shape_and_order(culsh):
         np.testing.assert_array_equal(st.getKnnDistances(), ref["knn_dists"])
         assert st.getTotalCandidates_unique() == int(ref["unique"].sum())
         assert st.profile()["candidates_mode"] == 1
+
+
+@pytest.mark.parametrize("graphs", [True, False])
+def test_stage_events_off(culsh, graphs):
+    """Without stage events the search returns the same results; the profile
+    says its stage times were not measured, and the reference-style times are
+    zero; with events back on, stage times are measured again."""
+    c = load_case("heavy")
+    ht = build_index(culsh, c)
+    st = culsh.SearchTables()
+    st.reset(ht, int(c["K"]), int(c["T"]))
+    st.set_graphs(graphs)
+    st.set_profiling(False)
+    for _ in range(2):
+        st.search(c["queries"], dataset=c["X"])
+        check_search(st, c)
+        np.testing.assert_array_equal(st.getKnnDistances(), c["knn_dists"])
+        pr = st.profile()
+        assert pr["stage_times"] == 0 and pr["project_ms"] == 0 and pr["candidates_ms"] == 0
+        assert pr["launches"] >= 4
+        assert st.getTimes()["distances"] == 0
+    st.set_profiling(True)
+    st.search(c["queries"], dataset=c["X"])
+    check_search(st, c)
+    pr = st.profile()
+    assert pr["stage_times"] == 1 and pr["probe_ms"] > 0
