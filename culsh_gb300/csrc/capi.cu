@@ -1059,11 +1059,14 @@ int plan_search(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* 
 // events); outside one they are ordinary records.
 int enqueue_search(const SearchPlan& P, cudaStream_t st, bool capturing, int* launches) {
     const unsigned int evf = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
-    CU_TRY(cudaMemsetAsync(P.cnu, 0, 8 * (size_t)P.Q, st));
-    CU_TRY(cudaMemsetAsync(P.stats, 0, 8 * 8, st));
     if (P.stage_events) CU_TRY(cudaEventRecordWithFlags(P.ev[0], st, evf));
+    ZeroWords zw;   // the projection kernel clears the non-unique counts and the statistics
+    zw.a = P.cnu;
+    zw.na = P.Q;
+    zw.b = P.stats;
+    zw.nb = 8;
     CU_TRY(launch_project_fp32(P.dQ, P.Q, P.D, P.AT, P.lmp, P.b, P.LM, P.W, nullptr, P.vals, nullptr, nullptr,
-                               nullptr, st, P.proj_tile));
+                               nullptr, st, P.proj_tile, zw));
     if (P.stage_events) CU_TRY(cudaEventRecordWithFlags(P.ev[1], st, evf));
     CU_TRY(launch_probe(P.pa, st));
     if (P.stage_events) CU_TRY(cudaEventRecordWithFlags(P.ev[2], st, evf));

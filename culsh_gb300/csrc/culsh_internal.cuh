@@ -134,11 +134,28 @@ struct LookupView {
 // codes != nullptr: floored codes [LM][n_pts] + per-block min/max partials
 // [grid_x][LM]; vals != nullptr: unfloored values [LM][n_pts].
 // tile picks the query-value tiling (0: 64x128, 1: 32x128, 2: 128x64 points x columns).
+// Word arrays a kernel zeroes on the way (grid-stride, every block takes
+// part): the search's first kernel clears the counters the later ones
+// accumulate into, instead of two memset nodes in the graph.
+struct ZeroWords {
+    unsigned long long* a = nullptr;
+    int64_t na = 0;
+    unsigned long long* b = nullptr;
+    int64_t nb = 0;
+    __device__ __forceinline__ void clear(int tid) const {
+        if (!na && !nb) return;
+        const int64_t nthreads = (int64_t)gridDim.x * gridDim.y * blockDim.x;
+        const int64_t g = ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * blockDim.x + tid;
+        for (int64_t i = g; i < na; i += nthreads) a[i] = 0ull;
+        for (int64_t i = g; i < nb; i += nthreads) b[i] = 0ull;
+    }
+};
+
 // AT: the projection matrix transposed, D rows of lmp floats (lmp = LM rounded
 // up to a multiple of 4, columns past LM zero, 16-byte aligned).
 cudaError_t launch_project_fp32(const float* X, int64_t n_pts, int D, const float* AT, int lmp, const float* b,
                                 int LM, float W, int32_t* codes, float* vals, int32_t* pmin, int32_t* pmax, int* err,
-                                cudaStream_t st, int tile = 0);
+                                cudaStream_t st, int tile = 0, ZeroWords zw = ZeroWords{});
 int project_grid_x(int64_t n_pts);
 // n floats, 16-byte aligned source and destination (src may be host memory
 // the device reads directly).

@@ -39,7 +39,8 @@ __global__ void __launch_bounds__(NT) k_project(const float* __restrict__ X, int
                                                 const float* __restrict__ AT, int lmp, const float* __restrict__ b,
                                                 int LM, float W, int32_t* __restrict__ codes,
                                                 float* __restrict__ vals, int32_t* __restrict__ pmin,
-                                                int32_t* __restrict__ pmax, int* __restrict__ err) {
+                                                int32_t* __restrict__ pmax, int* __restrict__ err,
+                                                ZeroWords zw) {
     constexpr int BN = 16 * PT;
     constexpr int BC = 16 * CT;
     constexpr int XP = BN + 2;   // padded X row: the transposing stores conflict at most 4 ways
@@ -56,6 +57,7 @@ __global__ void __launch_bounds__(NT) k_project(const float* __restrict__ X, int
     uint32_t (*Cs)[BN + 1] = reinterpret_cast<uint32_t (*)[BN + 1]>(smem);
 
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    zw.clear(tid);
     const int64_t n0 = (int64_t)blockIdx.x * BN;
     const int c0 = blockIdx.y * BC;
     const bool vec = (D & 3) == 0;
@@ -258,21 +260,21 @@ int project_grid_x(int64_t n_pts) { return (int)((n_pts + 127) / 128); }
 
 cudaError_t launch_project_fp32(const float* X, int64_t n_pts, int D, const float* AT, int lmp, const float* b,
                                 int LM, float W, int32_t* codes, float* vals, int32_t* pmin, int32_t* pmax, int* err,
-                                cudaStream_t st, int tile) {
+                                cudaStream_t st, int tile, ZeroWords zw) {
     if (n_pts <= 0) return cudaSuccess;
     if (lmp < LM || (lmp & 3) || ((uintptr_t)AT & 15)) return cudaErrorInvalidValue;
     if (codes) {
         k_project<true, 8, 4, 16><<<dim3(project_grid_x(n_pts), (LM + 63) / 64), NT, 0, st>>>(
-            X, n_pts, D, AT, lmp, b, LM, W, codes, nullptr, pmin, pmax, err);
+            X, n_pts, D, AT, lmp, b, LM, W, codes, nullptr, pmin, pmax, err, zw);
     } else if (tile == 1) {
         k_project<false, 2, 8, 64><<<dim3((unsigned)((n_pts + 31) / 32), (LM + 127) / 128), NT, 0, st>>>(
-            X, n_pts, D, AT, lmp, b, LM, W, nullptr, vals, nullptr, nullptr, err);
+            X, n_pts, D, AT, lmp, b, LM, W, nullptr, vals, nullptr, nullptr, err, zw);
     } else if (tile == 2) {
         k_project<false, 8, 4, 32><<<dim3((unsigned)((n_pts + 127) / 128), (LM + 63) / 64), NT, 0, st>>>(
-            X, n_pts, D, AT, lmp, b, LM, W, nullptr, vals, nullptr, nullptr, err);
+            X, n_pts, D, AT, lmp, b, LM, W, nullptr, vals, nullptr, nullptr, err, zw);
     } else {
         k_project<false, 4, 8, 32><<<dim3((unsigned)((n_pts + 63) / 64), (LM + 127) / 128), NT, 0, st>>>(
-            X, n_pts, D, AT, lmp, b, LM, W, nullptr, vals, nullptr, nullptr, err);
+            X, n_pts, D, AT, lmp, b, LM, W, nullptr, vals, nullptr, nullptr, err, zw);
     }
     return cudaGetLastError();
 }
