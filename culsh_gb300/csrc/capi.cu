@@ -1735,7 +1735,7 @@ int culsh_search_get_tuning(culsh_search* s, culsh_tuning* out) {
 
 int culsh_search_set_tuning(culsh_search* s, const culsh_tuning* in) {
     if (!s || !in) return fail(CULSH_ERR_INVALID_ARGUMENT, "null argument");
-    const bool ok = in->proj_tile >= 0 && in->proj_tile <= 2 &&
+    const bool ok = in->proj_tile >= 0 && in->proj_tile <= 4 &&
                     (in->probe_batch == 1 || in->probe_batch == 2 || in->probe_batch == 4) &&
                     (in->candidates_mode == 0 || in->candidates_mode == 1) &&
                     (in->ws_threads == 64 || in->ws_threads == 128 || in->ws_threads == 256 ||
@@ -1830,7 +1830,7 @@ int culsh_search_autotune(culsh_search* s, const float* d_queries, int Q, int* d
     float stage[4];
     float best_t = 0;
     // projection tiling
-    for (int tile = 0; tile <= 2; ++tile) {
+    for (int tile = 0; tile <= 4; ++tile) {
         s->tune = best;
         s->tune.proj_tile = tile;
         const int rc = measure(stage);

@@ -24,9 +24,9 @@ constexpr int NT = 256;   // threads: 16 (points) x 16 (columns), each PT x CT o
 
 // Block tile BN = 16*PT points x BC = 16*CT columns, BK dimensions per
 // shared-memory stage. Index builds use PT = 8, CT = 4, BK = 16; query batches
-// use PT = 4, CT = 8, BK = 32 by default (fewer barriers and shared-memory
-// loads per FMA, enough blocks for ten thousand queries), PT = 2 for small
-// batches or PT = 8, CT = 4, BK = 32 for large ones, as the search tuner picks.
+// take one of five tilings the search tuner picks (PT x CT = 4x8 by default,
+// 2x8, 8x4, 4x4, 2x4: fewer shared-memory loads per FMA against more blocks
+// in flight).
 //
 // Thread (tx, ty) owns points 32*(i/2) + 2*tx + (i%2), i < PT, so that a
 // half-warp's float2 reads of the X tile cover 128 contiguous bytes (no bank
@@ -271,6 +271,12 @@ cudaError_t launch_project_fp32(const float* X, int64_t n_pts, int D, const floa
             X, n_pts, D, AT, lmp, b, LM, W, nullptr, vals, nullptr, nullptr, err, zw);
     } else if (tile == 2) {
         k_project<false, 8, 4, 32><<<dim3((unsigned)((n_pts + 127) / 128), (LM + 63) / 64), NT, 0, st>>>(
+            X, n_pts, D, AT, lmp, b, LM, W, nullptr, vals, nullptr, nullptr, err, zw);
+    } else if (tile == 3) {
+        k_project<false, 4, 4, 32><<<dim3((unsigned)((n_pts + 63) / 64), (LM + 63) / 64), NT, 0, st>>>(
+            X, n_pts, D, AT, lmp, b, LM, W, nullptr, vals, nullptr, nullptr, err, zw);
+    } else if (tile == 4) {
+        k_project<false, 2, 4, 32><<<dim3((unsigned)((n_pts + 31) / 32), (LM + 63) / 64), NT, 0, st>>>(
             X, n_pts, D, AT, lmp, b, LM, W, nullptr, vals, nullptr, nullptr, err, zw);
     } else {
         k_project<false, 4, 8, 32><<<dim3((unsigned)((n_pts + 63) / 64), (LM + 127) / 128), NT, 0, st>>>(

@@ -134,7 +134,8 @@ int culsh_search_run_device(culsh_search* s, const float* d_queries, int Q, int*
  * otherwise); graphs are used on any stream but the legacy default stream
  * and never inside a caller's own capture. */
 typedef struct culsh_tuning {
-    int proj_tile;        /* query projection tiling: 0 (64x128), 1 (32x128), 2 (128x64) */
+    int proj_tile;        /* query projection tiling (points x columns per block): 0 (64x128),
+                             1 (32x128), 2 (128x64), 3 (64x64), 4 (32x64)               */
     int probe_batch;      /* multiprobe hash-group loads in flight per thread: 1, 2, 4   */
     int candidates_mode;  /* 0: one block per query; 1: persistent work-stealing grid   */
     int ws_threads;       /* work-stealing threads per item: 64, 128, 256, 512          */

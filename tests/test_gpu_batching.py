@@ -76,7 +76,7 @@ def test_every_tuning_configuration(culsh, name):
     st = culsh.SearchTables()
     st.reset(ht, int(c["K"]), int(c["T"]))
     M = c["A"].shape[1]
-    for tile, pch in itertools.product((0, 1, 2), (1, 2, 4)):
+    for tile, pch in itertools.product((0, 1, 2, 3, 4), (1, 2, 4)):
         launches = []
         for split in (0, 1):
             st.set_tuning(proj_tile=tile, probe_batch=pch, probe_split=split)
@@ -174,7 +174,7 @@ def test_autotune_keeps_results(culsh):
     st.reset(ht, K, T)
     side = torch.cuda.Stream()
     tune = st.autotune(q.data_ptr(), q.shape[0], ids.data_ptr(), d.data_ptr(), side.cuda_stream)
-    assert tune["configs_tried"] >= 118 and tune["search_ms"] > 0
+    assert tune["configs_tried"] >= 120 and tune["search_ms"] > 0
     assert tune["ws_set_slots"] in (4096, 8192, 16384)
     assert tune["distance_bf16"] in (0, 1)
     assert tune["probe_batch"] in (1, 2, 4) and tune["ws_threads"] in (64, 128, 256, 512)
