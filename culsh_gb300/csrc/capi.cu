@@ -198,7 +198,7 @@ struct SearchTune {
     int ws_chunk = 1024;   // non-unique candidates per id partition
     int dist_bf16 = 0;     // 1: BF16 candidate distances + certified FP32 rerank (work-stealing form)
     int ws_slots = 4096;   // shared hash-set slots per work item (4096, 8192 or 16384)
-    int probe_split = 0;   // 1: enumeration kernel, then one lookup thread per probe (M <= 16)
+    int probe_split = 0;   // M <= 16: 1 enumeration kernel + lookup kernel; 2 lookups at the enumeration's end
     int ws_order = 0;      // 1: plan queries in the locality order of their home bucket (work-stealing form)
 };
 constexpr size_t kPlanBytes = 1024;   // room for the graph key (checked below)
@@ -882,15 +882,17 @@ int plan_search(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* 
     {
         // CULSH_PROBE_SPLIT=0/1 overrides the tuning (the tests run both).
         const char* e = getenv("CULSH_PROBE_SPLIT");
-        const bool split = (e ? atoi(e) != 0 : tu.probe_split != 0) && M <= 16;
-        if (split) {
+        const int form = M <= 16 ? std::min(2, std::max(0, e ? atoi(e) : tu.probe_split)) : 0;
+        if (form > 0) {
             CU_TRY(s->ph.reserve((size_t)L * Q * T));
             CU_TRY(s->pmask.reserve((size_t)L * Q * T));
-            CU_TRY(s->pctx.reserve(3 * (size_t)L * Q));
-            P.pa.split = 1;
+            P.pa.split = form;
             P.pa.ph = s->ph.p;
             P.pa.pmask = s->pmask.p;
-            P.pa.pctx = s->pctx.p;
+            if (form == 1) {
+                CU_TRY(s->pctx.reserve(3 * (size_t)L * Q));
+                P.pa.pctx = s->pctx.p;
+            }
         }
     }
     CandArgs& ca = P.ca;
@@ -1743,7 +1745,7 @@ int culsh_search_set_tuning(culsh_search* s, const culsh_tuning* in) {
                     in->ws_blocks_per_sm >= 0 && in->ws_blocks_per_sm <= 64 && in->ws_chunk >= 64 &&
                     in->ws_chunk <= 65536 && (in->distance_bf16 == 0 || in->distance_bf16 == 1) &&
                     (in->ws_set_slots == 4096 || in->ws_set_slots == 8192 || in->ws_set_slots == 16384) &&
-                    (in->probe_split == 0 || in->probe_split == 1) && (in->ws_order == 0 || in->ws_order == 1);
+                    in->probe_split >= 0 && in->probe_split <= 2 && (in->ws_order == 0 || in->ws_order == 1);
     if (!ok) return fail(CULSH_ERR_INVALID_ARGUMENT, "tuning value out of range");
     s->tune.proj_tile = in->proj_tile;
     s->tune.probe_pch = in->probe_batch;
@@ -1843,13 +1845,14 @@ int culsh_search_autotune(culsh_search* s, const float* d_queries, int Q, int* d
             best.proj_tile = tile;
         }
     }
-    // probe form: fused with batch depth 1, 2 or 4, or split lookups (M <= 16)
-    const int pchs[4] = {1, 2, 4, 0};
-    const int nforms = s->ix->M <= 16 ? 4 : 3;
+    // probe form: fused with batch depth 1, 2 or 4, or (M <= 16) split
+    // lookups, or lookups at the end of the enumeration
+    const int pchs[5] = {1, 2, 4, 0, -1};
+    const int nforms = s->ix->M <= 16 ? 5 : 3;
     for (int i = 0; i < nforms; ++i) {
         s->tune = best;
-        s->tune.probe_split = pchs[i] == 0;
-        if (pchs[i]) s->tune.probe_pch = pchs[i];
+        s->tune.probe_split = pchs[i] == 0 ? 1 : pchs[i] < 0 ? 2 : 0;
+        if (pchs[i] > 0) s->tune.probe_pch = pchs[i];
         const int rc = measure(stage);
         if (rc != CULSH_OK) {
             s->tune = start;
@@ -1857,8 +1860,8 @@ int culsh_search_autotune(culsh_search* s, const float* d_queries, int Q, int* d
         }
         if (i == 0 || stage[1] < best_t) {
             best_t = stage[1];
-            best.probe_split = pchs[i] == 0;
-            if (pchs[i]) best.probe_pch = pchs[i];
+            best.probe_split = s->tune.probe_split;
+            if (pchs[i] > 0) best.probe_pch = pchs[i];
         }
     }
     // candidate stage

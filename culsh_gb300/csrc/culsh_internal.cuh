@@ -257,9 +257,11 @@ struct ProbeArgs {
     unsigned long long* cnu;   // [Q] non-unique candidate counts (accumulated)
     int small_codes;           // every |cmin|, |cmax| < 2^24 - 2 (set by the host)
     int pch;                   // fast kernel: probes whose group loads overlap (1, 2, 4)
-    // Split lookups (M <= 16, fast kernel): the enumeration kernel stores each
-    // valid probe's finished hash and mask and marks its query bucket -2;
-    // one thread per probe then checks the key filter and walks the hash.
+    // Split lookups (M <= 16, fast kernel). split = 1: the enumeration kernel
+    // stores each valid probe's finished hash and mask and marks its query
+    // bucket -2; k_probe_resolve then checks the key filter and walks the
+    // hash. split = 2: the enumeration kernel stores them and looks its
+    // pair's probes up itself, behind the filter, at its end.
     int split;
     unsigned long long* ph;    // [L][T][Q] finished hash of each pending probe
     uint32_t* pmask;           // [L][T][Q] its mask over the sorted deltas

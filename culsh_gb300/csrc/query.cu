@@ -457,8 +457,11 @@ __host__ __device__ constexpr size_t probe_fast_bytes_per_thread(int M, int T) {
 // PCH: probes whose group loads are in flight together (tuned: 1, 2 or 4).
 // MM > 0: M <= MM, deltas ordered in registers (order_deltas_net); MM = 0:
 // ranking and merge over the shared-memory slice.
-template <typename MaskT, int PCH, int MM, bool kSplit>
-__global__ void __launch_bounds__(PF, kSplit ? 8 : 6) k_probe_fast(ProbeArgs a) {
+// kForm: 0 fused (enumeration with batched lookups), 1 split (enumeration
+// only; k_probe_resolve looks up), 2 tail (enumerate every probe, then look
+// them all up behind the key filter at the end of the same kernel).
+template <typename MaskT, int PCH, int MM, int kForm>
+__global__ void __launch_bounds__(PF, kForm > 0 ? 8 : 6) k_probe_fast(ProbeArgs a) {
     extern __shared__ __align__(16) unsigned char psm[];
     const LookupView& lv = a.lv;
     const int Q = a.Q, T = a.T, L = lv.L, M = lv.M, KW = lv.KW;
@@ -607,25 +610,32 @@ __global__ void __launch_bounds__(PF, kSplit ? 8 : 6) k_probe_fast(ProbeArgs a) 
         }
         return probe;
     };
-    if constexpr (kSplit) {
-        // Pair context for the lookup kernel: home key and sorted deltas.
-        uint32_t ew[8];
+    if constexpr (kForm > 0) {
+        if constexpr (kForm == 1) {
+            // Pair context for the lookup kernel: home key and sorted deltas.
+            uint32_t ew[8];
 #pragma unroll
-        for (int w = 0; w < 8; ++w) ew[w] = 0;
-        if (T > 1) {
+            for (int w = 0; w < 8; ++w) ew[w] = 0;
+            if (T > 1) {
 #pragma unroll
-            for (int i = 0; i < 32; ++i)
-                if (i < M2) ew[i >> 2] |= (uint32_t)enc[i * PF] << (8 * (i & 3));
+                for (int i = 0; i < 32; ++i)
+                    if (i < M2) ew[i >> 2] |= (uint32_t)enc[i * PF] << (8 * (i & 3));
+            }
+            uint4* cx = a.pctx + idx * 3;
+            cx[0] = make_uint4((uint32_t)c.hkey, (uint32_t)(c.hkey >> 32), (uint32_t)(c.hkey >> 64),
+                               (uint32_t)(c.hkey >> 96));
+            cx[1] = make_uint4(ew[0], ew[1], ew[2], ew[3]);
+            cx[2] = make_uint4(ew[4], ew[5], ew[6], ew[7]);
         }
-        uint4* cx = a.pctx + idx * 3;
-        cx[0] = make_uint4((uint32_t)c.hkey, (uint32_t)(c.hkey >> 32), (uint32_t)(c.hkey >> 64),
-                           (uint32_t)(c.hkey >> 96));
-        cx[1] = make_uint4(ew[0], ew[1], ew[2], ew[3]);
-        cx[2] = make_uint4(ew[4], ew[5], ew[6], ew[7]);
         // Hash and mask of probe t at [l][t][q] (a warp's stores coalesce);
-        // the query buckets are staged four at a time for 16-byte stores.
+        // split form: the query buckets are staged four at a time for
+        // 16-byte stores; tail form: the probe's filter word is prefetched
+        // into L2 for the lookups at the end.
         const int64_t base = (int64_t)l * T * Q + q;
         const bool vec = (T & 3) == 0;
+        const uint32_t* filt = lv.filt ? lv.filt + __ldg(lv.fl_off + l) : nullptr;
+        const uint32_t fmask = lv.filt ? __ldg(lv.fl_mask + l) : 0u;
+        uint64_t vmask = 0;   // tail form: probes whose key is in range
         int s0 = -1, s1 = -1, s2 = -1, s3 = -1;
         for (int t = 0; t < T; ++t) {
             const MaskT probe = t > 0 ? next_probe() : (MaskT)0;
@@ -634,18 +644,93 @@ __global__ void __launch_bounds__(PF, kSplit ? 8 : 6) k_probe_fast(ProbeArgs a) 
             if (ok) {
                 a.ph[base + (int64_t)t * Q] = hh;
                 a.pmask[base + (int64_t)t * Q] = (uint32_t)probe;
+                if constexpr (kForm == 2) {
+                    vmask |= 1ull << t;
+                    if (filt) asm volatile("prefetch.global.L2 [%0];" ::"l"(filt + (filter_mix(hh) & fmask)));
+                }
             }
-            const int v = ok ? -2 : -1;
-            if (vec) {
-                const int r = t & 3;
-                s0 = r == 0 ? v : s0;
-                s1 = r == 1 ? v : s1;
-                s2 = r == 2 ? v : s2;
-                s3 = r == 3 ? v : s3;
-                if (r == 3) *reinterpret_cast<int4*>(qb + t - 3) = make_int4(s0, s1, s2, s3);
-            } else {
-                qb[t] = v;
+            if constexpr (kForm == 1) {
+                const int v = ok ? -2 : -1;
+                if (vec) {
+                    const int r = t & 3;
+                    s0 = r == 0 ? v : s0;
+                    s1 = r == 1 ? v : s1;
+                    s2 = r == 2 ? v : s2;
+                    s3 = r == 3 ? v : s3;
+                    if (r == 3) *reinterpret_cast<int4*>(qb + t - 3) = make_int4(s0, s1, s2, s3);
+                } else {
+                    qb[t] = v;
+                }
             }
+        }
+        if constexpr (kForm == 2) {
+            // Lookups, eight probes at a time: every filter word in flight
+            // together; the few probes the filter passes walk their hash
+            // group and verify the key (the pair's context is still here).
+            const uint32_t gmask = __ldg(lv.hmask + l);
+            const unsigned long long* slots = lv.hslots + __ldg(lv.hoff + l);
+            const uint64_t bo = __ldg(lv.boff + l);
+            unsigned long long cnu = 0;
+            for (int t0 = 0; t0 < T; t0 += 8) {
+                uint32_t fw[8], need[8];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    const int t = t0 + k;
+                    need[k] = 1u;
+                    fw[k] = 0u;
+                    if (t < T && ((vmask >> t) & 1)) {
+                        const uint32_t fx = filter_mix(a.ph[base + (int64_t)t * Q]);
+                        need[k] = filter_bits(fx);
+                        fw[k] = filt ? __ldg(filt + (fx & fmask)) : ~0u;
+                    }
+                }
+                uint32_t pass = 0;
+#pragma unroll
+                for (int k = 0; k < 8; ++k) pass |= (uint32_t)((fw[k] & need[k]) == need[k]) << k;
+#pragma unroll
+                for (int c4 = 0; c4 < 8; c4 += 4) {
+                    if (t0 + c4 >= T) break;
+                    if (vec) {
+                        *reinterpret_cast<int4*>(qb + t0 + c4) = make_int4(-1, -1, -1, -1);
+                    } else {
+                        for (int k = c4; k < c4 + 4 && t0 + k < T; ++k) qb[t0 + k] = -1;
+                    }
+                }
+#pragma unroll 1
+                for (; pass; pass &= pass - 1) {
+                    const int t = t0 + lowest_bit(pass);
+                    const uint64_t hh = a.ph[base + (int64_t)t * Q];
+                    const MaskT pm = (MaskT)a.pmask[base + (int64_t)t * Q];
+                    const uint32_t fp = slot_fp(hh);
+                    uint32_t h = (uint32_t)hh & gmask;
+                    int32_t res = -1;
+                    bool done = false;
+                    for (uint32_t p = 0; p <= gmask && !done; ++p) {
+                        const unsigned long long* grp = slots + (uint64_t)h * kGroupWords;
+                        const unsigned long long w = __ldg(grp);
+                        for (int e = 0; e < kGroupSlots && !done; ++e) {
+                            const uint32_t f = (uint32_t)(w >> (16 * e)) & 0xFFFFu;
+                            if (f == kEmptyFp) {
+                                done = true;
+                            } else if (f == fp) {
+                                const uint32_t bj = __ldg(reinterpret_cast<const uint32_t*>(grp + 1) + e);
+                                u128 k;
+                                probe_key(c, pm, k);
+                                if (key_matches(lv.ukeys + (bo + bj) * KW, k, KW)) {
+                                    res = (int32_t)bj;
+                                    done = true;
+                                }
+                            }
+                        }
+                        h = (h + 1) & gmask;
+                    }
+                    if (res >= 0) {
+                        qb[t] = res;
+                        cnu += __ldg(lv.sizes + bo + res);
+                    }
+                }
+            }
+            if (cnu) atomicAdd(a.cnu + q, cnu);
         }
         return;
     }
@@ -849,15 +934,15 @@ __global__ void __launch_bounds__(256, 5) k_probe_resolve(const __grid_constant_
     if (added) atomicAdd(a.cnu + q, added);
 }
 
-template <typename MaskT, int PCH, int MM, bool kSplit>
+template <typename MaskT, int PCH, int MM, int kForm>
 cudaError_t launch_probe_fast_v(const ProbeArgs& a, cudaStream_t st) {
     const size_t smem = (size_t)PF * probe_fast_bytes_per_thread<MaskT>(a.lv.M, a.T);
     static std::atomic<size_t> cap{0};   // dynamic shared memory this kernel is opted into
-    const cudaError_t e = opt_in_smem(k_probe_fast<MaskT, PCH, MM, kSplit>, smem, cap);
+    const cudaError_t e = opt_in_smem(k_probe_fast<MaskT, PCH, MM, kForm>, smem, cap);
     if (e != cudaSuccess) return e;
     const int64_t n = (int64_t)a.lv.L * a.Q;
-    k_probe_fast<MaskT, PCH, MM, kSplit><<<(unsigned)((n + PF - 1) / PF), PF, smem, st>>>(a);
-    if (kSplit) {
+    k_probe_fast<MaskT, PCH, MM, kForm><<<(unsigned)((n + PF - 1) / PF), PF, smem, st>>>(a);
+    if (kForm == 1) {
         const int64_t threads = n * ((a.T + kResolveSlots - 1) / kResolveSlots);
         k_probe_resolve<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(a);
     }
@@ -867,12 +952,13 @@ cudaError_t launch_probe_fast_v(const ProbeArgs& a, cudaStream_t st) {
 template <typename MaskT, int MM>
 cudaError_t launch_probe_fast_t(const ProbeArgs& a, cudaStream_t st) {
     if constexpr (sizeof(MaskT) == 4) {
-        if (a.split) return launch_probe_fast_v<MaskT, 1, MM, true>(a, st);
+        if (a.split == 2) return launch_probe_fast_v<MaskT, 1, MM, 2>(a, st);
+        if (a.split) return launch_probe_fast_v<MaskT, 1, MM, 1>(a, st);
     }
     switch (a.pch) {
-        case 1: return launch_probe_fast_v<MaskT, 1, MM, false>(a, st);
-        case 4: return launch_probe_fast_v<MaskT, 4, MM, false>(a, st);
-        default: return launch_probe_fast_v<MaskT, 2, MM, false>(a, st);
+        case 1: return launch_probe_fast_v<MaskT, 1, MM, 0>(a, st);
+        case 4: return launch_probe_fast_v<MaskT, 4, MM, 0>(a, st);
+        default: return launch_probe_fast_v<MaskT, 2, MM, 0>(a, st);
     }
 }
 
@@ -1056,7 +1142,7 @@ static bool probe_fast_eligible(const ProbeArgs& a) {
 
 int probe_launches(const ProbeArgs& a) {
     if ((int64_t)a.lv.L * a.Q <= 0) return 0;
-    return probe_fast_eligible(a) && a.split && a.lv.M <= 16 ? 2 : 1;
+    return probe_fast_eligible(a) && a.split == 1 && a.lv.M <= 16 ? 2 : 1;
 }
 
 cudaError_t launch_probe(const ProbeArgs& a, cudaStream_t st) {

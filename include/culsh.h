@@ -147,8 +147,10 @@ typedef struct culsh_tuning {
     int ws_set_slots;     /* work-stealing shared hash set per item: 4096, 8192 or 16384 slots */
     float search_ms;      /* culsh_search_autotune: median device ms of the choice       */
     int configs_tried;    /* culsh_search_autotune: configurations timed                 */
-    int probe_split;      /* 1 (M <= 16): enumerate every probe first, then look each up
-                             in its own thread behind a key filter (same results as 0) */
+    int probe_split;      /* M <= 16: 1 enumerate every probe first, then look each up in
+                             its own thread behind a key filter; 2 look a pair's probes
+                             up behind the filter at the end of its enumeration
+                             (same results as 0)                                        */
     int ws_order;         /* 1: work-stealing items planned in the locality order of the
                              queries' home buckets, so queries that share candidates run
                              together and share rows in L2 (same results as 0)         */

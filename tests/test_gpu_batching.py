@@ -78,12 +78,13 @@ def test_every_tuning_configuration(culsh, name):
     M = c["A"].shape[1]
     for tile, pch in itertools.product((0, 1, 2, 3, 4), (1, 2, 4)):
         launches = []
-        for split in (0, 1):
+        for split in (0, 1, 2):
             st.set_tuning(proj_tile=tile, probe_batch=pch, probe_split=split)
             st.search(c["queries"], dataset=c["X"])
             check_search(st, c)
             launches.append(st.profile()["launches"])
         assert launches[1] == launches[0] + (M <= 16)   # the split form's lookup kernel
+        assert launches[2] == launches[0]               # the tail form looks up in the same kernel
     st.set_tuning(proj_tile=0, probe_batch=2, probe_split=0, candidates_mode=0)
     st.search(c["queries"], dataset=c["X"])
     check_search(st, c)
@@ -154,7 +155,7 @@ def test_bf16_form_extreme_magnitudes_and_ties(culsh):
 def test_tuning_rejects_out_of_range(culsh):
     st = culsh.SearchTables()
     for bad in ({"probe_batch": 3}, {"proj_tile": 5}, {"ws_threads": 96}, {"ws_chunk": 8}, {"candidates_mode": 2},
-                {"distance_bf16": 2}, {"ws_set_slots": 5000}, {"probe_split": 2}, {"ws_order": 3}):
+                {"distance_bf16": 2}, {"ws_set_slots": 5000}, {"probe_split": 3}, {"ws_order": 3}):
         with pytest.raises(culsh.CulshError) as ei:
             st.set_tuning(**bad)
         assert ei.value.code == culsh.ERR_INVALID_ARGUMENT
@@ -178,7 +179,7 @@ def test_autotune_keeps_results(culsh):
     assert tune["ws_set_slots"] in (4096, 8192, 16384)
     assert tune["distance_bf16"] in (0, 1)
     assert tune["probe_batch"] in (1, 2, 4) and tune["ws_threads"] in (64, 128, 256, 512)
-    assert tune["probe_split"] in (0, 1) and tune["ws_order"] in (0, 1)
+    assert tune["probe_split"] in (0, 1, 2) and tune["ws_order"] in (0, 1)
     assert st.get_tuning()["probe_batch"] == tune["probe_batch"]
     torch.cuda.synchronize()
     np.testing.assert_array_equal(ids.cpu().numpy(), c["knn_ids"])

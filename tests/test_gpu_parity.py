@@ -252,12 +252,14 @@ def test_search_general_probe_kernel(culsh, name, monkeypatch):
     check_search(st, c)
 
 
+@pytest.mark.parametrize("form", ["1", "2"])
 @pytest.mark.parametrize("name", golden_cases())
-def test_search_split_probe_lookups(culsh, name, monkeypatch):
-    """Split lookups (every probe enumerated first, then one lookup thread per
-    probe behind the key filter) give exactly the fused kernel's results:
-    query buckets, non-unique counts, ids and distances."""
-    monkeypatch.setenv("CULSH_PROBE_SPLIT", "1")
+def test_search_split_probe_lookups(culsh, name, form, monkeypatch):
+    """Split lookups (every probe enumerated first, then looked up behind the
+    key filter: one thread per probe in a second kernel, or the pair's own
+    thread at the end of its enumeration) give exactly the fused kernel's
+    results: query buckets, non-unique counts, ids and distances."""
+    monkeypatch.setenv("CULSH_PROBE_SPLIT", form)
     c = load_case(name)
     ht = build_index(culsh, c)
     st = culsh.SearchTables()
@@ -267,7 +269,7 @@ def test_search_split_probe_lookups(culsh, name, monkeypatch):
     np.testing.assert_array_equal(st.getKnnDistances(), c["knn_dists"])
 
 
-@pytest.mark.parametrize("split", ["0", "1"])
+@pytest.mark.parametrize("split", ["0", "1", "2"])
 @pytest.mark.parametrize("M,T,ties", [(9, 16, False), (12, 16, False), (12, 16, True), (16, 24, False),
                                        (16, 16, True), (5, 9, True), (10, 32, False), (16, 64, False),
                                        (12, 48, True), (16, 40, True)])
@@ -278,7 +280,7 @@ def test_probe_order_register_network(culsh, M, T, ties, split, monkeypatch):
     and kNN ids match the oracle. The tie cases mix queries with integer
     projections and W = 4 or 8 (downs are multiples of 1/W, so M > W downs
     must tie, and downs of 1/2 tie with ups) with noisy queries whose deltas
-    are all distinct. Both probe forms (fused and split lookups) run. T > 16
+    are all distinct. Every probe form (fused, split, tail lookups) runs. T > 16
     also exercises the capped candidate list of the enumeration."""
     import oracle
     monkeypatch.setenv("CULSH_PROBE_SPLIT", split)
