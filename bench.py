@@ -557,12 +557,14 @@ def run_culsh(args):
     kernel_name = {"project": "k_project", "probe": "k_probe", "candidates": "k_candidates"}[dom]
     kernel_label = kernel_name
     if dom == "probe":
-        # the probe stage is one fused kernel or, in the split form (M <= 16),
-        # the enumeration kernel plus the lookup kernel
+        # the probe stage is one fused kernel or (M <= 16) the enumeration
+        # kernel plus the lookup kernel (split form), or one kernel that looks
+        # its probes up at the end (tail form)
         env = os.environ.get("CULSH_PROBE_SPLIT")
-        split = (env != "0" if env is not None else bool(st.get_tuning().get("probe_split", 0))) and M <= 16
-        kernel_name = "k_probe_split" if split else "k_probe_fused"
-        kernel_label = "k_probe_fast (enumeration) + k_probe_resolve" if split else "k_probe_fast"
+        form = (int(env) if env is not None else int(st.get_tuning().get("probe_split", 0))) if M <= 16 else 0
+        kernel_name = {1: "k_probe_split", 2: "k_probe_tail"}.get(form, "k_probe_fused")
+        kernel_label = {1: "k_probe_fast (enumeration) + k_probe_resolve",
+                        2: "k_probe_fast (enumeration + lookups at its end)"}.get(form, "k_probe_fast")
     roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 5), "traffic": ncu_traffic(kernel_name, name),
                 "kernel": kernel_label, "algorithmic_bytes": sb[dom], "peak_source": f"{peak_kind} hbm_gbs",
