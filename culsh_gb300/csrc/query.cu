@@ -635,7 +635,12 @@ __global__ void __launch_bounds__(PF, kForm > 0 ? 8 : 6) k_probe_fast(ProbeArgs 
         const bool vec = (T & 3) == 0;
         const uint32_t* filt = lv.filt ? lv.filt + __ldg(lv.fl_off + l) : nullptr;
         const uint32_t fmask = lv.filt ? __ldg(lv.fl_mask + l) : 0u;
-        uint64_t vmask = 0;   // tail form: probes whose key is in range
+        // Tail form: the filter word of probe t is loaded as the probe is
+        // made and checked one probe later (the next enumeration step hides
+        // its latency); `pass` collects the probes the filter lets through.
+        uint64_t pass = 0;
+        uint32_t pfw = 0u, pneed = 1u;
+        int pt = -1;
         int s0 = -1, s1 = -1, s2 = -1, s3 = -1;
         for (int t = 0; t < T; ++t) {
             const MaskT probe = t > 0 ? next_probe() : (MaskT)0;
@@ -644,9 +649,15 @@ __global__ void __launch_bounds__(PF, kForm > 0 ? 8 : 6) k_probe_fast(ProbeArgs 
             if (ok) {
                 a.ph[base + (int64_t)t * Q] = hh;
                 a.pmask[base + (int64_t)t * Q] = (uint32_t)probe;
-                if constexpr (kForm == 2) {
-                    vmask |= 1ull << t;
-                    if (filt) asm volatile("prefetch.global.L2 [%0];" ::"l"(filt + (filter_mix(hh) & fmask)));
+            }
+            if constexpr (kForm == 2) {
+                if (pt >= 0 && (pfw & pneed) == pneed) pass |= 1ull << pt;
+                pt = -1;
+                if (ok) {
+                    const uint32_t fx = filter_mix(hh);
+                    pneed = filter_bits(fx);
+                    pfw = filt ? __ldg(filt + (fx & fmask)) : ~0u;
+                    pt = t;
                 }
             }
             if constexpr (kForm == 1) {
@@ -664,70 +675,51 @@ __global__ void __launch_bounds__(PF, kForm > 0 ? 8 : 6) k_probe_fast(ProbeArgs 
             }
         }
         if constexpr (kForm == 2) {
-            // Lookups, eight probes at a time: every filter word in flight
-            // together; the few probes the filter passes walk their hash
-            // group and verify the key (the pair's context is still here).
+            if (pt >= 0 && (pfw & pneed) == pneed) pass |= 1ull << pt;
+            // Every probe a miss, then the few the filter passed: walk the
+            // hash group, verify the key (the pair's context is still here).
+            for (int t4 = 0; t4 < T; t4 += 4) {
+                if (vec) {
+                    *reinterpret_cast<int4*>(qb + t4) = make_int4(-1, -1, -1, -1);
+                } else {
+                    for (int k = t4; k < t4 + 4 && k < T; ++k) qb[k] = -1;
+                }
+            }
             const uint32_t gmask = __ldg(lv.hmask + l);
             const unsigned long long* slots = lv.hslots + __ldg(lv.hoff + l);
             const uint64_t bo = __ldg(lv.boff + l);
             unsigned long long cnu = 0;
-            for (int t0 = 0; t0 < T; t0 += 8) {
-                uint32_t fw[8], need[8];
-#pragma unroll
-                for (int k = 0; k < 8; ++k) {
-                    const int t = t0 + k;
-                    need[k] = 1u;
-                    fw[k] = 0u;
-                    if (t < T && ((vmask >> t) & 1)) {
-                        const uint32_t fx = filter_mix(a.ph[base + (int64_t)t * Q]);
-                        need[k] = filter_bits(fx);
-                        fw[k] = filt ? __ldg(filt + (fx & fmask)) : ~0u;
-                    }
-                }
-                uint32_t pass = 0;
-#pragma unroll
-                for (int k = 0; k < 8; ++k) pass |= (uint32_t)((fw[k] & need[k]) == need[k]) << k;
-#pragma unroll
-                for (int c4 = 0; c4 < 8; c4 += 4) {
-                    if (t0 + c4 >= T) break;
-                    if (vec) {
-                        *reinterpret_cast<int4*>(qb + t0 + c4) = make_int4(-1, -1, -1, -1);
-                    } else {
-                        for (int k = c4; k < c4 + 4 && t0 + k < T; ++k) qb[t0 + k] = -1;
-                    }
-                }
 #pragma unroll 1
-                for (; pass; pass &= pass - 1) {
-                    const int t = t0 + lowest_bit(pass);
-                    const uint64_t hh = a.ph[base + (int64_t)t * Q];
-                    const MaskT pm = (MaskT)a.pmask[base + (int64_t)t * Q];
-                    const uint32_t fp = slot_fp(hh);
-                    uint32_t h = (uint32_t)hh & gmask;
-                    int32_t res = -1;
-                    bool done = false;
-                    for (uint32_t p = 0; p <= gmask && !done; ++p) {
-                        const unsigned long long* grp = slots + (uint64_t)h * kGroupWords;
-                        const unsigned long long w = __ldg(grp);
-                        for (int e = 0; e < kGroupSlots && !done; ++e) {
-                            const uint32_t f = (uint32_t)(w >> (16 * e)) & 0xFFFFu;
-                            if (f == kEmptyFp) {
+            for (; pass; pass &= pass - 1) {
+                const int t = __ffsll((long long)pass) - 1;
+                const uint64_t hh = a.ph[base + (int64_t)t * Q];
+                const MaskT pm = (MaskT)a.pmask[base + (int64_t)t * Q];
+                const uint32_t fp = slot_fp(hh);
+                uint32_t h = (uint32_t)hh & gmask;
+                int32_t res = -1;
+                bool done = false;
+                for (uint32_t p = 0; p <= gmask && !done; ++p) {
+                    const unsigned long long* grp = slots + (uint64_t)h * kGroupWords;
+                    const unsigned long long w = __ldg(grp);
+                    for (int e = 0; e < kGroupSlots && !done; ++e) {
+                        const uint32_t f = (uint32_t)(w >> (16 * e)) & 0xFFFFu;
+                        if (f == kEmptyFp) {
+                            done = true;
+                        } else if (f == fp) {
+                            const uint32_t bj = __ldg(reinterpret_cast<const uint32_t*>(grp + 1) + e);
+                            u128 k;
+                            probe_key(c, pm, k);
+                            if (key_matches(lv.ukeys + (bo + bj) * KW, k, KW)) {
+                                res = (int32_t)bj;
                                 done = true;
-                            } else if (f == fp) {
-                                const uint32_t bj = __ldg(reinterpret_cast<const uint32_t*>(grp + 1) + e);
-                                u128 k;
-                                probe_key(c, pm, k);
-                                if (key_matches(lv.ukeys + (bo + bj) * KW, k, KW)) {
-                                    res = (int32_t)bj;
-                                    done = true;
-                                }
                             }
                         }
-                        h = (h + 1) & gmask;
                     }
-                    if (res >= 0) {
-                        qb[t] = res;
-                        cnu += __ldg(lv.sizes + bo + res);
-                    }
+                    h = (h + 1) & gmask;
+                }
+                if (res >= 0) {
+                    qb[t] = res;
+                    cnu += __ldg(lv.sizes + bo + res);
                 }
             }
             if (cnu) atomicAdd(a.cnu + q, cnu);
