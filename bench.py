@@ -176,7 +176,9 @@ def ncu_traffic(kernel: str, workload: str):
 
 
 # ---------------------------------------------------------------------------
-# algorithmic bytes per stage (one launch over Q queries); see the design doc
+# algorithmic bytes per stage (one launch over Q queries): what each stage must
+# read and write at least (hash groups, candidate rows, outputs), not what the
+# kernels move
 
 def stage_bytes(cfg, Q, K, T, KW, hits, nonunique, unique):
     L, M, D = cfg["L"], cfg["M"], cfg["D"]
