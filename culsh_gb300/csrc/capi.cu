@@ -823,7 +823,7 @@ struct SearchPlan {
     ProbeArgs pa;
     int probe_generic;
     int use_ws, ws_grid, use_dense, dense_grid;
-    CandArgs ca{};
+    CandArgs ca;
     WsArgs wa;
     unsigned long long* stats;
     unsigned long long* h_stats;
