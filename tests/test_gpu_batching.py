@@ -303,3 +303,32 @@ def test_stage_events_off(culsh, graphs):
     check_search(st, c)
     pr = st.profile()
     assert pr["stage_times"] == 1 and pr["probe_ms"] > 0
+
+
+def test_wide_items_large_k_and_single_query(culsh):
+    """Edge shapes for the wide work-stealing options: a K whose per-warp
+    lists cannot fit a 512-thread item beside a 16,384-slot set (the search
+    falls back to the per-query kernel), a single query with the locality
+    order, and T not a multiple of four in the tail probe form."""
+    import oracle
+    c = load_case("heavy")
+    ht = build_index(culsh, c)
+    X, Qm = c["X"], c["queries"]
+    L, M, D = c["A"].shape
+    idx = oracle.build_index(X, c["A"], c["b"], float(c["W"]))
+    st = culsh.SearchTables()
+    K, T = 1500, int(c["T"])
+    ref = oracle.search(idx, X, Qm, K, T)
+    st.reset(ht, K, T)
+    st.set_tuning(candidates_mode=1, ws_threads=512, ws_set_slots=16384, ws_chunk=8192, ws_order=1)
+    st.search(Qm, dataset=X)
+    np.testing.assert_array_equal(st.getKnnIds(), ref["knn_ids"])
+    np.testing.assert_array_equal(st.getKnnDistances(), ref["knn_dists"])
+    assert st.profile()["candidates_mode"] == 0   # item state too large: per-query kernel
+    K = int(c["K"])
+    ref1 = oracle.search(idx, X, Qm[:1], K, 7)
+    st.reset(ht, K, 7)
+    st.set_tuning(ws_threads=512, ws_set_slots=16384, ws_chunk=8192, ws_order=1, probe_split=2)
+    st.search(Qm[:1], dataset=X)
+    np.testing.assert_array_equal(st.getKnnIds(), ref1["knn_ids"])
+    np.testing.assert_array_equal(st.getQueryBuckets(0), ref1["qbuckets"][0].reshape(1, 7))
