@@ -253,20 +253,26 @@ __device__ __forceinline__ bool probe_key(const FastProbeCtx& c, MaskT mask, u12
 }
 
 // Lookup hash of a probe mask (the home hash +- the multiplier of every
-// perturbed column); returns false when a column leaves [cmin, cmax].
+// perturbed column, accumulated in the same walk over the mask: a column
+// perturbed both up and down adds +R - R = 0 mod 2^64, as it keeps its home
+// code); returns false when a column leaves [cmin, cmax].
 template <typename MaskT>
 __device__ __forceinline__ bool probe_hash(const FastProbeCtx& c, MaskT mask, uint64_t& hh) {
     uint32_t up = 0, dn = 0;
+    uint64_t h = c.h0;
     for (MaskT b = mask; b; b &= b - 1) {
         const int e = c.enc[lowest_bit(b) * PF];
-        if (e & 0x80) up |= 1u << (e & 0x3f);
-        else dn |= 1u << (e & 0x3f);
+        const uint64_t r = __ldg(c.rmul + (e & 0x3f));
+        if (e & 0x80) {
+            up |= 1u << (e & 0x3f);
+            h += r;
+        } else {
+            dn |= 1u << (e & 0x3f);
+            h -= r;
+        }
     }
     const uint32_t nu = up & ~dn, nd = dn & ~up;
     if ((~(nu | nd) & c.allM & ~c.ok0) | (nu & ~c.okUp) | (nd & ~c.okDn)) return false;
-    uint64_t h = c.h0;
-    for (uint32_t b = nu; b; b &= b - 1) h += __ldg(c.rmul + lowest_bit(b));
-    for (uint32_t b = nd; b; b &= b - 1) h -= __ldg(c.rmul + lowest_bit(b));
     hh = hash_finish(h);
     return true;
 }
