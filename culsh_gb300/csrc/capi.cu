@@ -233,12 +233,16 @@ struct culsh_search {
     int occ_val = 1;
     long long rechecked = 0;   // BF16 form: candidates re-read in FP32 by the last search
     int dense_queries = 0;     // queries of the last search that took the bitmap kernel
-    int host_path = 0;  // last search: 0 device buffers, 1 staged host copies, 2 direct host access
+    int host_path = 0;  // last search: 0 device buffers, 1 staged host copies, 2 direct host access,
+                        // 3 direct host access with the copy fused into the projection
     SearchTune tune;
     bool use_graphs = true;
     bool stage_events = true;        // record the four stage events (culsh_search_set_profiling)
     bool last_stage_events = true;   // whether the last search recorded them
     cudaGraphExec_t gexec = nullptr;     // cached search graph and the plan it was captured from
+    cudaGraph_t graph = nullptr;         // the captured graph (its projection node is updated in place)
+    cudaGraphNode_t gproj = nullptr;     // projection node of the fused host-copy form, if found
+    const float* gsrc = nullptr;         // host query rows the instantiated projection node reads
     unsigned char gplan[kPlanBytes] = {};
     int glaunches = 0, graph_mode = 0;
     PinBuf<int32_t> h_ids, h_qb;
@@ -248,6 +252,7 @@ struct culsh_search {
 
     ~culsh_search() {
         if (gexec) cudaGraphExecDestroy(gexec);
+        if (graph) cudaGraphDestroy(graph);
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
         if (stream) cudaStreamDestroy(stream);
@@ -817,6 +822,7 @@ struct SearchPlan {
     const float* dQ;
     int Q, D, LM, proj_tile, lmp;
     float W;
+    float* xcopy;   // fused host-copy form: dQ is the caller's host rows, copied here on the way
     const float* AT;
     const float* b;
     float* vals;
@@ -837,7 +843,7 @@ static_assert(sizeof(SearchPlan) <= kPlanBytes, "graph key buffer too small");
 // Sizes every buffer of a search of Q queries and fills the plan. Allocates
 // (when buffers grow) but launches nothing.
 int plan_search(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* d_d, cudaStream_t st,
-                SearchPlan* out) {
+                SearchPlan* out, const float* proj_src = nullptr) {
     culsh_index* ix = s->ix;
     const int L = ix->L, M = ix->M, D = ix->D, K = s->K, T = s->T, LM = L * M;
     const float* dX = ix->dev_x();
@@ -865,6 +871,13 @@ int plan_search(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* 
     P.D = D;
     P.LM = LM;
     P.proj_tile = tu.proj_tile;
+    if (proj_src) {
+        // The projection reads the caller's rows (host memory the device can
+        // access) and writes them to dQ, which the candidate stage reads.
+        P.dQ = proj_src;
+        P.xcopy = const_cast<float*>(dQ);
+        P.proj_tile = 5;
+    }
     P.W = ix->W;
     P.AT = ix->dAT.p;
     P.lmp = ix->lmp;
@@ -1068,7 +1081,7 @@ int enqueue_search(const SearchPlan& P, cudaStream_t st, bool capturing, int* la
     zw.b = P.stats;
     zw.nb = 8;
     CU_TRY(launch_project_fp32(P.dQ, P.Q, P.D, P.AT, P.lmp, P.b, P.LM, P.W, nullptr, P.vals, nullptr, nullptr,
-                               nullptr, st, P.proj_tile, zw));
+                               nullptr, st, P.proj_tile, zw, P.xcopy));
     if (P.stage_events) CU_TRY(cudaEventRecordWithFlags(P.ev[1], st, evf));
     CU_TRY(launch_probe(P.pa, st));
     if (P.stage_events) CU_TRY(cudaEventRecordWithFlags(P.ev[2], st, evf));
@@ -1086,6 +1099,15 @@ int enqueue_search(const SearchPlan& P, cudaStream_t st, bool capturing, int* la
     return CULSH_OK;
 }
 
+void drop_graph(culsh_search* s) {
+    if (s->gexec) cudaGraphExecDestroy(s->gexec);
+    if (s->graph) cudaGraphDestroy(s->graph);
+    s->gexec = nullptr;
+    s->graph = nullptr;
+    s->gproj = nullptr;
+    s->gsrc = nullptr;
+}
+
 // CULSH_NO_GRAPH (or culsh_search_set_graphs(s, 0)) runs the launches
 // directly instead of through the cached graph.
 bool graphs_enabled(const culsh_search* s, cudaStream_t st) {
@@ -1095,23 +1117,71 @@ bool graphs_enabled(const culsh_search* s, cudaStream_t st) {
     return true;
 }
 
+// The kernel node of g that launches fn, or null.
+cudaGraphNode_t find_kernel_node(cudaGraph_t g, const void* fn) {
+    size_t n = 0;
+    if (cudaGraphGetNodes(g, nullptr, &n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (cudaGraphGetNodes(g, nodes.data(), &n) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    for (size_t i = 0; i < n; ++i) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nodes[i], &t) != cudaSuccess || t != cudaGraphNodeTypeKernel) continue;
+        cudaKernelNodeParams kp;
+        if (cudaGraphKernelNodeGetParams(nodes[i], &kp) == cudaSuccess && kp.func == fn) return nodes[i];
+    }
+    cudaGetLastError();
+    return nullptr;
+}
+
+// Points the instantiated projection node of the fused host-copy form at
+// other host rows (later launches of the graph only). False when the node
+// cannot be updated: the caller then captures the graph again.
+bool set_projection_source(culsh_search* s, const float* src) {
+    if (!s->gproj) return false;
+    cudaKernelNodeParams kp;
+    if (cudaGraphKernelNodeGetParams(s->gproj, &kp) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    void* args[kProjectArgs];
+    for (int i = 0; i < kProjectArgs; ++i) args[i] = kp.kernelParams[i];
+    const float* x = src;
+    args[0] = &x;
+    kp.kernelParams = args;
+    kp.extra = nullptr;
+    if (cudaGraphExecKernelNodeSetParams(s->gexec, s->gproj, &kp) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    s->gsrc = src;
+    return true;
+}
+
 // Runs the plan: replays the cached graph when the plan is unchanged,
-// re-captures it otherwise, or launches directly when graphs are off.
+// re-captures it otherwise, or launches directly when graphs are off. In the
+// fused host-copy form the caller's rows are not part of the key: a replay
+// over other rows updates the projection node in place.
 int run_plan(culsh_search* s, const SearchPlan& P, cudaStream_t st) {
     if (!graphs_enabled(s, st)) {
         s->graph_mode = 0;
         return enqueue_search(P, st, false, &s->launches);
     }
-    if (s->gexec && std::memcmp(&P, &s->gplan, sizeof(P)) == 0) {
+    SearchPlan key = P;
+    if (P.xcopy) key.dQ = nullptr;
+    if (s->gexec && std::memcmp(&key, &s->gplan, sizeof(key)) == 0 &&
+        (!P.xcopy || P.dQ == s->gsrc || set_projection_source(s, P.dQ))) {
         CU_TRY(cudaGraphLaunch(s->gexec, st));
         s->launches = s->glaunches;
         s->graph_mode = 2;
         return CULSH_OK;
     }
-    if (s->gexec) {
-        cudaGraphExecDestroy(s->gexec);
-        s->gexec = nullptr;
-    }
+    drop_graph(s);
     CU_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
     int launches = 0;
     const int rc = enqueue_search(P, st, true, &launches);
@@ -1123,12 +1193,15 @@ int run_plan(culsh_search* s, const SearchPlan& P, cudaStream_t st) {
     }
     if (ec != cudaSuccess) return fail(CULSH_ERR_DEVICE, "search graph capture: %s", cudaGetErrorString(ec));
     const cudaError_t ei = cudaGraphInstantiate(&s->gexec, g, 0);
-    cudaGraphDestroy(g);
     if (ei != cudaSuccess) {
+        cudaGraphDestroy(g);
         s->gexec = nullptr;
         return fail(CULSH_ERR_DEVICE, "search graph instantiation: %s", cudaGetErrorString(ei));
     }
-    std::memcpy(&s->gplan, &P, sizeof(P));
+    s->graph = g;
+    s->gproj = P.xcopy ? find_kernel_node(g, project_copy_kernel()) : nullptr;
+    s->gsrc = P.dQ;
+    std::memcpy(&s->gplan, &key, sizeof(key));
     s->glaunches = launches;
     CU_TRY(cudaGraphLaunch(s->gexec, st));
     s->launches = launches;
@@ -1220,11 +1293,12 @@ int finish_search(culsh_search* s, const SearchPlan& P, cudaStream_t st) {
 // (which may grow buffers) and graph capture hold the process-wide lock, so
 // that searches on other threads (the serving loop's slots) never free device
 // memory during a capture; launches and the wait for results do not.
-int search_device(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* d_d, cudaStream_t st) {
+int search_device(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* d_d, cudaStream_t st,
+                  const float* proj_src = nullptr) {
     SearchPlan P;
     {
         std::lock_guard<std::mutex> lk(alloc_capture_mutex());
-        TRY(plan_search(s, dQ, Q, d_ids, d_d, st, &P));
+        TRY(plan_search(s, dQ, Q, d_ids, d_d, st, &P, proj_src));
         s->last_stage_events = P.stage_events != 0;
         s->host_copy_timed = false;
         s->host_path = 0;
@@ -1583,15 +1657,21 @@ int culsh_search_run(culsh_search* s, const float* queries, int Q, const float* 
     CU_TRY(s->h_d.reserve((size_t)Q * K));
     if (dbg) fprintf(dbg, "[SearchTables::search]\tPerforming searching. (Q, K, T) = (%d, %d, %d)\n", Q, K, s->T);
     if (direct_host_access() && ((uintptr_t)queries & 15u) == 0) {
-        // One kernel reads the caller's (pageable) queries through the host
-        // page tables into the device query buffer (one pass, 16-byte loads,
-        // hence the alignment condition), and the search writes its results
-        // into the pinned result buffers: no staging copies, and the graph
-        // key does not depend on the caller's buffer.
+        // The kernels read the caller's (pageable) queries through the host
+        // page tables (16-byte loads, hence the alignment condition) and the
+        // search writes its results into the pinned result buffers: no
+        // staging copies. With L*M <= 192 the projection reads the rows
+        // itself and writes them to the device query buffer on the way, for
+        // the candidate stage; otherwise a copy kernel does that first.
         CU_TRY(s->dq.reserve((size_t)Q * D));
-        CU_TRY(launch_copy_f32(queries, s->dq.p, (int64_t)Q * D, st));
-        TRY(search_device(s, s->dq.p, Q, s->h_ids.p, s->h_d.p, st));
-        s->host_path = 2;
+        if (ix->L * ix->M <= 192 && getenv("CULSH_NO_FUSED_COPY") == nullptr) {
+            TRY(search_device(s, s->dq.p, Q, s->h_ids.p, s->h_d.p, st, queries));
+            s->host_path = 3;
+        } else {
+            CU_TRY(launch_copy_f32(queries, s->dq.p, (int64_t)Q * D, st));
+            TRY(search_device(s, s->dq.p, Q, s->h_ids.p, s->h_d.p, st));
+            s->host_path = 2;
+        }
     } else {
         CU_TRY(s->dq.reserve((size_t)Q * D));
         CU_TRY(s->oids.reserve((size_t)Q * K));
@@ -1681,10 +1761,7 @@ long long culsh_search_estimate_bytes(const culsh_index* ix, int Q, int K, int T
 int culsh_search_release(culsh_search* s) {
     if (!s) return fail(CULSH_ERR_INVALID_ARGUMENT, "null search");
     std::lock_guard<std::mutex> lk(alloc_capture_mutex());
-    if (s->gexec) {
-        cudaGraphExecDestroy(s->gexec);
-        s->gexec = nullptr;
-    }
+    drop_graph(s);
     s->dq.release();
     s->vals.release();
     s->od.release();

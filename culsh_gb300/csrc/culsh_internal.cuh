@@ -155,8 +155,12 @@ struct ZeroWords {
 // up to a multiple of 4, columns past LM zero, 16-byte aligned).
 cudaError_t launch_project_fp32(const float* X, int64_t n_pts, int D, const float* AT, int lmp, const float* b,
                                 int LM, float W, int32_t* codes, float* vals, int32_t* pmin, int32_t* pmax, int* err,
-                                cudaStream_t st, int tile = 0, ZeroWords zw = ZeroWords{});
+                                cudaStream_t st, int tile = 0, ZeroWords zw = ZeroWords{}, float* xcopy = nullptr);
 int project_grid_x(int64_t n_pts);
+// The kernel of tiling 5 (xcopy form), for finding its node in a captured
+// graph, and its number of parameters (the first is the rows it reads).
+const void* project_copy_kernel();
+constexpr int kProjectArgs = 15;
 // n floats, 16-byte aligned source and destination (src may be host memory
 // the device reads directly).
 cudaError_t launch_copy_f32(const float* src, float* dst, int64_t n, cudaStream_t st);

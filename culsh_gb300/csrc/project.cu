@@ -26,7 +26,9 @@ constexpr int NT = 256;   // threads: 16 (points) x 16 (columns), each PT x CT o
 // shared-memory stage. Index builds use PT = 8, CT = 4, BK = 16; query batches
 // take one of five tilings the search tuner picks (PT x CT = 4x8 by default,
 // 2x8, 8x4, 4x4, 2x4: fewer shared-memory loads per FMA against more blocks
-// in flight).
+// in flight), and 2x12 (all of L*M <= 192 columns in one block) when the
+// queries are read straight from host memory and copied to the device on
+// the way (xcopy).
 //
 // Thread (tx, ty) owns points 32*(i/2) + 2*tx + (i%2), i < PT, so that a
 // half-warp's float2 reads of the X tile cover 128 contiguous bytes (no bank
@@ -34,13 +36,13 @@ constexpr int NT = 256;   // threads: 16 (points) x 16 (columns), each PT x CT o
 // transposed (AT[d][c], rows of lmp >= LM floats, columns past LM zero) with
 // coalesced float4 loads. The next stage's tiles are loaded into registers
 // while the current one is multiplied.
-template <bool kCodes, int PT, int CT, int BK>
-__global__ void __launch_bounds__(NT) k_project(const float* __restrict__ X, int64_t n_pts, int D,
+template <bool kCodes, int PT, int CT, int BK, bool kCopy = false>
+__global__ void __launch_bounds__(NT, kCopy ? 2 : 0) k_project(const float* __restrict__ X, int64_t n_pts, int D,
                                                 const float* __restrict__ AT, int lmp, const float* __restrict__ b,
                                                 int LM, float W, int32_t* __restrict__ codes,
                                                 float* __restrict__ vals, int32_t* __restrict__ pmin,
                                                 int32_t* __restrict__ pmax, int* __restrict__ err,
-                                                ZeroWords zw) {
+                                                ZeroWords zw, float* __restrict__ xcopy) {
     constexpr int BN = 16 * PT;
     constexpr int BC = 16 * CT;
     constexpr int XP = BN + 2;   // padded X row: the transposing stores conflict at most 4 ways
@@ -75,7 +77,10 @@ __global__ void __launch_bounds__(NT) k_project(const float* __restrict__ X, int
                 const int64_t gn = n0 + p;
                 const int gd = d0 + dq * 4;
                 float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (gn < n_pts && gd < D) v = __ldg(reinterpret_cast<const float4*>(X + gn * D + gd));
+                if (gn < n_pts && gd < D) {
+                    v = __ldg(reinterpret_cast<const float4*>(X + gn * D + gd));
+                    if constexpr (kCopy) *reinterpret_cast<float4*>(xcopy + gn * D + gd) = v;
+                }
                 xr[4 * r + 0] = v.x;
                 xr[4 * r + 1] = v.y;
                 xr[4 * r + 2] = v.z;
@@ -88,6 +93,9 @@ __global__ void __launch_bounds__(NT) k_project(const float* __restrict__ X, int
                 const int64_t gn = n0 + p;
                 const int gd = d0 + dd;
                 xr[r] = (gn < n_pts && gd < D) ? __ldg(X + gn * D + gd) : 0.0f;
+                if constexpr (kCopy) {
+                    if (gn < n_pts && gd < D) xcopy[gn * D + gd] = xr[r];
+                }
             }
         }
 #pragma unroll
@@ -260,30 +268,47 @@ int project_grid_x(int64_t n_pts) { return (int)((n_pts + 127) / 128); }
 
 cudaError_t launch_project_fp32(const float* X, int64_t n_pts, int D, const float* AT, int lmp, const float* b,
                                 int LM, float W, int32_t* codes, float* vals, int32_t* pmin, int32_t* pmax, int* err,
-                                cudaStream_t st, int tile, ZeroWords zw) {
+                                cudaStream_t st, int tile, ZeroWords zw, float* xcopy) {
     if (n_pts <= 0) return cudaSuccess;
     if (lmp < LM || (lmp & 3) || ((uintptr_t)AT & 15)) return cudaErrorInvalidValue;
+    // xcopy (the rows also written to device memory as they are read): one
+    // column block, so that every row is read exactly once
+    if (xcopy && (codes || tile != 5 || LM > 192)) return cudaErrorInvalidValue;
     if (codes) {
         k_project<true, 8, 4, 16><<<dim3(project_grid_x(n_pts), (LM + 63) / 64), NT, 0, st>>>(
-            X, n_pts, D, AT, lmp, b, LM, W, codes, nullptr, pmin, pmax, err, zw);
+            X, n_pts, D, AT, lmp, b, LM, W, codes, nullptr, pmin, pmax, err, zw, nullptr);
     } else if (tile == 1) {
         k_project<false, 2, 8, 64><<<dim3((unsigned)((n_pts + 31) / 32), (LM + 127) / 128), NT, 0, st>>>(
-            X, n_pts, D, AT, lmp, b, LM, W, nullptr, vals, nullptr, nullptr, err, zw);
+            X, n_pts, D, AT, lmp, b, LM, W, nullptr, vals, nullptr, nullptr, err, zw, nullptr);
     } else if (tile == 2) {
         k_project<false, 8, 4, 32><<<dim3((unsigned)((n_pts + 127) / 128), (LM + 63) / 64), NT, 0, st>>>(
-            X, n_pts, D, AT, lmp, b, LM, W, nullptr, vals, nullptr, nullptr, err, zw);
+            X, n_pts, D, AT, lmp, b, LM, W, nullptr, vals, nullptr, nullptr, err, zw, nullptr);
     } else if (tile == 3) {
         k_project<false, 4, 4, 32><<<dim3((unsigned)((n_pts + 63) / 64), (LM + 63) / 64), NT, 0, st>>>(
-            X, n_pts, D, AT, lmp, b, LM, W, nullptr, vals, nullptr, nullptr, err, zw);
+            X, n_pts, D, AT, lmp, b, LM, W, nullptr, vals, nullptr, nullptr, err, zw, nullptr);
     } else if (tile == 4) {
         k_project<false, 2, 4, 32><<<dim3((unsigned)((n_pts + 31) / 32), (LM + 63) / 64), NT, 0, st>>>(
-            X, n_pts, D, AT, lmp, b, LM, W, nullptr, vals, nullptr, nullptr, err, zw);
+            X, n_pts, D, AT, lmp, b, LM, W, nullptr, vals, nullptr, nullptr, err, zw, nullptr);
+    } else if (tile == 5) {
+        if (!xcopy) return cudaErrorInvalidValue;   // tiling 5 serves the copying form only
+        k_project<false, 2, 12, 32, true><<<dim3((unsigned)((n_pts + 31) / 32), (LM + 191) / 192), NT, 0, st>>>(
+            X, n_pts, D, AT, lmp, b, LM, W, nullptr, vals, nullptr, nullptr, err, zw, xcopy);
     } else {
         k_project<false, 4, 8, 32><<<dim3((unsigned)((n_pts + 63) / 64), (LM + 127) / 128), NT, 0, st>>>(
-            X, n_pts, D, AT, lmp, b, LM, W, nullptr, vals, nullptr, nullptr, err, zw);
+            X, n_pts, D, AT, lmp, b, LM, W, nullptr, vals, nullptr, nullptr, err, zw, nullptr);
     }
     return cudaGetLastError();
 }
+
+template <typename F>
+struct arity;
+template <typename R, typename... A>
+struct arity<R(A...)> {
+    static constexpr int value = sizeof...(A);
+};
+static_assert(arity<decltype(k_project<false, 2, 12, 32, true>)>::value == kProjectArgs, "projection parameters");
+
+const void* project_copy_kernel() { return reinterpret_cast<const void*>(&k_project<false, 2, 12, 32, true>); }
 
 cudaError_t launch_minmax_reduce(const int32_t* pmin, const int32_t* pmax, int nparts, int LM, int32_t* cmin,
                                  int32_t* cmax, cudaStream_t st) {

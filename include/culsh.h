@@ -212,7 +212,10 @@ typedef struct culsh_search_profile {
                             1: host buffers staged through device copies;
                             2: host buffers read and written by the kernels
                             directly (device with pageable memory access,
-                            16-byte aligned queries)                          */
+                            16-byte aligned queries), a copy kernel moving
+                            the queries to the device; 3: as 2, with the
+                            projection reading the queries and writing them
+                            to the device on the way (L*M <= 192)            */
     int stage_times;     /* 1: the stage times above were measured; 0: stage
                             events off (culsh_search_set_profiling)          */
 } culsh_search_profile;

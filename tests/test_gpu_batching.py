@@ -242,10 +242,50 @@ def test_host_search_direct_and_copy_paths(culsh, name, monkeypatch):
             np.testing.assert_array_equal(st.getKnnDistances(), c["knn_dists"])
             path = st.profile()["host_path"]
             if env is None and q is c["queries"]:
-                assert path in (1, 2)   # 2 where the device reads pageable memory (Grace-Blackwell)
+                assert path in (1, 3)   # 3 where the device reads pageable memory (Grace-Blackwell)
             else:
                 assert path == 1
     assert D > 0
+
+
+@pytest.mark.parametrize("name", ["mix_d16_t8", "odd_d13", "m40_t70"])
+def test_host_search_fused_copy_over_changing_buffers(culsh, name, monkeypatch):
+    """Where the device reads pageable memory, the projection reads the
+    caller's rows itself and copies them to the device for the candidate
+    stage (L*M <= 192). The cached search graph is replayed over other host
+    buffers by updating its projection node in place: rows in reverse order
+    give the rows of results in reverse order, fewer rows capture again. The
+    copy-kernel form (CULSH_NO_FUSED_COPY) and direct launches
+    (CULSH_NO_GRAPH) give the same results."""
+    c = load_case(name)
+    ht = build_index(culsh, c)
+    st = culsh.SearchTables()
+    st.reset(ht, int(c["K"]), int(c["T"]))
+    q0 = c["queries"]
+    q1 = np.ascontiguousarray(q0[::-1])
+    q2 = q0.copy()
+    q3 = q0[:7].copy()
+    ids, dists = c["knn_ids"], c["knn_dists"]
+    want = [(ids, dists), (ids[::-1], dists[::-1]), (ids[:7], dists[:7])]
+    seq = [(q0, 0, 1), (q1, 1, 2), (q2, 0, 2), (q1, 1, 2), (q3, 2, 1), (q3, 2, 2), (q0, 0, 1), (q2, 0, 2)]
+    for env in (None, "CULSH_NO_FUSED_COPY", "CULSH_NO_GRAPH"):
+        monkeypatch.delenv("CULSH_NO_FUSED_COPY", raising=False)
+        monkeypatch.delenv("CULSH_NO_GRAPH", raising=False)
+        if env:
+            monkeypatch.setenv(env, "1")
+        for i, (q, w, mode) in enumerate(seq):
+            st.search(q, dataset=c["X"])
+            np.testing.assert_array_equal(st.getKnnIds(), want[w][0], err_msg=f"{env} step {i}")
+            np.testing.assert_array_equal(st.getKnnDistances(), want[w][1], err_msg=f"{env} step {i}")
+            p = st.profile()
+            if p["host_path"] == 1:
+                continue   # no pageable memory access on this device
+            assert p["host_path"] == (2 if env == "CULSH_NO_FUSED_COPY" else 3)
+            if env == "CULSH_NO_GRAPH":
+                assert p["graph_mode"] == 0
+            elif env is None and i > 0:
+                # replayed (with the node pointed at the new rows) or captured anew
+                assert p["graph_mode"] == mode, f"step {i}"
 
 
 def test_clustered_queries_every_item_shape_and_order(culsh):
