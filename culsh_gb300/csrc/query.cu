@@ -450,14 +450,19 @@ __device__ __noinline__ void order_deltas_heap(const float* dn, uint8_t* enc, in
 // sets the shared memory per thread and hence the occupancy.
 __host__ __device__ constexpr int probe_cand_cap(int T) { return T > 16 ? (T + 1) / 2 + 1 : T; }
 // Slots of the list: one more than the cap while capping, for the entry
-// appended before the drop; T otherwise (the list never exceeds T - 1 + 1).
-__host__ __device__ constexpr int probe_cand_slots(int T) { return T > 16 ? probe_cand_cap(T) + 1 : T; }
+// appended before the drop; T - 1 otherwise (step t < T - 1 appends at most
+// at index t; the last step, T - 1, does not expand: nothing reads the list
+// after it).
+__host__ __device__ constexpr int probe_cand_slots(int T) {
+    return T > 16 ? probe_cand_cap(T) + 1 : (T > 1 ? T - 1 : 1);
+}
 
-// Per-thread shared-memory slice of the fast kernel, in bytes per thread.
+// Per-thread shared-memory slice of the fast kernel, in bytes per thread;
+// the rank slice ord[M] only where the deltas are ordered in shared memory.
 template <typename MaskT>
-__host__ __device__ constexpr size_t probe_fast_bytes_per_thread(int M, int T) {
+__host__ __device__ constexpr size_t probe_fast_bytes_per_thread(int M, int T, bool ranks = true) {
     return sizeof(MaskT) * (size_t)probe_cand_slots(T) + sizeof(float) * (size_t)(M + probe_cand_slots(T)) +
-           (size_t)(2 * M + M);
+           (size_t)(2 * M + (ranks ? M : 0));
 }
 
 // PCH: probes whose group loads are in flight together (tuned: 1, 2 or 4).
@@ -467,7 +472,7 @@ __host__ __device__ constexpr size_t probe_fast_bytes_per_thread(int M, int T) {
 // only; k_probe_resolve looks up), 2 tail (enumerate every probe, then look
 // them all up behind the key filter at the end of the same kernel).
 template <typename MaskT, int PCH, int MM, int kForm>
-__global__ void __launch_bounds__(PF, kForm > 0 ? 8 : 6) k_probe_fast(ProbeArgs a) {
+__global__ void __launch_bounds__(PF, kForm == 2 && MM <= 12 ? 9 : (kForm > 0 ? 8 : 6)) k_probe_fast(ProbeArgs a) {
     extern __shared__ __align__(16) unsigned char psm[];
     const LookupView& lv = a.lv;
     const int Q = a.Q, T = a.T, L = lv.L, M = lv.M, KW = lv.KW;
@@ -475,7 +480,7 @@ __global__ void __launch_bounds__(PF, kForm > 0 ? 8 : 6) k_probe_fast(ProbeArgs 
     const int M2 = 2 * M;
     // Strided per-thread slices (element i of a thread at [i * PF + tid]):
     // comb[S] (MaskT), dn[M], cd[S] (f32), enc[2M] (sorted delta -> column
-    // | up << 7), ord[M] (u8), S = probe_cand_slots(T). Each slice is placed
+    // | up << 7), ord[M] (u8; MM = 0 only), S = probe_cand_slots(T). Each slice is placed
     // from the block's base; the thread offset is added last, in units of the
     // slice's own element type.
     const int CAP = probe_cand_cap(T), SLOTS = probe_cand_slots(T);
@@ -577,7 +582,7 @@ __global__ void __launch_bounds__(PF, kForm > 0 ? 8 : 6) k_probe_fast(ProbeArgs 
     // One enumeration step (cuLSH_Kernels.cu:216-255): probe t > 0 is the
     // candidate of smallest delta sum (the first of equal sums), which is
     // then shifted in place and expanded into a new candidate.
-    auto next_probe = [&]() -> MaskT {
+    auto next_probe = [&](bool expand) -> MaskT {
         float mn = FLT_MAX;
         int mi = 0;
         for (int i = 0; i < size; ++i) {
@@ -589,7 +594,7 @@ __global__ void __launch_bounds__(PF, kForm > 0 ? 8 : 6) k_probe_fast(ProbeArgs 
         }
         const MaskT probe = comb[mi * PF];
         const int top = highest_bit(probe);
-        if (top < M2 - 1) {
+        if (expand && top < M2 - 1) {
             const MaskT p1 = probe | ((MaskT)1 << (top + 1));
             const float m1 = __fadd_rn(mn, sv(top + 1));
             comb[mi * PF] = p1;
@@ -649,7 +654,7 @@ __global__ void __launch_bounds__(PF, kForm > 0 ? 8 : 6) k_probe_fast(ProbeArgs 
         int pt = -1;
         int s0 = -1, s1 = -1, s2 = -1, s3 = -1;
         for (int t = 0; t < T; ++t) {
-            const MaskT probe = t > 0 ? next_probe() : (MaskT)0;
+            const MaskT probe = t > 0 ? next_probe(t < T - 1) : (MaskT)0;
             uint64_t hh;
             const bool ok = probe_hash(c, probe, hh);
             if (ok) {
@@ -752,7 +757,7 @@ __global__ void __launch_bounds__(PF, kForm > 0 ? 8 : 6) k_probe_fast(ProbeArgs 
             fw[j] = ~0ull;
             hsv[j] = fpv[j] = 0;
             if (t < T) {
-                const MaskT probe = t > 0 ? next_probe() : (MaskT)0;
+                const MaskT probe = t > 0 ? next_probe(t < T - 1) : (MaskT)0;
                 pm[j] = probe;
                 uint64_t hh;
                 if (probe_hash(c, probe, hh)) {
@@ -934,7 +939,7 @@ __global__ void __launch_bounds__(256, 5) k_probe_resolve(const __grid_constant_
 
 template <typename MaskT, int PCH, int MM, int kForm>
 cudaError_t launch_probe_fast_v(const ProbeArgs& a, cudaStream_t st) {
-    const size_t smem = (size_t)PF * probe_fast_bytes_per_thread<MaskT>(a.lv.M, a.T);
+    const size_t smem = (size_t)PF * probe_fast_bytes_per_thread<MaskT>(a.lv.M, a.T, MM == 0);
     static std::atomic<size_t> cap{0};   // dynamic shared memory this kernel is opted into
     const cudaError_t e = opt_in_smem(k_probe_fast<MaskT, PCH, MM, kForm>, smem, cap);
     if (e != cudaSuccess) return e;
