@@ -596,14 +596,17 @@ def run_culsh(args):
             a[...] = Qm
 
         def host_loop(bufs):
-            for i in range(args.warmup):
+            # the warm-up touches every buffer once (as a serving loop's
+            # reused staging buffers are); timed steps continue the rotation
+            w = max(args.warmup, n_rot)
+            for i in range(w):
                 st_h.search(bufs[i % n_rot], Q, X)
             if dist is not None:
                 dist.barrier()
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             for i in range(args.steps):
-                st_h.search(bufs[(args.warmup + i) % n_rot], Q, X)
+                st_h.search(bufs[(w + i) % n_rot], Q, X)
             el_max = reduce_max(dist, time.perf_counter() - t0, dev)
             assert np.array_equal(st_h.getKnnIds(), ids.cpu().numpy()), "host and device API results differ"
             return aggregate_throughput(Q * args.steps, world, el_max), st_h.profile()["host_path"]
