@@ -241,3 +241,33 @@ def test_cli_short_file_and_bad_sizes(culsh, tmp_path):
     assert r.returncode == 1 and "Could not load data matrix" in r.stdout
     r = subprocess.run([cli, str(f), "4", "2", "1", "2", "1.0", "3", "1", "1"], capture_output=True, text=True)
     assert r.returncode == 1 and "Invalid sizes" in r.stdout
+
+
+@pytest.mark.parametrize("cname,pyname", [("culsh_times", "_Times"), ("culsh_index_profile", "_IndexProfile"),
+                                          ("culsh_tuning", "_Tuning"), ("culsh_search_profile", "_Profile"),
+                                          ("culsh_server_config", "_ServerConfig"),
+                                          ("culsh_server_stats", "_ServerStats")])
+def test_ctypes_mirrors_match_the_header(culsh, cname, pyname, tmp_path):
+    """Every ctypes structure of the Python mirror has the C struct's size and,
+    field by field, its offsets and sizes (a C program compiled against
+    include/culsh.h prints them)."""
+    import ctypes
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    py = getattr(culsh, pyname)
+    fields = [f[0] for f in py._fields_]
+    lines = [f'printf("size %zu\\n", sizeof({cname}));']
+    for f in fields:
+        lines.append(f'printf("{f} %zu %zu\\n", offsetof({cname}, {f}), sizeof((({cname}*)0)->{f}));')
+    src = tmp_path / "layout.c"
+    src.write_text("#include <stddef.h>\n#include <stdio.h>\n#include \"culsh.h\"\nint main(void) {\n" +
+                   "\n".join("    " + l for l in lines) + "\n    return 0;\n}\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    assert out[0] == f"size {ctypes.sizeof(py)}", (cname, out[0], ctypes.sizeof(py))
+    for line, f in zip(out[1:], fields):
+        name, off, size = line.split()
+        d = getattr(py, f)
+        assert (name, int(off), int(size)) == (f, d.offset, d.size), (cname, line, d.offset, d.size)
