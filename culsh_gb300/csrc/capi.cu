@@ -1129,14 +1129,16 @@ cudaGraphNode_t find_kernel_node(cudaGraph_t g, const void* fn) {
         cudaGetLastError();
         return nullptr;
     }
-    for (size_t i = 0; i < n; ++i) {
+    cudaGraphNode_t found = nullptr;
+    for (size_t i = 0; i < n && !found; ++i) {
         cudaGraphNodeType t;
         if (cudaGraphNodeGetType(nodes[i], &t) != cudaSuccess || t != cudaGraphNodeTypeKernel) continue;
         cudaKernelNodeParams kp;
-        if (cudaGraphKernelNodeGetParams(nodes[i], &kp) == cudaSuccess && kp.func == fn) return nodes[i];
+        if (cudaGraphKernelNodeGetParams(nodes[i], &kp) == cudaSuccess && kp.func == fn) found = nodes[i];
     }
+    // a failed query above must not surface as the next launch's error
     cudaGetLastError();
-    return nullptr;
+    return found;
 }
 
 // Points the instantiated projection node of the fused host-copy form at
