@@ -8,9 +8,12 @@ The arithmetic lives in ``oracle.cpp`` (a C++17 + OpenMP restatement of the
 reference, each function citing ``cuLSH_*.cu`` file:line). This module only
 builds it (``make -C oracle``) and wraps it with numpy arrays.
 
-Parity status: unpinned against the reference build (no tests, fixtures or
-CPU path exist in the reference; it needs a GPU). Pinned instead by
-hand-traced known answers and an independent transliteration (tests/refsim.py).
+Parity status: the reference ships no tests, fixtures or CPU path, and its
+build needs a GPU. The oracle is pinned against the reference's own kernel
+file compiled for the host (``make -C oracle ref`` into ``oracle/_ref``, run
+by ``ref_kernels()``: projection epilogue, multiprobe enumeration, top-K
+heap), where the reference tree is present, and by hand-traced known answers
+and an independent transliteration (tests/refsim.py).
 """
 
 from __future__ import annotations
@@ -24,8 +27,10 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "build", "liboracle.so")
+_REF_PATH = os.path.join(_HERE, "_ref", "libref_kernels.so")
 _lock = threading.Lock()
 _lib = None
+_ref = None
 
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 _f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
@@ -43,6 +48,36 @@ def build() -> str:
     if not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB_PATH
+
+
+def build_ref() -> str | None:
+    """Compile the reference's kernel file for the host into oracle/_ref when
+    the reference tree is present (the Makefile's `ref` target); returns the
+    library path, or None when it was not built."""
+    srcs = [os.path.join(_HERE, f) for f in ("ref_kernels_host.cpp", "ref_shim.h")]
+    if not os.path.exists(_REF_PATH) or os.path.getmtime(_REF_PATH) < max(os.path.getmtime(f) for f in srcs):
+        subprocess.run(["make", "-s", "-C", _HERE, "ref"], check=True)
+    return _REF_PATH if os.path.exists(_REF_PATH) else None
+
+
+def ref_kernels():
+    """The reference's own kernels run on the host (oracle/_ref), or None when
+    they were not built here (no reference tree) or do not load on this
+    machine."""
+    global _ref
+    with _lock:
+        if _ref is None:
+            if not os.path.exists(_REF_PATH):
+                return None
+            try:
+                R = ctypes.CDLL(_REF_PATH)
+            except OSError:
+                return None
+            R.ref_projection_epilogue.argtypes = [_f32p, _int, _int, _f32p, _flt, _int]
+            R.ref_probing_codes.argtypes = [_f32p, _int, _int, _int, _f32p]
+            R.ref_topk.argtypes = [_int, _int, _u32p, _u32p, _u32p, ctypes.c_uint, _f32p, _i32p, _f32p]
+            _ref = R
+    return _ref
 
 
 def lib():
