@@ -12,7 +12,7 @@ Parity status: the reference ships no tests, fixtures or CPU path, and its
 build needs a GPU. The oracle is pinned against the reference's own kernel
 file compiled for the host (``make -C oracle ref`` into ``oracle/_ref``, run
 by ``ref_kernels()``: projection epilogue, multiprobe enumeration, top-K
-heap), where the reference tree is present, and by hand-traced known answers
+heap, distances), where the reference tree is present, and by hand-traced known answers
 and an independent transliteration (tests/refsim.py).
 """
 
@@ -76,6 +76,7 @@ def ref_kernels():
             R.ref_projection_epilogue.argtypes = [_f32p, _int, _int, _f32p, _flt, _int]
             R.ref_probing_codes.argtypes = [_f32p, _int, _int, _int, _f32p]
             R.ref_topk.argtypes = [_int, _int, _u32p, _u32p, _u32p, ctypes.c_uint, _f32p, _i32p, _f32p]
+            R.ref_distances.argtypes = [_f32p, _int, _int, _f32p, _int, _u32p, _u32p, ctypes.c_uint, _f32p]
             _ref = R
     return _ref
 

@@ -14,8 +14,8 @@
 // the host, though (ref_shim.h, ref_kernels_host.cpp, the Makefile's `ref`
 // target), and tests/test_oracle_refkernels.py checks this restatement bit
 // for bit against the reference's own projection epilogue, multiprobe
-// enumeration and top-K heap kernels run that way. The dot product (cuBLAS),
-// the distance reduction and the Thrust sorts are pinned instead by
+// enumeration, top-K heap and distance kernels run that way. The dot product
+// (cuBLAS) and the Thrust sorts are pinned instead by
 // hand-traced known-answer cases derived from reading the reference code
 // (tests/test_oracle_kat.py), exact-rational emulation, and an independent
 // line-by-line Python transliteration of the reference's multiprobe and top-K

@@ -14,11 +14,20 @@
 //                            (cuLSH_Querying.cu:63-119)
 //   ref_topk                 kernel_configureIds + kernel_sortIds as
 //                            calculateIds launches them (cuLSH_Querying.cu:231-277)
+//   ref_distances            kernel_calculateDistances as calculateDistances
+//                            launches it (cuLSH_Querying.cu:284-343)
+//
+// The file is compiled with floating-point contraction on, as nvcc's default
+// (-fmad=true) compiles the reference: its one multiply feeding an add, the
+// distance accumulation, becomes a fused multiply-add on both.
 #include "cuLSH_Kernels.cu"
 
+#include <barrier>
+#include <thread>
 #include <vector>
 
 thread_local ref_dim3 threadIdx, blockIdx, blockDim, gridDim;
+thread_local void (*ref_sync_hook)() = nullptr;
 
 namespace {
 
@@ -43,6 +52,39 @@ void launch(ref_dim3 grid, ref_dim3 block, F body) {
 }
 
 unsigned cdiv(unsigned a, unsigned b) { return (a + b - 1) / b; }
+
+// A launch whose blocks synchronise: each block runs as one host thread per
+// CUDA thread, blocks one after another, __syncthreads() on the block's
+// barrier (every thread of the reference kernel reaches each one).
+std::barrier<>* g_block_barrier = nullptr;
+void block_sync() { g_block_barrier->arrive_and_wait(); }
+
+template <class F>
+void launch_cooperative(ref_dim3 grid, ref_dim3 block, F body) {
+    const unsigned nt = block.x * block.y * block.z;
+    for (unsigned bz = 0; bz < grid.z; ++bz)
+        for (unsigned by = 0; by < grid.y; ++by)
+            for (unsigned bx = 0; bx < grid.x; ++bx) {
+                std::barrier<> bar((std::ptrdiff_t)nt);
+                g_block_barrier = &bar;
+                std::vector<std::thread> threads;
+                threads.reserve(nt);
+                for (unsigned tz = 0; tz < block.z; ++tz)
+                    for (unsigned ty = 0; ty < block.y; ++ty)
+                        for (unsigned tx = 0; tx < block.x; ++tx)
+                            threads.emplace_back([&, tx, ty, tz, bx, by, bz] {
+                                gridDim = grid;
+                                blockDim = block;
+                                blockIdx = ref_dim3{bx, by, bz};
+                                threadIdx = ref_dim3{tx, ty, tz};
+                                ref_sync_hook = block_sync;
+                                body();
+                                ref_sync_hook = nullptr;
+                            });
+                for (auto& t : threads) t.join();
+                g_block_barrier = nullptr;
+            }
+}
 
 }  // namespace
 
@@ -96,6 +138,23 @@ int ref_topk(int Q, int K, const unsigned* ids, const unsigned* starts, const un
     const ref_dim3 block{kBlock * kBlock, 1, 1}, grid{cdiv(Q, kBlock * kBlock), 1, 1};
     launch(grid, block, [&] { cuLSH::kernel_configureIds(out_d, out_ids, Q, K, total, dist, ids, starts, sizes); });
     launch(grid, block, [&] { cuLSH::kernel_sortIds(out_d, out_ids, Q, K); });
+    return 0;
+}
+
+// Squared L2 distance of each (query qidx[i], point cand[i]) pair, i < total;
+// queries Q x D and data N x D row-major (point-contiguous). One launch of up
+// to 65535 * 32 pairs, as the reference chunks them.
+int ref_distances(const float* queries, int D, int Q, const float* data, int N, const unsigned* cand,
+                  const unsigned* qidx, unsigned total, float* out) {
+    if (D <= 0 || total > 65535u * BLOCK_SIZE_Y) return -1;
+    if (total == 0) return 0;
+    const unsigned nb = cdiv(total, BLOCK_SIZE_Y);
+    // the kernel writes a result for every row of its last block, in range or not
+    std::vector<float> d((size_t)nb * BLOCK_SIZE_Y, 0.0f);
+    launch_cooperative(ref_dim3{1, nb, 1}, ref_dim3{BLOCK_SIZE_REDUCE, BLOCK_SIZE_Y, 1}, [&] {
+        cuLSH::kernel_calculateDistances(d.data(), total, queries, D, Q, data, N, cand, qidx);
+    });
+    for (unsigned i = 0; i < total; ++i) out[i] = d[i];
     return 0;
 }
 

@@ -4,10 +4,11 @@
  *
  * Test infrastructure only (tests/test_oracle_refkernels.py). A kernel runs
  * as a loop over its grid that calls the kernel body once per thread with
- * blockIdx/threadIdx set (ref_kernels_host.cpp); that is exact for the kernels
- * used here, which share no memory between threads and have no barriers.
- * kernel_calculateDistances (shared memory + __syncthreads) compiles but is
- * not run.
+ * blockIdx/threadIdx set (ref_kernels_host.cpp), which is exact for kernels
+ * that share nothing between threads. kernel_calculateDistances (shared memory
+ * + __syncthreads) runs each block as one host thread per CUDA thread: its
+ * __shared__ array becomes a function-local static, and __syncthreads() waits
+ * on the block's barrier through ref_sync_hook.
  *
  * The three macros below are the values cuLSH.h:71-77 gives them; that header
  * itself needs the CUDA libraries and is not included. */
@@ -31,7 +32,10 @@ struct ref_dim3 {
 };
 extern thread_local ref_dim3 threadIdx, blockIdx, blockDim, gridDim;
 
-static inline void __syncthreads() {}
+extern thread_local void (*ref_sync_hook)();
+static inline void __syncthreads() {
+    if (ref_sync_hook) ref_sync_hook();
+}
 /* Round toward +infinity to int / unsigned. The arguments here are
  * log2f(n) of small positive n, where that is the ceiling. */
 static inline int __float2int_ru(float x) { return (int)std::ceil(x); }

@@ -1,8 +1,8 @@
 """The oracle against the reference itself: the reference's own kernel file
 (cuLSH_Kernels.cu) compiled for the host into oracle/_ref and run with the
 buffer preparation and launch shapes of its host code (ref_kernels_host.cpp).
-Projection epilogue, multiprobe enumeration and the top-K heap must agree
-bit for bit with the oracle. Skipped where the reference tree was not
+Projection epilogue, multiprobe enumeration, the top-K heap and the
+distance kernel must agree bit for bit with the oracle. Skipped where the reference tree was not
 present at build time (oracle/_ref absent)."""
 
 import numpy as np
@@ -102,3 +102,29 @@ def test_topk_heap():
             np.testing.assert_array_equal(wd, od[q * K:(q + 1) * K])
             cases += 1
     assert cases > 1000
+
+
+def test_distances():
+    """The reference's distance kernel (eight lanes, shared-memory tree,
+    launched as calculateDistances launches it; its accumulation fused as
+    nvcc fuses it) against the oracle's lane-order distance: D from 1 to 299,
+    real and integer data, ragged pair counts."""
+    rng = np.random.default_rng(14)
+    pairs = 0
+    for trial in range(40):
+        D, N, Q = int(rng.integers(1, 300)), 40, 6
+        if trial % 3 == 0:
+            data = rng.integers(0, 255, (N, D)).astype(np.float32)
+            qs = rng.integers(0, 255, (Q, D)).astype(np.float32)
+        else:
+            data = rng.normal(0, 3, (N, D)).astype(np.float32)
+            qs = rng.normal(0, 3, (Q, D)).astype(np.float32)
+        total = int(rng.integers(1, 100))
+        cand = rng.integers(0, N, total).astype(np.uint32)
+        qidx = rng.integers(0, Q, total).astype(np.uint32)
+        out = np.zeros(total, np.float32)
+        assert ref.ref_distances(qs, D, Q, data, N, cand, qidx, total, out) == 0
+        want = np.array([oracle.distance(qs[qidx[i]], data[cand[i]]) for i in range(total)], np.float32)
+        np.testing.assert_array_equal(want, out, err_msg=f"D={D}")
+        pairs += total
+    assert pairs > 1000
