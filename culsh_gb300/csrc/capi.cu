@@ -3,10 +3,12 @@
 // Mirrors the state and call sequence of cuLSH::HashTables
 // (cuLSH_HashTables.cu) and cuLSH::SearchTables (cuLSH_SearchTables.cu), with
 // the data kept resident on one GPU: index() uploads the dataset once and
-// builds every table with four kernels (projection, key packing, one radix
-// sort over all tables, run-length + hash), and search() runs the whole query
-// path in three launches. Host copies of the bucket arrays and query buckets
-// are produced lazily, only when a getter or save() needs them.
+// builds all tables together, each stage one pass over every table
+// (projection with exact codes, key packing, one radix sort over all tables,
+// run-length encoding, bucket hash and key filters), and search() replays the
+// whole query path (projection, multiprobe, candidate stage: four to nine
+// kernels) as one captured CUDA graph. Host copies of the bucket arrays and
+// query buckets are produced lazily, only when a getter or save() needs them.
 #include <algorithm>
 #include <cerrno>
 #include <climits>
