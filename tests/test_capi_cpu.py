@@ -271,3 +271,64 @@ def test_ctypes_mirrors_match_the_header(culsh, cname, pyname, tmp_path):
         name, off, size = line.split()
         d = getattr(py, f)
         assert (name, int(off), int(size)) == (f, d.offset, d.size), (cname, line, d.offset, d.size)
+
+
+DROPIN_LOAD_SRC = r"""
+#include <cstdio>
+#include "cuLSH.h"
+// argv[1]: an index file; argv[2]: the getters' arrays, written in the file's
+// own order; argv[3]: where save() writes the index again.
+int main(int argc, char** argv) {
+    if (argc != 4) return 2;
+    cuLSH::HashTables ht;
+    if (ht.reset("/nonexistent/missing.index")) return 3;   // must fail, with the message on stdout
+    if (!ht.reset(argv[1])) return 4;
+    const int N = ht.getN(), D = ht.getD(), L = ht.getL(), M = ht.getM();
+    const float W = ht.getW();
+    FILE* o = fopen(argv[2], "wb");
+    const int hdr[4] = {N, D, L, M};
+    fwrite(hdr, 4, 4, o);
+    fwrite(&W, 4, 1, o);
+    for (int l = 0; l < L; ++l) {
+        fwrite(ht.getA(l), 4, (size_t)D * M, o);
+        fwrite(ht.getb(l), 4, (size_t)M, o);
+    }
+    fwrite(ht.getBuckets(), 4, (size_t)L, o);
+    for (int l = 0; l < L; ++l) {
+        const unsigned B = ht.getBuckets(l);
+        fwrite(ht.getBuckets_totalIndices(l), 4, (size_t)N, o);
+        fwrite(ht.getBuckets_startingIndices(l), 4, B, o);
+        fwrite(ht.getBuckets_sizes(l), 4, B, o);
+        fwrite(ht.getBuckets_codes(l), 4, (size_t)B * M, o);
+    }
+    fclose(o);
+    if (ht.getA(L) || ht.getBuckets_totalIndices(-1)) return 5;   // out-of-range tables read as null
+    if (!ht.save(argv[3])) return 6;
+    return 0;
+}
+"""
+
+
+def test_dropin_header_load_getters_save_without_gpu(culsh, tmp_path):
+    """The C++ drop-in (include/cuLSH.h) on the CPU: reset(file) of a missing
+    file returns false and prints the error on stdout; reset(file) of the
+    oracle's index file fills every getter, whose arrays written in the file's
+    order give the file back byte for byte, as does save(); out-of-range
+    tables read as null."""
+    src = tmp_path / "dropin_load.cpp"
+    src.write_text(DROPIN_LOAD_SRC)
+    exe = tmp_path / "dropin_load"
+    libdir = os.path.dirname(culsh.LIB_PATH)
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe),
+                    "-L", libdir, "-lculsh", f"-Wl,-rpath,{libdir}"], check=True)
+    dump, saved = tmp_path / "getters.bin", tmp_path / "saved.index"
+    r = subprocess.run([str(exe), INDEX_BIN, str(dump), str(saved)], capture_output=True, text=True)
+    assert r.returncode == 0, (r.returncode, r.stdout, r.stderr)
+    assert r.stdout.startswith("[Error @ ") and "missing.index" in r.stdout, r.stdout
+    original = open(INDEX_BIN, "rb").read()
+    assert dump.read_bytes() == original
+    assert saved.read_bytes() == original
+    c = load_case("odd_d13")
+    L, M, D = c["A"].shape
+    hdr = np.frombuffer(original[:16], np.int32)
+    assert tuple(hdr) == (c["X"].shape[0], D, L, M)
