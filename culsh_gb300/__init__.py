@@ -56,14 +56,16 @@ class _Profile(ctypes.Structure):
     _fields_ = [("project_ms", ctypes.c_float), ("probe_ms", ctypes.c_float), ("candidates_ms", ctypes.c_float),
                 ("launches", ctypes.c_int), ("deferred_queries", ctypes.c_int), ("key_words", ctypes.c_int),
                 ("candidates_mode", ctypes.c_int), ("graph_mode", ctypes.c_int), ("rechecked", ctypes.c_longlong),
-                ("dense_queries", ctypes.c_int), ("host_path", ctypes.c_int), ("stage_times", ctypes.c_int)]
+                ("dense_queries", ctypes.c_int), ("host_path", ctypes.c_int), ("stage_times", ctypes.c_int),
+                ("knn_queries", ctypes.c_int), ("knn_fallback", ctypes.c_int)]
 
 
 class _Tuning(ctypes.Structure):
     _fields_ = [("proj_tile", ctypes.c_int), ("probe_batch", ctypes.c_int), ("candidates_mode", ctypes.c_int),
                 ("ws_threads", ctypes.c_int), ("ws_blocks_per_sm", ctypes.c_int), ("ws_chunk", ctypes.c_int),
                 ("distance_bf16", ctypes.c_int), ("ws_set_slots", ctypes.c_int), ("search_ms", ctypes.c_float),
-                ("configs_tried", ctypes.c_int), ("probe_split", ctypes.c_int), ("ws_order", ctypes.c_int)]
+                ("configs_tried", ctypes.c_int), ("probe_split", ctypes.c_int), ("ws_order", ctypes.c_int),
+                ("dense_tc", ctypes.c_int), ("dense_min", ctypes.c_int)]
 
 
 class _IndexProfile(ctypes.Structure):

@@ -19,7 +19,7 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libculsh.so")
 
-SOURCES = ["project.cu", "project_tc.cu", "sort.cu", "query.cu", "candidates.cu", "capi.cu", "serve.cu"]
+SOURCES = ["project.cu", "project_tc.cu", "sort.cu", "query.cu", "candidates.cu", "knn_tc.cu", "capi.cu", "serve.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

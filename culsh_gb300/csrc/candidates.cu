@@ -563,6 +563,69 @@ __global__ void __launch_bounds__(DT, 1) k_candidates_dense(WsArgs a) {
     }
 }
 
+// Membership rows of the dense queries for the tensor-core path
+// (knn_tc.cu): query k of the dense list gets row bm[k][0 .. nwp) with bit i
+// set when point i is one of its candidates (nwp - ceil(N/32) padding words
+// stay zero). The bits are set in an N-bit bitmap in shared memory from the
+// query's bucket ids (every matched bucket over the L tables and T probes,
+// as the reference's candidate lists, cuLSH_SearchTables.cu:321-364) and
+// copied out once; their count is the query's unique candidate count.
+// Persistent grid, one query per CTA at a time.
+__global__ void __launch_bounds__(DT, 1) k_cand_bitmap(WsArgs a, uint32_t* __restrict__ bm, int nwp) {
+    extern __shared__ __align__(16) uint32_t bits[];
+    __shared__ GatherSmem<DT, GCH> s_gather;
+    __shared__ int s_q, s_k;
+    __shared__ unsigned long long s_cnt[DW];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned int ndense = *a.n_dense;
+    for (;;) {
+        if (tid == 0) {
+            const unsigned int k = atomicAdd(a.dense_next, 1u);
+            s_k = (int)k;
+            s_q = k < ndense ? a.dense_q[k] : -1;
+        }
+        __syncthreads();
+        const int q = s_q, k = s_k;
+        if (q < 0) break;
+        for (int i = tid; i < nwp; i += DT) bits[i] = 0u;
+        __syncthreads();
+        const BucketView bv{a.qbuckets, a.boff, a.starts, a.sizes, a.ids, a.N, a.L, a.T, a.Q};
+        gather_bucket_ids<DT, GCH>(bv, q, s_gather,
+                                   [&](uint32_t id) { atomicOr(&bits[id >> 5], 1u << (id & 31)); });
+        __syncthreads();
+        uint32_t* row = bm + (int64_t)k * nwp;
+        unsigned long long cnt = 0;
+        for (int i = tid * 4; i < nwp; i += DT * 4) {
+            const uint4 v = *reinterpret_cast<const uint4*>(bits + i);
+            *reinterpret_cast<uint4*>(row + i) = v;
+            cnt += __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        if (lane == 0) s_cnt[warp] = cnt;
+        __syncthreads();
+        if (tid == 0) {
+            unsigned long long U = 0;
+            for (int w = 0; w < DW; ++w) U += s_cnt[w];
+            a.cu[q] = U;
+            atomicAdd(a.totals + 0, U);
+            atomicAdd(a.totals + 1, a.cnu[q]);
+        }
+        __syncthreads();
+    }
+}
+
+size_t bitmap_smem_bytes(int64_t N) { return 4 * (size_t)((((N + 31) >> 5) + 3) & ~3ll); }
+
+cudaError_t launch_cand_bitmap(const WsArgs& a, uint32_t* bm, int nwp, int grid, cudaStream_t st) {
+    static std::atomic<size_t> cap{0};
+    const size_t smem = 4 * (size_t)nwp;
+    const cudaError_t e = opt_in_smem(k_cand_bitmap, smem, cap);
+    if (e != cudaSuccess) return e;
+    k_cand_bitmap<<<grid, DT, smem, st>>>(a, bm, nwp);
+    return cudaGetLastError();
+}
+
 size_t dense_smem_bytes(int64_t N, int D, int K) {
     const size_t nwp = (size_t)((((N + 31) >> 5) + 3) & ~3ll);
     return sizeof(float) * (size_t)((D + 3) & ~3) + 4 * nwp + 4 * (size_t)DT * 32 +

@@ -142,6 +142,12 @@ struct culsh_index {
     DevBuf<uint16_t> xb;    // bf16 copy of the device dataset (search precision form), built on first use
     DevBuf<uint8_t> xflag;  // per row: 1 exact in bf16, 2 always re-check in FP32, 0 bound applies
     bool xb_valid = false;
+    // tensor-core k-NN rows of the dataset (bf16 parts, weights, flags), built on first use
+    DevBuf<uint16_t> kx_h, kx_l;
+    DevBuf<float> kw_exact, kw_bound;
+    DevBuf<KnnState> kstate;
+    KnnState h_kstate{};
+    bool kx_valid = false;
     int KW = 1;
     std::vector<int32_t> h_cmin, h_cmax;
     std::vector<uint8_t> h_fbits;
@@ -202,8 +208,10 @@ struct SearchTune {
     int ws_slots = 4096;   // shared hash-set slots per work item (4096, 8192 or 16384)
     int probe_split = 0;   // M <= 16: 1 enumeration kernel + lookup kernel; 2 lookups at the enumeration's end
     int ws_order = 0;      // 1: plan queries in the locality order of their home bucket (work-stealing form)
+    int dense_tc = 1;      // 1: dense queries take the tensor-core path (membership rows + masked GEMM)
+    int dense_min = 0;     // non-unique candidates that make a query dense (0: the form's default)
 };
-constexpr size_t kPlanBytes = 1024;   // room for the graph key (checked below)
+constexpr size_t kPlanBytes = 2048;   // room for the graph key (checked below)
 
 struct culsh_search {
     culsh_index* ix = nullptr;
@@ -230,6 +238,13 @@ struct culsh_search {
     DevBuf<uint8_t> item_p;
     DevBuf<float> part_d;
     DevBuf<uint32_t> part_i;
+    // tensor-core k-NN path: membership rows, query rows, partial lists, fallback list
+    DevBuf<uint32_t> kbm;
+    DevBuf<uint16_t> kq_h, kq_l;
+    DevBuf<float> kq_sq, kq_base, kpart_key;
+    DevBuf<uint32_t> kpart_id;
+    DevBuf<int> kpart_n, kfallback;
+    int knn_queries = 0, knn_fallback = 0;   // last search: dense queries on the tensor cores, re-run
     int sms = 0, smem_optin = 0, ws_used = 0, ws_overflow = 0;
     long long occ_key = -1;
     int occ_val = 1;
@@ -291,6 +306,7 @@ void clear_index_state(culsh_index* ix) {
     ix->x_borrow = nullptr;
     ix->proj_on_dev = false;
     ix->xb_valid = false;
+    ix->kx_valid = false;
 }
 
 int upload_projection(culsh_index* ix, cudaStream_t st) {
@@ -806,6 +822,15 @@ namespace {
 int forced_per_query() { return getenv("CULSH_CANDIDATES_PER_QUERY") != nullptr; }
 
 constexpr int kWsPartitions = 64;              // most partitions of one query
+
+// Statistics words of a search (device, cleared by its first kernel, copied
+// to the host after it): [0] unique and [1] non-unique candidate totals,
+// [2] overflow-arena top, [3] deferred queries, [4] work-stealing item
+// counter (low) and overflow flag (high), [5] items, [6] BF16 re-checks,
+// [7] dense queries (low) and their claim counter (high), [8..9] the dense
+// queries' k-NN row state, [10] tensor-core fallback queries, [11] its error
+// flags, [12..13] totals of re-runs that must not count twice.
+constexpr int kStatWords = 16;
 constexpr size_t kWsPartialBytes = size_t(64) << 20;
 
 // CULSH_WS_PARTITIONS (1..64) and CULSH_WS_ITEMS lower the partition count
@@ -831,6 +856,9 @@ struct SearchPlan {
     ProbeArgs pa;
     int probe_generic;
     int use_ws, ws_grid, use_dense, dense_grid;
+    int use_knn;        // dense queries on the tensor cores (membership rows + masked GEMM)
+    uint32_t* kbm;      // their membership rows
+    KnnSearch kn;
     CandArgs ca;
     WsArgs wa;
     unsigned long long* stats;
@@ -841,6 +869,98 @@ struct SearchPlan {
 };
 
 static_assert(sizeof(SearchPlan) <= kPlanBytes, "graph key buffer too small");
+
+// Dataset rows of the tensor-core k-NN path (bf16 parts, weights, flags),
+// made once per dataset. The stream is drained before they are published:
+// searches on other streams read them as soon as they see them.
+int ensure_knn_rows(culsh_index* ix, cudaStream_t st) {
+    if (ix->kx_valid) return CULSH_OK;
+    const int N = ix->N, D = ix->D, Dp = (D + 63) / 64 * 64;
+    const int64_t pad = ((int64_t)N + 255) / 256 * 256;
+    CU_TRY(ix->kx_h.reserve((size_t)N * Dp));
+    CU_TRY(ix->kx_l.reserve((size_t)N * Dp));
+    CU_TRY(ix->kw_exact.reserve((size_t)pad));
+    CU_TRY(ix->kw_bound.reserve((size_t)pad));
+    CU_TRY(ix->kstate.reserve(1));
+    CU_TRY(cudaMemsetAsync(ix->kstate.p, 0, sizeof(KnnState), st));
+    CU_TRY(launch_knn_rows_dataset(ix->dev_x(), N, D, Dp, ix->kx_h.p, ix->kx_l.p, ix->kw_exact.p, ix->kw_bound.p, pad,
+                                   knn_bound_factor(D), ix->kstate.p, st));
+    CU_TRY(cudaMemcpyAsync(&ix->h_kstate, ix->kstate.p, sizeof(KnnState), cudaMemcpyDeviceToHost, st));
+    CU_TRY(cudaStreamSynchronize(st));
+    ix->kx_valid = true;
+    return CULSH_OK;
+}
+
+// Whether the dataset's values allow the exact form (integers of magnitude
+// <= 256, D max|v|^2 < 2^24 and D (max - min)^2 < 2^24); the queries must
+// qualify too, which the kernels check on the device.
+bool knn_dataset_exact(const culsh_index* ix) {
+    const KnnState& k = ix->h_kstate;
+    if (k.flags & (kKnnNotSmallInt | kKnnNonFinite) || k.mneg == 0 || k.mpos == 0) return false;
+    const long long lo = 257 - k.mneg, hi = k.mpos - 257, mag = std::max(-lo, hi);
+    return (long long)ix->D * mag * mag < (1ll << 24) && (long long)ix->D * (hi - lo) * (hi - lo) < (1ll << 24);
+}
+
+// Membership rows above this size send the dense queries to the SIMT kernel.
+constexpr size_t kKnnMaxBitmapBytes = size_t(16) << 30;
+
+// Plans the tensor-core path for the dense queries of a search of Q queries
+// (sets *ok); it declines dimensions above 128, K above kMaxKnnK, datasets
+// whose N-bit bitmap does not fit a block's shared memory and membership rows
+// above kKnnMaxBitmapBytes.
+int plan_knn(culsh_search* s, SearchPlan& P, int Q, int32_t* d_ids, float* d_d, cudaStream_t st, bool* ok) {
+    *ok = false;
+    culsh_index* ix = s->ix;
+    KnnSearch& k = P.kn;
+    k.N = ix->N;
+    k.D = ix->D;
+    k.K = s->K;
+    k.Qcap = (Q + kKnnTileQ - 1) / kKnnTileQ * kKnnTileQ;
+    k.grid = s->sms;
+    if (!knn_plan(k, s->smem_optin)) return CULSH_OK;
+    if (bitmap_smem_bytes(ix->N) + 8192 > (size_t)s->smem_optin) return CULSH_OK;
+    const size_t bm_words = (size_t)k.Qcap * k.nwp;
+    if (4 * bm_words > kKnnMaxBitmapBytes) return CULSH_OK;
+    TRY(ensure_knn_rows(ix, st));
+    if (ix->h_kstate.flags & kKnnNonFinite) return CULSH_OK;
+    k.exact_possible = knn_dataset_exact(ix) && k.ops_exact > 0;
+    k.C = knn_bound_factor(ix->D);
+    CU_TRY(s->kbm.reserve(bm_words));
+    CU_TRY(s->kq_h.reserve((size_t)k.Qcap * k.Dp));
+    CU_TRY(s->kq_l.reserve((size_t)k.Qcap * k.Dp));
+    CU_TRY(s->kq_sq.reserve(k.Qcap));
+    CU_TRY(s->kq_base.reserve(k.Qcap));
+    CU_TRY(s->kpart_key.reserve(knn_part_entries(k)));
+    CU_TRY(s->kpart_id.reserve(knn_part_entries(k)));
+    CU_TRY(s->kpart_n.reserve(knn_part_lists(k)));
+    CU_TRY(s->kfallback.reserve(k.Qcap));
+    k.xh = ix->kx_h.p;
+    k.xl = ix->kx_l.p;
+    k.w_exact = ix->kw_exact.p;
+    k.w_bound = ix->kw_bound.p;
+    k.dstate = ix->kstate.p;
+    k.X = ix->dev_x();
+    k.queries = P.ca.queries;
+    k.dense_q = s->dense_q.p;
+    k.n_dense = P.wa.n_dense;
+    k.qh = s->kq_h.p;
+    k.ql = s->kq_l.p;
+    k.qsq = s->kq_sq.p;
+    k.qbase = s->kq_base.p;
+    k.qstate = reinterpret_cast<KnnState*>(s->stats.p + 8);
+    k.bm = s->kbm.p;
+    k.part_key = s->kpart_key.p;
+    k.part_id = s->kpart_id.p;
+    k.part_n = s->kpart_n.p;
+    k.out_ids = d_ids;
+    k.out_d = d_d;
+    k.fallback = s->kfallback.p;
+    k.n_fallback = reinterpret_cast<unsigned int*>(s->stats.p + 10);
+    k.err = reinterpret_cast<int*>(s->stats.p + 11);
+    P.kbm = s->kbm.p;
+    *ok = true;
+    return CULSH_OK;
+}
 
 // Sizes every buffer of a search of Q queries and fills the plan. Allocates
 // (when buffers grow) but launches nothing.
@@ -856,9 +976,9 @@ int plan_search(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* 
     CU_TRY(s->qb.reserve((size_t)L * Q * T));
     CU_TRY(s->cnu.reserve(Q));
     CU_TRY(s->cu.reserve(Q));
-    CU_TRY(s->stats.reserve(8));
+    CU_TRY(s->stats.reserve(kStatWords));
     CU_TRY(s->deferred.reserve(2 * (size_t)Q));
-    CU_TRY(s->h_stats.reserve(8));
+    CU_TRY(s->h_stats.reserve(kStatWords));
     const size_t cap_words = arena_cap_words();
     const size_t init_words = std::min(kArenaInitialWords, cap_words);
     if (s->arena.n < init_words || s->arena.n > cap_words) {
@@ -1026,22 +1146,38 @@ int plan_search(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* 
         a.slots = tu.ws_slots;
         a.bf16 = bf16;
         // Dense form: queries with at least dense_min non-unique candidates
-        // (max(32768, N/16), or CULSH_DENSE_MIN) take the bitmap kernel,
-        // launched only when some query could reach it (L*T*largest bucket)
-        // and the N-bit bitmap fits the shared memory of a block.
-        unsigned long long dmin = std::max<unsigned long long>(32768ull, (unsigned long long)ix->N / 16);
-        if (const char* e = getenv("CULSH_DENSE_MIN")) dmin = std::max(1ll, atoll(e));
-        const bool dense_fits = dense_smem_bytes(ix->N, D, K) + 8192 <= (size_t)s->smem_optin;
-        const bool dense_reachable = (unsigned long long)L * T * ix->max_bucket >= dmin;
-        P.use_dense = dense_fits && dense_reachable;
+        // take the tensor-core path (membership rows and a masked GEMM over
+        // the whole dataset; default threshold max(4096, N/256)) or, where
+        // that path does not apply, the SIMT bitmap kernel (max(32768, N/16)).
+        // The tuning or CULSH_DENSE_MIN override the threshold. The dense
+        // kernels are launched only when some query could reach it (L*T*largest
+        // bucket) and the N-bit bitmap fits the shared memory of a block.
+        a.n_dense = reinterpret_cast<unsigned int*>(s->stats.p + 7);
+        a.dense_next = reinterpret_cast<unsigned int*>(s->stats.p + 7) + 1;
+        const unsigned long long reach = (unsigned long long)L * T * ix->max_bucket;
+        auto dense_min_for = [&](bool tc) {
+            unsigned long long d = tc ? std::max<unsigned long long>(4096ull, (unsigned long long)ix->N / 256)
+                                      : std::max<unsigned long long>(32768ull, (unsigned long long)ix->N / 16);
+            if (tu.dense_min > 0) d = (unsigned long long)tu.dense_min;
+            if (const char* e = getenv("CULSH_DENSE_MIN")) d = std::max(1ll, atoll(e));
+            return d;
+        };
+        bool knn = false;
+        if (tu.dense_tc && !getenv("CULSH_NO_KNN_TC") && reach >= dense_min_for(true)) {
+            CU_TRY(s->dense_q.reserve(Q));
+            TRY(plan_knn(s, P, Q, d_ids, d_d, st, &knn));
+        }
+        const unsigned long long dmin = dense_min_for(knn);
+        const bool dense_fits = knn || dense_smem_bytes(ix->N, D, K) + 8192 <= (size_t)s->smem_optin;
+        P.use_dense = dense_fits && reach >= dmin;
+        P.use_knn = P.use_dense && knn;
         a.dense_min = P.use_dense ? dmin : ~0ull;
         if (P.use_dense) {
             CU_TRY(s->dense_q.reserve(Q));
             a.dense_q = s->dense_q.p;
             P.dense_grid = s->sms;
+            if (P.use_knn) P.kn.dense_q = s->dense_q.p;
         }
-        a.n_dense = reinterpret_cast<unsigned int*>(s->stats.p + 7);
-        a.dense_next = reinterpret_cast<unsigned int*>(s->stats.p + 7) + 1;
         if (tu.ws_order) {
             CU_TRY(s->qorder.reserve(Q));
             CU_TRY(s->qorder_bins.reserve(kOrderBins + 1));
@@ -1081,7 +1217,7 @@ int enqueue_search(const SearchPlan& P, cudaStream_t st, bool capturing, int* la
     zw.a = P.cnu;
     zw.na = P.Q;
     zw.b = P.stats;
-    zw.nb = 8;
+    zw.nb = kStatWords;
     CU_TRY(launch_project_fp32(P.dQ, P.Q, P.D, P.AT, P.lmp, P.b, P.LM, P.W, nullptr, P.vals, nullptr, nullptr,
                                nullptr, st, P.proj_tile, zw, P.xcopy));
     if (P.stage_events) CU_TRY(cudaEventRecordWithFlags(P.ev[1], st, evf));
@@ -1091,13 +1227,19 @@ int enqueue_search(const SearchPlan& P, cudaStream_t st, bool capturing, int* la
         if (P.wa.order) CU_TRY(launch_order_queries(P.wa, st));
         CU_TRY(launch_plan_items(P.wa, st));
         CU_TRY(launch_candidates_ws(P.wa, P.ws_grid, st));
-        if (P.use_dense) CU_TRY(launch_candidates_dense(P.wa, P.dense_grid, st));
+        if (P.use_knn) {
+            CU_TRY(launch_cand_bitmap(P.wa, P.kbm, P.kn.nwp, P.dense_grid, st));
+            CU_TRY(launch_knn_search(P.kn, st));
+        } else if (P.use_dense) {
+            CU_TRY(launch_candidates_dense(P.wa, P.dense_grid, st));
+        }
     } else {
         CU_TRY(launch_candidates(P.ca, st));
     }
     if (P.stage_events) CU_TRY(cudaEventRecordWithFlags(P.ev[3], st, evf));
-    CU_TRY(cudaMemcpyAsync(P.h_stats, P.stats, 8 * 8, cudaMemcpyDeviceToHost, st));
-    *launches = (P.use_ws ? (P.use_dense ? 4 : 3) + (P.wa.order ? 3 : 0) : 2) + probe_launches(P.pa);
+    CU_TRY(cudaMemcpyAsync(P.h_stats, P.stats, 8 * kStatWords, cudaMemcpyDeviceToHost, st));
+    const int dense_launches = P.use_knn ? 1 + knn_launches(P.kn) : (P.use_dense ? 1 : 0);
+    *launches = (P.use_ws ? 3 + dense_launches + (P.wa.order ? 3 : 0) : 2) + probe_launches(P.pa);
     return CULSH_OK;
 }
 
@@ -1213,6 +1355,60 @@ int run_plan(culsh_search* s, const SearchPlan& P, cudaStream_t st) {
     return CULSH_OK;
 }
 
+// Runs the per-query candidate kernel over the queries of dl, in chunks whose
+// candidate sets fit the overflow arena, growing the arena as far as free
+// memory allows (cuLSH_SearchTables.cu:282-306: a query whose candidates
+// alone do not fit fails the search). tmpl gives the kernel's arguments; its
+// totals pointer decides where the chunk's counts go.
+int rerun_queries(culsh_search* s, const CandArgs& tmpl, std::vector<int> dl, int Q, cudaStream_t st) {
+    const size_t cap_words = arena_cap_words();
+    std::vector<unsigned long long> cnu(Q);
+    CU_TRY(cudaMemcpyAsync(cnu.data(), s->cnu.p, 8 * (size_t)Q, cudaMemcpyDeviceToHost, st));
+    CU_TRY(cudaStreamSynchronize(st));
+    std::sort(dl.begin(), dl.end());
+    size_t need_max = 0, need_all = 0;
+    for (int q : dl) {
+        need_max = std::max(need_max, cand_arena_words(cnu[q]));
+        need_all += cand_arena_words(cnu[q]);
+    }
+    size_t freeb = 0, totalb = 0;
+    CU_TRY(cudaMemGetInfo(&freeb, &totalb));
+    size_t avail_words = (freeb + 4 * s->arena.n > (size_t)(64 << 20)) ? (freeb + 4 * s->arena.n - (64 << 20)) / 4 : 0;
+    avail_words = std::min(avail_words, cap_words);
+    if (need_max > avail_words) {
+        for (int q : dl)
+            if (cand_arena_words(cnu[q]) == need_max)
+                return fail(CULSH_ERR_OUT_OF_MEMORY,
+                            "Cannot load all candidates for computation of knn ids of query %d/%d...", q + 1, Q);
+    }
+    const size_t want = std::min(need_all, avail_words);
+    if (want > s->arena.n) {
+        std::lock_guard<std::mutex> lk(alloc_capture_mutex());
+        s->arena.release();
+        CU_TRY(s->arena.reserve(want));
+    }
+    size_t i = 0;
+    while (i < dl.size()) {
+        size_t j = i, words = 0;
+        while (j < dl.size() && words + cand_arena_words(cnu[dl[j]]) <= s->arena.n) words += cand_arena_words(cnu[dl[j++]]);
+        CU_TRY(cudaMemcpyAsync(s->deferred.p, dl.data() + i, 4 * (j - i), cudaMemcpyHostToDevice, st));
+        CU_TRY(cudaMemsetAsync(s->stats.p + 2, 0, 16, st));
+        CandArgs cb = tmpl;
+        cb.arena = s->arena.p;
+        cb.arena_words = s->arena.n;
+        cb.qlist = s->deferred.p;
+        cb.nq = (int)(j - i);
+        cb.deferred = s->deferred.p + (j - i);  // never written: the chunk fits
+        CU_TRY(launch_candidates(cb, st));
+        s->launches += 1;
+        CU_TRY(cudaMemcpyAsync(s->h_stats.p, s->stats.p, 8 * 4, cudaMemcpyDeviceToHost, st));
+        CU_TRY(cudaStreamSynchronize(st));
+        if ((s->h_stats.p[3] & 0xffffffffu) != 0) return fail(CULSH_ERR_DEVICE, "candidate admission failed");
+        i = j;
+    }
+    return CULSH_OK;
+}
+
 // After the plan ran: waits for its statistics, re-runs the candidate stage
 // per query when a work-stealing partition overflowed, and admits the
 // queries whose candidate sets did not fit the arena in chunks
@@ -1229,65 +1425,40 @@ int finish_search(culsh_search* s, const SearchPlan& P, cudaStream_t st) {
         // partial-list buffers): redo the stage with the per-query kernel,
         // whose global arena takes any set size.
         s->ws_overflow = 1;
-        CU_TRY(cudaMemsetAsync(s->stats.p, 0, 8 * 8, st));
+        CU_TRY(cudaMemsetAsync(s->stats.p, 0, 8 * kStatWords, st));
         CU_TRY(launch_candidates(ca, st));
         s->launches += 1;
-        CU_TRY(cudaMemcpyAsync(s->h_stats.p, s->stats.p, 8 * 8, cudaMemcpyDeviceToHost, st));
+        CU_TRY(cudaMemcpyAsync(s->h_stats.p, s->stats.p, 8 * kStatWords, cudaMemcpyDeviceToHost, st));
         CU_TRY(cudaStreamSynchronize(st));
     }
     unsigned int ndef = (unsigned int)(s->h_stats.p[3] & 0xffffffffu);
     if (ndef) {
-        const size_t cap_words = arena_cap_words();
         std::vector<int> dl(ndef);
-        std::vector<unsigned long long> cnu(Q);
         CU_TRY(cudaMemcpyAsync(dl.data(), s->deferred.p, 4 * (size_t)ndef, cudaMemcpyDeviceToHost, st));
-        CU_TRY(cudaMemcpyAsync(cnu.data(), s->cnu.p, 8 * (size_t)Q, cudaMemcpyDeviceToHost, st));
         CU_TRY(cudaStreamSynchronize(st));
-        std::sort(dl.begin(), dl.end());
         s->deferred_queries = (int)ndef;
-        size_t need_max = 0, need_all = 0;
-        for (int q : dl) {
-            need_max = std::max(need_max, cand_arena_words(cnu[q]));
-            need_all += cand_arena_words(cnu[q]);
-        }
-        size_t freeb = 0, totalb = 0;
-        CU_TRY(cudaMemGetInfo(&freeb, &totalb));
-        size_t avail_words = (freeb + 4 * s->arena.n > (size_t)(64 << 20)) ? (freeb + 4 * s->arena.n - (64 << 20)) / 4 : 0;
-        avail_words = std::min(avail_words, cap_words);
-        if (need_max > avail_words) {
-            for (int q : dl)
-                if (cand_arena_words(cnu[q]) == need_max)
-                    return fail(CULSH_ERR_OUT_OF_MEMORY,
-                                "Cannot load all candidates for computation of knn ids of query %d/%d...", q + 1, Q);
-        }
-        const size_t want = std::min(need_all, avail_words);
-        if (want > s->arena.n) {
-            std::lock_guard<std::mutex> lk(alloc_capture_mutex());
-            s->arena.release();
-            CU_TRY(s->arena.reserve(want));
-        }
-        size_t i = 0;
-        while (i < dl.size()) {
-            size_t j = i, words = 0;
-            while (j < dl.size() && words + cand_arena_words(cnu[dl[j]]) <= s->arena.n) words += cand_arena_words(cnu[dl[j++]]);
-            CU_TRY(cudaMemcpyAsync(s->deferred.p, dl.data() + i, 4 * (j - i), cudaMemcpyHostToDevice, st));
-            CU_TRY(cudaMemsetAsync(s->stats.p + 2, 0, 16, st));
-            CandArgs cb = ca;
-            cb.arena = s->arena.p;
-            cb.arena_words = s->arena.n;
-            cb.qlist = s->deferred.p;
-            cb.nq = (int)(j - i);
-            cb.deferred = s->deferred.p + (j - i);  // never written: the chunk fits
-            CU_TRY(launch_candidates(cb, st));
-            s->launches += 1;
-            CU_TRY(cudaMemcpyAsync(s->h_stats.p, s->stats.p, 8 * 4, cudaMemcpyDeviceToHost, st));
-            CU_TRY(cudaStreamSynchronize(st));
-            if ((s->h_stats.p[3] & 0xffffffffu) != 0) return fail(CULSH_ERR_DEVICE, "candidate admission failed");
-            i = j;
-        }
+        TRY(rerun_queries(s, ca, std::move(dl), Q, st));
     }
     s->tot_unique = s->h_stats.p[0];
     s->tot_nonunique = s->h_stats.p[1];
+    s->knn_queries = s->knn_fallback = 0;
+    if (P.use_knn && !s->ws_overflow) {
+        if ((s->h_stats.p[11] & 0xffffffffu) != 0)
+            return fail(CULSH_ERR_DEVICE, "tensor-core k-NN: a bounded device wait gave up");
+        s->knn_queries = (int)(s->h_stats.p[7] & 0xffffffffu);
+        // queries whose bound-form lists could not prove their top-K: the
+        // exact per-query kernel (their counts were taken already)
+        const unsigned int nfb = (unsigned int)(s->h_stats.p[10] & 0xffffffffu);
+        if (nfb) {
+            std::vector<int> fl(nfb);
+            CU_TRY(cudaMemcpyAsync(fl.data(), s->kfallback.p, 4 * (size_t)nfb, cudaMemcpyDeviceToHost, st));
+            CU_TRY(cudaStreamSynchronize(st));
+            CandArgs cb = ca;
+            cb.totals = s->stats.p + 12;
+            TRY(rerun_queries(s, cb, std::move(fl), Q, st));
+            s->knn_fallback = (int)nfb;
+        }
+    }
     s->rechecked = P.use_ws && P.wa.bf16 && !s->ws_overflow ? (long long)s->h_stats.p[6] : 0;
     s->dense_queries = P.use_ws && P.use_dense && !s->ws_overflow ? (int)(s->h_stats.p[7] & 0xffffffffu) : 0;
     return CULSH_OK;
@@ -1516,6 +1687,7 @@ int culsh_index_load(culsh_index* ix, const char* path, FILE* dbg) {
     ix->indexed = ix->host_valid = true;
     ix->dev_valid = false;
     ix->xb_valid = false;
+    ix->kx_valid = false;
     if (dbg)
         fprintf(dbg, "[HashTables::load]\tIndexing structure loaded from file \"%s\", (N, D, L, M, W) = (%d, %d, %d, %d, %.2f)\n",
                 path, N, D, L, M, W);
@@ -1654,6 +1826,7 @@ int culsh_search_run(culsh_search* s, const float* queries, int Q, const float* 
         CU_TRY(cudaMemcpyAsync(ix->X.p, dataset, sizeof(float) * (size_t)ix->N * ix->D, cudaMemcpyHostToDevice, st));
         ix->x_src = dataset;
         ix->xb_valid = false;
+        ix->kx_valid = false;
     }
     if (!ix->dev_x()) return fail(CULSH_ERR_INVALID_ARGUMENT, "null dataset and no dataset on the device");
     const int D = ix->D, K = s->K;
@@ -1746,6 +1919,15 @@ long long culsh_search_device_bytes(culsh_search* s) {
     add(s->dense_q);
     add(s->qorder);
     add(s->qorder_bins);
+    add(s->kbm);
+    add(s->kq_h);
+    add(s->kq_l);
+    add(s->kq_sq);
+    add(s->kq_base);
+    add(s->kpart_key);
+    add(s->kpart_id);
+    add(s->kpart_n);
+    add(s->kfallback);
     return (long long)b;
 }
 
@@ -1759,6 +1941,15 @@ long long culsh_search_estimate_bytes(const culsh_index* ix, int Q, int K, int T
     b += 16 * q + cap * per_item;   // per-query plan arrays, dense-query list, partial lists
     b += 4 * q + 4 * (kOrderBins + 1);   // locality order
     if (M <= 16) b += 12 * L * q * (size_t)T + 48 * L * q;   // split probe lookups
+    if (ix->D <= 128 && K <= kMaxKnnK) {
+        // tensor-core path for dense queries: membership rows, query rows,
+        // partial lists (at most 160 CTAs' list sets plus one per query tile)
+        const size_t qc = (q + kKnnTileQ - 1) / kKnnTileQ * kKnnTileQ, dp = ((size_t)ix->D + 63) / 64 * 64;
+        const size_t nwp = (((size_t)ix->N + 31) / 32 + 3) / 4 * 4;
+        const size_t lists = (160 + qc / kKnnTileQ) * 2 * kKnnTileQ;
+        const size_t bmb = 4 * qc * nwp;
+        if (bmb <= kKnnMaxBitmapBytes) b += bmb + 4 * qc * dp + 12 * qc + lists * (4 + 8 * (size_t)kMaxKnnK);
+    }
     return (long long)b;
 }
 
@@ -1790,6 +1981,15 @@ int culsh_search_release(culsh_search* s) {
     s->dense_q.release();
     s->qorder.release();
     s->qorder_bins.release();
+    s->kbm.release();
+    s->kq_h.release();
+    s->kq_l.release();
+    s->kq_sq.release();
+    s->kq_base.release();
+    s->kpart_key.release();
+    s->kpart_id.release();
+    s->kpart_n.release();
+    s->kfallback.release();
     s->Q = 0;
     s->searched = false;
     s->qb_host_valid = false;
@@ -1807,6 +2007,8 @@ static void tune_to_c(const SearchTune& t, culsh_tuning* o) {
     o->ws_set_slots = t.ws_slots;
     o->probe_split = t.probe_split;
     o->ws_order = t.ws_order;
+    o->dense_tc = t.dense_tc;
+    o->dense_min = t.dense_min;
 }
 
 int culsh_search_get_tuning(culsh_search* s, culsh_tuning* out) {
@@ -1826,7 +2028,8 @@ int culsh_search_set_tuning(culsh_search* s, const culsh_tuning* in) {
                     in->ws_blocks_per_sm >= 0 && in->ws_blocks_per_sm <= 64 && in->ws_chunk >= 64 &&
                     in->ws_chunk <= 65536 && (in->distance_bf16 == 0 || in->distance_bf16 == 1) &&
                     (in->ws_set_slots == 4096 || in->ws_set_slots == 8192 || in->ws_set_slots == 16384) &&
-                    in->probe_split >= 0 && in->probe_split <= 2 && (in->ws_order == 0 || in->ws_order == 1);
+                    in->probe_split >= 0 && in->probe_split <= 2 && (in->ws_order == 0 || in->ws_order == 1) &&
+                    (in->dense_tc == 0 || in->dense_tc == 1) && in->dense_min >= 0;
     if (!ok) return fail(CULSH_ERR_INVALID_ARGUMENT, "tuning value out of range");
     s->tune.proj_tile = in->proj_tile;
     s->tune.probe_pch = in->probe_batch;
@@ -1838,6 +2041,8 @@ int culsh_search_set_tuning(culsh_search* s, const culsh_tuning* in) {
     s->tune.ws_slots = in->ws_set_slots;
     s->tune.probe_split = in->probe_split;
     s->tune.ws_order = in->ws_order;
+    s->tune.dense_tc = in->dense_tc;
+    s->tune.dense_min = in->dense_min;
     return CULSH_OK;
 }
 
@@ -2002,6 +2207,30 @@ int culsh_search_autotune(culsh_search* s, const float* d_queries, int Q, int* d
             }
         }
     }
+    {
+        // dense queries: tensor-core path or SIMT bitmap kernel, and (tensor
+        // cores) the threshold from which a query is dense
+        const unsigned long long N = (unsigned long long)s->ix->N;
+        const int mins[3] = {0, (int)std::max(1024ull, N / 1024), (int)std::max(1024ull, N / 64)};
+        const SearchTune base_t = best;
+        for (int tc = 0; tc < 2; ++tc)
+            for (int mi = 0; mi < 3; ++mi) {
+                if ((tc == 0 && mi > 0) || (tc == base_t.dense_tc && mins[mi] == base_t.dense_min)) continue;
+                SearchTune t = base_t;
+                t.dense_tc = tc;
+                t.dense_min = mins[mi];
+                s->tune = t;
+                const int rc = measure(stage);
+                if (rc != CULSH_OK) {
+                    s->tune = start;
+                    return rc;
+                }
+                if (stage[2] < best_t) {
+                    best = t;
+                    best_t = stage[2];
+                }
+            }
+    }
     s->tune = best;
     const int rc = measure(stage);
     if (rc != CULSH_OK) return rc;
@@ -2066,6 +2295,8 @@ int culsh_search_profile_get(culsh_search* s, culsh_search_profile* out) {
     out->rechecked = s->rechecked;
     out->dense_queries = s->dense_queries;
     out->host_path = s->host_path;
+    out->knn_queries = s->knn_queries;
+    out->knn_fallback = s->knn_fallback;
     return CULSH_OK;
 }
 

@@ -357,6 +357,80 @@ cudaError_t launch_bf16_rows(const float* X, int64_t N, int D, uint16_t* xb, uin
 cudaError_t launch_plan_items(const WsArgs& a, cudaStream_t st);
 cudaError_t launch_candidates_ws(const WsArgs& a, int grid, cudaStream_t st);
 
+// ---------------------------------------------------------------------------
+// Tensor-core k-NN over candidate membership rows (knn_tc.cu): the dense
+// queries' candidate distances and top-K as a masked GEMM.
+
+// Properties of a set of rows (the dataset, or one search's dense queries),
+// accumulated by k_knn_rows. Zero is the empty state.
+enum KnnFlags : int {
+    kKnnHasLo = 1,         // some value is not exact in bf16
+    kKnnNotSmallInt = 2,   // some value is not an integer of magnitude <= 256
+    kKnnNonFinite = 4,
+};
+struct KnnState {
+    int flags;
+    int mneg;   // max over the small-integer values v of 257 - v (0: none)
+    int mpos;   // max over them of v + 257
+    int pad;
+};
+constexpr int kMaxKnnK = 64;    // list length limit of the tensor-core k-NN path
+constexpr int kKnnTileQ = 128;  // queries per tensor-core tile
+
+// Everything the k-NN kernels of one search read and write.
+struct KnnSearch {
+    int N, D, Dp, K, Qcap;            // Qcap: rows of the query buffers (a multiple of 128)
+    int grid;                          // persistent CTAs of the tensor-core kernels
+    int exact_possible;                // dataset qualifies for the exact form (launch its kernel)
+    int kl_exact, kl_bound;            // list length per query (exact: K; bound: K + margin)
+    int ops_exact, ops_bound;          // point-tile ring stages per form
+    size_t smem_exact, smem_bound;     // dynamic shared memory per form
+    int nwp;                           // membership words per query row (a multiple of 4)
+    float C;                           // bound-form factor (|d~ - d| <= C S)
+    // dataset side (per index)
+    const void* xh;                    // [N][Dp] bf16
+    const void* xl;                    // [N][Dp] bf16
+    const float* w_exact;              // [ntp256 * 256]: |x|^2, FLT_MAX past N
+    const float* w_bound;              // [ntp256 * 256]: |x|^2 - C |x|^2_up, FLT_MAX past N
+    const KnnState* dstate;
+    const float* X;                    // [N][D] f32 (the bound form's exact recomputation)
+    // query side (per search)
+    const float* queries;              // [Q][D] f32
+    const int* dense_q;                // dense list (query ids)
+    const unsigned int* n_dense;
+    void* qh;                          // [Qcap][Dp] bf16, dense-list order
+    void* ql;
+    float* qsq;                        // [Qcap]
+    float* qbase;                      // [Qcap]
+    KnnState* qstate;                  // cleared before the search
+    const uint32_t* bm;                // [Qcap][nwp] membership rows (k_cand_bitmap)
+    float* part_key;                   // partial lists, see k_knn_tc
+    uint32_t* part_id;
+    int* part_n;
+    int32_t* out_ids;
+    float* out_d;
+    int* fallback;                     // [Qcap] queries the bound form could not prove
+    unsigned int* n_fallback;
+    int* err;
+};
+// Buffer sizes of one search (elements).
+size_t knn_part_entries(const KnnSearch& k);   // part_key / part_id entries
+size_t knn_part_lists(const KnnSearch& k);     // part_n entries
+// Plans the shared memory and stages of both forms for D, K on this device;
+// false when the tensor-core path cannot serve them (D > 128, K too large).
+bool knn_plan(KnnSearch& k, int max_smem);
+// The bound-form factor C for dimension D (see knn_tc.cu).
+float knn_bound_factor(int D);
+// Dataset rows: bf16 parts, weights, flags (once per index).
+cudaError_t launch_knn_rows_dataset(const float* X, int64_t N, int D, int Dp, void* xh, void* xl, float* w_exact,
+                                    float* w_bound, int64_t pad, float C, KnnState* st, cudaStream_t s);
+// Query rows, tensor-core kernels and merge of one search (3 or 4 launches).
+cudaError_t launch_knn_search(const KnnSearch& k, cudaStream_t s);
+int knn_launches(const KnnSearch& k);
+// Membership rows of the dense queries (candidates.cu).
+size_t bitmap_smem_bytes(int64_t N);
+cudaError_t launch_cand_bitmap(const WsArgs& a, uint32_t* bm, int nwp, int grid, cudaStream_t st);
+
 // Opts `func` into `dyn` bytes of dynamic shared memory when static plus
 // dynamic shared memory could pass the 48 KB default (the kernels here keep
 // at most 12 KB static). The opted-in size only grows (`cap` records it per

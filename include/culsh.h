@@ -154,6 +154,14 @@ typedef struct culsh_tuning {
     int ws_order;         /* 1: work-stealing items planned in the locality order of the
                              queries' home buckets, so queries that share candidates run
                              together and share rows in L2 (same results as 0)         */
+    int dense_tc;         /* 1: dense queries (see dense_min) take the tensor-core path:
+                             an N-bit candidate membership row per query, then q.x for
+                             all points by tcgen05 GEMM tiles with the top-K kept in the
+                             epilogue, exact distances (same results as 0); 0: the SIMT
+                             bitmap kernel                                              */
+    int dense_min;        /* non-unique candidates from which a query is dense; 0: the
+                             default, max(4096, N/256) for the tensor-core path and
+                             max(32768, N/16) for the SIMT bitmap kernel               */
 } culsh_tuning;
 
 /* Times the search over the tuning space on the caller's queries (device
@@ -218,6 +226,10 @@ typedef struct culsh_search_profile {
                             to the device on the way (L*M <= 192)            */
     int stage_times;     /* 1: the stage times above were measured; 0: stage
                             events off (culsh_search_set_profiling)          */
+    int knn_queries;     /* dense queries served by the tensor-core path     */
+    int knn_fallback;    /* of those, queries whose bound-form lists could not
+                            prove the top-K, re-run by the exact per-query
+                            kernel                                          */
 } culsh_search_profile;
 int culsh_search_profile_get(culsh_search* s, culsh_search_profile* out);
 
