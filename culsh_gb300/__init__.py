@@ -337,7 +337,8 @@ class SearchTables:
     def set_tuning(self, **kw):
         """Sets tuning fields (proj_tile, probe_batch, probe_split,
         candidates_mode, ws_threads, ws_blocks_per_sm, ws_chunk,
-        distance_bf16, ws_set_slots, ws_order); others keep their value."""
+        distance_bf16, ws_set_slots, ws_order, dense_tc, dense_min); others keep
+        their value."""
         t = _Tuning()
         _check(lib().culsh_search_get_tuning(self._h, ctypes.byref(t)))
         for k, v in kw.items():

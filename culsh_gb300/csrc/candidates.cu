@@ -570,14 +570,31 @@ __global__ void __launch_bounds__(DT, 1) k_candidates_dense(WsArgs a) {
 // query's bucket ids (every matched bucket over the L tables and T probes,
 // as the reference's candidate lists, cuLSH_SearchTables.cu:321-364) and
 // copied out once; their count is the query's unique candidate count.
-// Persistent grid, one query per CTA at a time.
-__global__ void __launch_bounds__(DT, 1) k_cand_bitmap(WsArgs a, uint32_t* __restrict__ bm, int nwp) {
+// Persistent grid, one query per CTA at a time, 1024 threads. The matched
+// buckets are cut into units of at most BSEG consecutive ids; warp w takes
+// units w, w + 32, ..., loads 32 x BU ids at a time (coalesced: a bucket's
+// ids are contiguous, BU loads in flight per lane) and ORs their bits in.
+constexpr int BT = 1024;
+constexpr int BU = 8;
+constexpr uint32_t BSEG = 1024;
+constexpr int BCH = 256;   // (table, probe) slots per compaction chunk
+
+struct BitmapSmem {
+    uint64_t base[BCH];     // ids offset of each matched bucket
+    uint32_t size[BCH];
+    uint32_t upre[BCH + 1]; // units before each matched bucket
+    uint32_t n;
+};
+
+__global__ void __launch_bounds__(BT, 1) k_cand_bitmap(WsArgs a, uint32_t* __restrict__ bm, int nwp) {
     extern __shared__ __align__(16) uint32_t bits[];
-    __shared__ GatherSmem<DT, GCH> s_gather;
+    __shared__ BitmapSmem g;
     __shared__ int s_q, s_k;
-    __shared__ unsigned long long s_cnt[DW];
+    __shared__ unsigned long long s_cnt[BT / 32];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int NW = BT / 32;
     const unsigned int ndense = *a.n_dense;
+    const int T = a.T, LT = a.L * a.T;
     for (;;) {
         if (tid == 0) {
             const unsigned int k = atomicAdd(a.dense_next, 1u);
@@ -587,15 +604,79 @@ __global__ void __launch_bounds__(DT, 1) k_cand_bitmap(WsArgs a, uint32_t* __res
         __syncthreads();
         const int q = s_q, k = s_k;
         if (q < 0) break;
-        for (int i = tid; i < nwp; i += DT) bits[i] = 0u;
-        __syncthreads();
-        const BucketView bv{a.qbuckets, a.boff, a.starts, a.sizes, a.ids, a.N, a.L, a.T, a.Q};
-        gather_bucket_ids<DT, GCH>(bv, q, s_gather,
-                                   [&](uint32_t id) { atomicOr(&bits[id >> 5], 1u << (id & 31)); });
-        __syncthreads();
+        for (int i = tid * 4; i < nwp; i += BT * 4) *reinterpret_cast<uint4*>(bits + i) = make_uint4(0u, 0u, 0u, 0u);
+        for (int c0 = 0; c0 < LT; c0 += BCH) {
+            // matched buckets of this chunk of (table, probe) slots, with sizes
+            if (tid == 0) g.n = 0;
+            __syncthreads();
+            const int c1 = min(LT, c0 + BCH);
+            for (int e = c0 + tid; e < c1; e += BT) {
+                const int l = e / T, t = e - l * T;
+                const int32_t j = __ldg(a.qbuckets + (int64_t)l * a.Q * T + (int64_t)q * T + t);
+                if (j >= 0) {
+                    const uint64_t gi = __ldg(a.boff + l) + (uint32_t)j;
+                    const uint32_t st = __ldg(a.starts + gi), sz = __ldg(a.sizes + gi);
+                    if (sz) {
+                        const uint32_t kk = atomicAdd(&g.n, 1u);
+                        g.base[kk] = (uint64_t)l * (uint64_t)a.N + st;
+                        g.size[kk] = sz;
+                    }
+                }
+            }
+            __syncthreads();
+            const uint32_t n = g.n;
+            if (n == 0) continue;   // uniform
+            if (warp == 0) {
+                // exclusive scan of the units per bucket
+                uint32_t carry = 0;
+                for (uint32_t b0 = 0; b0 < n; b0 += 32) {
+                    const uint32_t kk = b0 + lane;
+                    const uint32_t c = kk < n ? (g.size[kk] + BSEG - 1) / BSEG : 0u;
+                    uint32_t x = c;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+                        if (lane >= o) x += y;
+                    }
+                    if (kk < n) g.upre[kk] = carry + x - c;
+                    carry += __shfl_sync(0xffffffffu, x, 31);
+                }
+                if (lane == 0) g.upre[n] = carry;
+            }
+            __syncthreads();
+            const uint32_t units = g.upre[n];
+            for (uint32_t u = warp; u < units; u += NW) {
+                // bucket of unit u: the last b with upre[b] <= u
+                uint32_t lo = 0, hi = n - 1;
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi + 1) >> 1;
+                    if (g.upre[mid] <= u) lo = mid;
+                    else hi = mid - 1;
+                }
+                const uint32_t off = (u - g.upre[lo]) * BSEG;
+                const uint32_t cnt = min(BSEG, g.size[lo] - off);
+                const uint32_t* src = a.ids + g.base[lo] + off;
+                uint32_t j0 = 0;
+                for (; j0 + 32 * BU <= cnt; j0 += 32 * BU) {   // full blocks: BU loads in flight per lane
+                    uint32_t v[BU];
+#pragma unroll
+                    for (int b = 0; b < BU; ++b) v[b] = __ldg(src + j0 + b * 32 + lane);
+#pragma unroll
+                    for (int b = 0; b < BU; ++b) atomicOr(&bits[v[b] >> 5], 1u << (v[b] & 31));
+                }
+                for (; j0 < cnt; j0 += 32) {
+                    const uint32_t j = j0 + lane;
+                    if (j < cnt) {
+                        const uint32_t v = __ldg(src + j);
+                        atomicOr(&bits[v >> 5], 1u << (v & 31));
+                    }
+                }
+            }
+            __syncthreads();
+        }
         uint32_t* row = bm + (int64_t)k * nwp;
         unsigned long long cnt = 0;
-        for (int i = tid * 4; i < nwp; i += DT * 4) {
+        for (int i = tid * 4; i < nwp; i += BT * 4) {
             const uint4 v = *reinterpret_cast<const uint4*>(bits + i);
             *reinterpret_cast<uint4*>(row + i) = v;
             cnt += __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
@@ -606,7 +687,7 @@ __global__ void __launch_bounds__(DT, 1) k_cand_bitmap(WsArgs a, uint32_t* __res
         __syncthreads();
         if (tid == 0) {
             unsigned long long U = 0;
-            for (int w = 0; w < DW; ++w) U += s_cnt[w];
+            for (int w = 0; w < NW; ++w) U += s_cnt[w];
             a.cu[q] = U;
             atomicAdd(a.totals + 0, U);
             atomicAdd(a.totals + 1, a.cnu[q]);
@@ -622,7 +703,7 @@ cudaError_t launch_cand_bitmap(const WsArgs& a, uint32_t* bm, int nwp, int grid,
     const size_t smem = 4 * (size_t)nwp;
     const cudaError_t e = opt_in_smem(k_cand_bitmap, smem, cap);
     if (e != cudaSuccess) return e;
-    k_cand_bitmap<<<grid, DT, smem, st>>>(a, bm, nwp);
+    k_cand_bitmap<<<grid, BT, smem, st>>>(a, bm, nwp);
     return cudaGetLastError();
 }
 

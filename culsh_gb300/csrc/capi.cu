@@ -915,7 +915,7 @@ int plan_knn(culsh_search* s, SearchPlan& P, int Q, int32_t* d_ids, float* d_d, 
     k.N = ix->N;
     k.D = ix->D;
     k.K = s->K;
-    k.Qcap = (Q + kKnnTileQ - 1) / kKnnTileQ * kKnnTileQ;
+    k.Qcap = (Q + 2 * kKnnTileQ - 1) / (2 * kKnnTileQ) * (2 * kKnnTileQ);   // whole 256-query tiles
     k.grid = s->sms;
     if (!knn_plan(k, s->smem_optin)) return CULSH_OK;
     if (bitmap_smem_bytes(ix->N) + 8192 > (size_t)s->smem_optin) return CULSH_OK;
@@ -1944,7 +1944,8 @@ long long culsh_search_estimate_bytes(const culsh_index* ix, int Q, int K, int T
     if (ix->D <= 128 && K <= kMaxKnnK) {
         // tensor-core path for dense queries: membership rows, query rows,
         // partial lists (at most 160 CTAs' list sets plus one per query tile)
-        const size_t qc = (q + kKnnTileQ - 1) / kKnnTileQ * kKnnTileQ, dp = ((size_t)ix->D + 63) / 64 * 64;
+        const size_t qc = (q + 2 * kKnnTileQ - 1) / (2 * kKnnTileQ) * (2 * kKnnTileQ);
+        const size_t dp = ((size_t)ix->D + 63) / 64 * 64;
         const size_t nwp = (((size_t)ix->N + 31) / 32 + 3) / 4 * 4;
         const size_t lists = (160 + qc / kKnnTileQ) * 2 * kKnnTileQ;
         const size_t bmb = 4 * qc * nwp;

@@ -67,7 +67,10 @@
 namespace culsh {
 namespace {
 
-constexpr int KM = 128;                 // queries per tile (TMEM lanes)
+constexpr int KM = 128;                 // rows of one MMA (TMEM lanes)
+constexpr int kBn = 128;                // points per tile
+constexpr int kMqExact = 256;           // queries per tile, exact form (two MMAs share a point tile)
+constexpr int kMqBound = 128;           // queries per tile, bound form (three products per element)
 constexpr uint32_t kKnnPoll = 1u << 26;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -160,6 +163,64 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// The 128 accumulator columns [taddr, taddr + 128) of this thread's TMEM lane,
+// loaded and waited for in one statement, so that no use of r can be
+// scheduled before the wait.
+__device__ __forceinline__ void tmem_ld128(uint32_t taddr, uint32_t (&r)[128]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%128];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%32, %33, %34, %35, %36, %37, %38, %39, %40, %41, %42, %43, %44, "
+        "%45, %46, %47, %48, %49, %50, %51, %52, %53, %54, %55, %56, %57, %58, %59, %60, %61, %62, %63}, [%128+32];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%64, %65, %66, %67, %68, %69, %70, %71, %72, %73, %74, %75, %76, "
+        "%77, %78, %79, %80, %81, %82, %83, %84, %85, %86, %87, %88, %89, %90, %91, %92, %93, %94, %95}, [%128+64];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%96, %97, %98, %99, %100, %101, %102, %103, %104, %105, %106, %107, "
+        "%108, %109, %110, %111, %112, %113, %114, %115, %116, %117, %118, %119, %120, %121, %122, %123, %124, %125, "
+        "%126, %127}, [%128+96];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]),
+          "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]),
+          "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]),
+          "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]), "=r"(r[56]),
+          "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63]), "=r"(r[64]),
+          "=r"(r[65]), "=r"(r[66]), "=r"(r[67]), "=r"(r[68]), "=r"(r[69]), "=r"(r[70]), "=r"(r[71]), "=r"(r[72]),
+          "=r"(r[73]), "=r"(r[74]), "=r"(r[75]), "=r"(r[76]), "=r"(r[77]), "=r"(r[78]), "=r"(r[79]), "=r"(r[80]),
+          "=r"(r[81]), "=r"(r[82]), "=r"(r[83]), "=r"(r[84]), "=r"(r[85]), "=r"(r[86]), "=r"(r[87]), "=r"(r[88]),
+          "=r"(r[89]), "=r"(r[90]), "=r"(r[91]), "=r"(r[92]), "=r"(r[93]), "=r"(r[94]), "=r"(r[95]), "=r"(r[96]),
+          "=r"(r[97]), "=r"(r[98]), "=r"(r[99]), "=r"(r[100]), "=r"(r[101]), "=r"(r[102]), "=r"(r[103]),
+          "=r"(r[104]), "=r"(r[105]), "=r"(r[106]), "=r"(r[107]), "=r"(r[108]), "=r"(r[109]), "=r"(r[110]),
+          "=r"(r[111]), "=r"(r[112]), "=r"(r[113]), "=r"(r[114]), "=r"(r[115]), "=r"(r[116]), "=r"(r[117]),
+          "=r"(r[118]), "=r"(r[119]), "=r"(r[120]), "=r"(r[121]), "=r"(r[122]), "=r"(r[123]), "=r"(r[124]),
+          "=r"(r[125]), "=r"(r[126]), "=r"(r[127])
+        : "r"(taddr)
+        : "memory");
+}
+
+// Element k (0..31) of 32 register values, by a tree of selects on k's bits
+// (no local memory).
+__device__ __forceinline__ float select32(const uint32_t* v, int k) {
+    float a[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) a[i] = __uint_as_float((k & 1) ? v[2 * i + 1] : v[2 * i]);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[i] = (k & 2) ? a[2 * i + 1] : a[2 * i];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) a[i] = (k & 4) ? a[2 * i + 1] : a[2 * i];
+#pragma unroll
+    for (int i = 0; i < 2; ++i) a[i] = (k & 8) ? a[2 * i + 1] : a[2 * i];
+    return (k & 16) ? a[1] : a[0];
+}
+
+// Three-input minimum (sm_100 and later).
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
 // Exact form of the search (see the file comment), from the flags and value
 // ranges of the dataset and of the dense queries.
 __device__ __forceinline__ bool exact_form(const KnnState* ds, const KnnState* qs, int D) {
@@ -194,19 +255,22 @@ __device__ __forceinline__ int owner_cta(long long p, long long U, int G) {
     return (int)(((p + 1) * G - 1) / U);
 }
 
-template <int BN, int NEPI, bool kExact>
+// MQ queries per tile (MQ / 128 MMAs of M = 128 share each point tile of BN
+// points), NEPI epilogue warps (one query each per lane: 32 * NEPI == MQ).
+template <int BN, int MQ, int NEPI, bool kExact>
 __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
     k_knn_tc(const __grid_constant__ CUtensorMap tm_qh, const __grid_constant__ CUtensorMap tm_ql,
              const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CUtensorMap tm_xl,
              const __grid_constant__ CUtensorMap tm_bm, KnnArgs a) {
-    constexpr int NT = 32 * NEPI;          // list-keeping threads
-    constexpr int NH = kExact ? 2 : 1;     // column halves (exact form: two warps per lane quadrant)
+    constexpr int NT = 32 * NEPI;          // list-keeping threads, one query each
+    constexpr int MH = MQ / KM;            // M = 128 halves of the query tile
     constexpr int BW = BN / 32;            // membership words per query row and point tile
-    constexpr uint32_t kTmemCols = 2 * BN;
+    constexpr uint32_t kTmemCols = 2 * MH * BN;
+    static_assert(NT == MQ && BW == 4, "one list per query; four membership words per tile row");
     // the other form's kernel runs (the exact one only where it was launched)
     if ((a.exact_launched && exact_form(a.dstate, a.qstate, a.D)) != kExact) return;
     const unsigned int nd = *a.n_dense;
-    const long long nqt = ((long long)nd + KM - 1) / KM;
+    const long long nqt = ((long long)nd + MQ - 1) / MQ;
     const long long ntp = kExact ? a.ntp_exact : a.ntp_bound;
     const long long U = nqt * ntp;
     const int G = (int)min((long long)gridDim.x, U);
@@ -220,13 +284,13 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
 
     extern __shared__ __align__(1024) unsigned char smraw[];
     unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
-    const uint32_t qbytes = (uint32_t)KM * Dp * 2, xbytes = (uint32_t)BN * Dp * 2;
+    const uint32_t qbytes = (uint32_t)MQ * Dp * 2, xbytes = (uint32_t)BN * Dp * 2;
     unsigned char* sQh = base;
     unsigned char* sQl = sQh + qbytes;                                  // bound form only
     unsigned char* sX = sQh + (kExact ? 1u : 2u) * qbytes;             // op ring: [xh][xl] per stage
     const uint32_t op_stride = (kExact ? 1u : 2u) * xbytes;
     unsigned char* sE = sX + (size_t)ops * op_stride;                  // ep ring: [membership][weights] per stage
-    const uint32_t bm_bytes = (uint32_t)KM * BW * 4, w_bytes = (uint32_t)BN * 4;
+    const uint32_t bm_bytes = (uint32_t)MQ * BW * 4, w_bytes = (uint32_t)BN * 4;
     const uint32_t ep_stride = bm_bytes + w_bytes;
     float* lkey = reinterpret_cast<float*>(sE + (size_t)eps * ep_stride);   // [Kl][NT]
     uint32_t* lid = reinterpret_cast<uint32_t*>(lkey + (size_t)Kl * NT);
@@ -287,8 +351,8 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
                 if (j >= 1 && !bar_wait(a_empty, (uint32_t)((j - 1) & 1), abort_flag, a.err, true)) break;
                 bar_expect_tx(a_full, qbytes * (need_ql ? 2u : 1u));
                 for (int k = 0; k < atoms; ++k) {
-                    tma_2d(sQh + (size_t)k * KM * 128, &tm_qh, a_full, k * 64, (int)(qt * KM));
-                    if (need_ql) tma_2d(sQl + (size_t)k * KM * 128, &tm_ql, a_full, k * 64, (int)(qt * KM));
+                    tma_2d(sQh + (size_t)k * MQ * 128, &tm_qh, a_full, k * 64, (int)(qt * MQ));
+                    if (need_ql) tma_2d(sQl + (size_t)k * MQ * 128, &tm_ql, a_full, k * 64, (int)(qt * MQ));
                 }
             }
             const int s = (int)(i % ops);
@@ -303,7 +367,7 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
             if (i >= eps && !bar_wait(empty_ep + e, (uint32_t)((i / eps - 1) & 1), abort_flag, a.err, true)) break;
             unsigned char* es = sE + (size_t)e * ep_stride;
             bar_expect_tx(full_ep + e, ep_stride);
-            tma_2d(es, &tm_bm, full_ep + e, (int)(pt * BW), (int)(qt * KM));
+            tma_2d(es, &tm_bm, full_ep + e, (int)(pt * BW), (int)(qt * MQ));
             bulk_copy(es + bm_bytes, (kExact ? a.w_exact : a.w_bound) + pt * BN, w_bytes, full_ep + e);
         }
         // Drain: every copy issued into a ring stage completes before exit.
@@ -338,16 +402,18 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
             const int s = (int)(i % ops);
             if (!bar_wait(full_op + s, (uint32_t)((i / ops) & 1), abort_flag, a.err, true)) break;
             fence_after();
-            const uint32_t d = tmem + (uint32_t)(acc * BN);
             const uint32_t qh = smem_addr(sQh), ql = smem_addr(sQl);
             const uint32_t xh = smem_addr(sX + (size_t)s * op_stride), xl = xh + xbytes;
-            for (int ks = 0; ks < ksteps; ++ks) {
-                const uint32_t ao = (uint32_t)((ks >> 2) * KM * 128 + (ks & 3) * 32);
-                const uint32_t bo = (uint32_t)((ks >> 2) * BN * 128 + (ks & 3) * 32);
-                mma_bf16(d, desc_sw128(qh + ao), desc_sw128(xh + bo), idesc, ks > 0 ? 1u : 0u);
-                if (!kExact) {
-                    if (need_xl) mma_bf16(d, desc_sw128(qh + ao), desc_sw128(xl + bo), idesc, 1u);
-                    if (need_ql) mma_bf16(d, desc_sw128(ql + ao), desc_sw128(xh + bo), idesc, 1u);
+            for (int hq = 0; hq < MH; ++hq) {
+                const uint32_t d = tmem + (uint32_t)((acc * MH + hq) * BN);
+                for (int ks = 0; ks < ksteps; ++ks) {
+                    const uint32_t ao = (uint32_t)((ks >> 2) * MQ * 128 + hq * KM * 128 + (ks & 3) * 32);
+                    const uint32_t bo = (uint32_t)((ks >> 2) * BN * 128 + (ks & 3) * 32);
+                    mma_bf16(d, desc_sw128(qh + ao), desc_sw128(xh + bo), idesc, ks > 0 ? 1u : 0u);
+                    if (!kExact) {
+                        if (need_xl) mma_bf16(d, desc_sw128(qh + ao), desc_sw128(xl + bo), idesc, 1u);
+                        if (need_ql) mma_bf16(d, desc_sw128(ql + ao), desc_sw128(xh + bo), idesc, 1u);
+                    }
                 }
             }
             mma_commit(empty_op + s);
@@ -360,8 +426,8 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
         // ---- epilogue: ranking keys, per-query lists ----
         const int ew = warp - 2;
         const int quad = warp & 3;
-        const int half = NH == 2 ? (ew >> 2) : 0;
-        const int row = quad * 32 + lane;
+        const int hq = ew >> 2;                       // query half (its own accumulator)
+        const int row = hq * KM + quad * 32 + lane;   // query of the tile
         const int lt = ew * 32 + lane;
         float* mk = lkey + lt;
         uint32_t* mi = lid + lt;
@@ -371,12 +437,12 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
         long long i = 0;
         auto flush = [&](long long qt) {
             const long long set = (long long)blockIdx.x + qt;
-            const long long lb = (set * NH + half) * (long long)Kl;
+            const long long lb = set * (long long)Kl;
             for (int k = 0; k < n; ++k) {
-                a.part_key[(lb + k) * KM + row] = mk[k * NT];
-                a.part_id[(lb + k) * KM + row] = mi[k * NT];
+                a.part_key[(lb + k) * MQ + row] = mk[k * NT];
+                a.part_id[(lb + k) * MQ + row] = mi[k * NT];
             }
-            a.part_n[(set * NH + half) * KM + row] = n;
+            a.part_n[set * MQ + row] = n;
         };
         for (long long p = p0; p < p1; ++p, ++i) {
             const long long qt = p / ntp, pt = p - qt * ntp;
@@ -395,54 +461,61 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
             if (!__all_sync(0xffffffffu, ok)) break;
             fence_after();
             const unsigned char* es = sE + (size_t)e * ep_stride;
-            const uint4 mw = *reinterpret_cast<const uint4*>(es + (size_t)row * BW * 4 + half * 16);
-            const float* wv = reinterpret_cast<const float*>(es + bm_bytes) + half * 128;
-            const uint32_t id0 = (uint32_t)(pt * BN + half * 128);
-            const uint32_t tbase = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(acc * BN + half * 128);
-#pragma unroll 1
+            const uint4 mw = *reinterpret_cast<const uint4*>(es + (size_t)row * BW * 4);
+            const float* wv = reinterpret_cast<const float*>(es + bm_bytes);
+            const uint32_t id0 = (uint32_t)(pt * BN);
+            const uint32_t tbase = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)((acc * MH + hq) * BN);
+            uint32_t r[128];
+            tmem_ld128(tbase, r);
+            // keys t = w - 2 q.x (packed FMA, in place)
+#pragma unroll
+            for (int j = 0; j < 128; j += 4) {
+                const float4 w4 = *reinterpret_cast<const float4*>(wv + j);
+                const float2 a = __ffma2_rn(make_float2(-2.0f, -2.0f),
+                                            make_float2(__uint_as_float(r[j]), __uint_as_float(r[j + 1])),
+                                            make_float2(w4.x, w4.y));
+                const float2 b = __ffma2_rn(make_float2(-2.0f, -2.0f),
+                                            make_float2(__uint_as_float(r[j + 2]), __uint_as_float(r[j + 3])),
+                                            make_float2(w4.z, w4.w));
+                r[j] = __float_as_uint(a.x);
+                r[j + 1] = __float_as_uint(a.y);
+                r[j + 2] = __float_as_uint(b.x);
+                r[j + 3] = __float_as_uint(b.y);
+            }
+#pragma unroll
             for (int c = 0; c < 4; ++c) {
-                uint32_t r[32];
-                __syncwarp();   // lanes that took the insert path rejoin before the warp-wide load
-                tmem_ld32(tbase + (uint32_t)(c * 32), r);
                 const uint32_t mbits = c == 0 ? mw.x : c == 1 ? mw.y : c == 2 ? mw.z : mw.w;
-                float t[32];
+                const uint32_t* rc = r + c * 32;
+                float mm[11];
 #pragma unroll
-                for (int q4 = 0; q4 < 8; ++q4) {
-                    const float4 w4 = *reinterpret_cast<const float4*>(wv + c * 32 + q4 * 4);
-                    t[q4 * 4 + 0] = __fmaf_rn(-2.0f, __uint_as_float(r[q4 * 4 + 0]), w4.x);
-                    t[q4 * 4 + 1] = __fmaf_rn(-2.0f, __uint_as_float(r[q4 * 4 + 1]), w4.y);
-                    t[q4 * 4 + 2] = __fmaf_rn(-2.0f, __uint_as_float(r[q4 * 4 + 2]), w4.z);
-                    t[q4 * 4 + 3] = __fmaf_rn(-2.0f, __uint_as_float(r[q4 * 4 + 3]), w4.w);
-                }
-                float m = t[0];
-#pragma unroll
-                for (int k = 1; k < 32; ++k) m = fminf(m, t[k]);
+                for (int k = 0; k < 10; ++k)
+                    mm[k] = fmin3(__uint_as_float(rc[3 * k]), __uint_as_float(rc[3 * k + 1]), __uint_as_float(rc[3 * k + 2]));
+                mm[10] = fminf(__uint_as_float(rc[30]), __uint_as_float(rc[31]));
+                const float m = fmin3(fmin3(mm[0], mm[1], mm[2]), fmin3(mm[3], mm[4], mm[5]),
+                                      fmin3(fmin3(mm[6], mm[7], mm[8]), mm[9], mm[10]));
                 if (m < thr && mbits) {
+                    // this lane's candidate columns whose key beats its list;
+                    // lanes insert in parallel, each into its own sorted list
                     uint32_t pm = 0;
 #pragma unroll
-                    for (int k = 0; k < 32; ++k) pm |= (t[k] < thr ? 1u : 0u) << k;
+                    for (int k = 0; k < 32; ++k) pm |= (__uint_as_float(rc[k]) < thr ? 1u : 0u) << k;
                     pm &= mbits;
-                    if (pm) {
-                        float sp[32];
-#pragma unroll
-                        for (int k = 0; k < 32; ++k) sp[k] = t[k];
-                        for (; pm; pm &= pm - 1) {
-                            const int k = __ffs((int)pm) - 1;
-                            const float key = sp[k];
-                            if (!(key < thr)) continue;
-                            // sorted insert: ids arrive in ascending order, so a key
-                            // equal to a listed one goes after it
-                            int pos = n < Kl ? n : Kl - 1;
-                            while (pos > 0 && mk[(pos - 1) * NT] > key) {
-                                mk[pos * NT] = mk[(pos - 1) * NT];
-                                mi[pos * NT] = mi[(pos - 1) * NT];
-                                --pos;
-                            }
-                            mk[pos * NT] = key;
-                            mi[pos * NT] = id0 + (uint32_t)(c * 32 + k);
-                            if (n < Kl) ++n;
-                            if (n == Kl) thr = mk[(Kl - 1) * NT];
+                    for (; pm; pm &= pm - 1) {
+                        const int k = __ffs((int)pm) - 1;
+                        const float key = select32(rc, k);
+                        if (!(key < thr)) continue;
+                        // ids arrive in ascending order, so a key equal to a
+                        // listed one goes after it
+                        int pos = n < Kl ? n : Kl - 1;
+                        while (pos > 0 && mk[(pos - 1) * NT] > key) {
+                            mk[pos * NT] = mk[(pos - 1) * NT];
+                            mi[pos * NT] = mi[(pos - 1) * NT];
+                            --pos;
                         }
+                        mk[pos * NT] = key;
+                        mi[pos * NT] = id0 + (uint32_t)(c * 32 + k);
+                        if (n < Kl) ++n;
+                        if (n == Kl) thr = mk[(Kl - 1) * NT];
                     }
                 }
             }
@@ -561,6 +634,7 @@ __device__ __forceinline__ float lane_order_distance(const float* __restrict__ q
 }
 
 constexpr int MERGE_WARPS = 4;
+constexpr int kEpStages = 4;   // membership / weight ring stages
 
 // Merges the partial lists of each dense query into its top-K (one warp per
 // query). Lists are walked in ascending key order and left as soon as the
@@ -575,19 +649,18 @@ __global__ void __launch_bounds__(32 * MERGE_WARPS) k_knn_merge(KnnSearch k) {
     const unsigned int nd = *k.n_dense;
     const bool exact = k.exact_possible && exact_form(k.dstate, k.qstate, k.D);
     const int K = k.K;
-    const int NH = exact ? 2 : 1;
     const int Kl = exact ? k.kl_exact : k.kl_bound;
-    const int BN = exact ? 256 : 128;
-    const long long ntp = (k.N + BN - 1) / BN;
-    const long long nqt = ((long long)nd + KM - 1) / KM;
+    const int MQ = exact ? kMqExact : kMqBound;
+    const long long ntp = (k.N + kBn - 1) / kBn;
+    const long long nqt = ((long long)nd + MQ - 1) / MQ;
     const long long U = nqt * ntp;
     const int G = (int)min((long long)k.grid, U);
     float* wd = s_d[w];
     uint32_t* wi = s_i[w];
     for (long long i = (long long)blockIdx.x * MERGE_WARPS + w; i < nd; i += (long long)gridDim.x * MERGE_WARPS) {
         const int q = k.dense_q[i];
-        const long long qt = i / KM;
-        const int r = (int)(i - qt * KM);
+        const long long qt = i / MQ;
+        const int r = (int)(i - qt * MQ);
         const int c0 = owner_cta(qt * ntp, U, G), c1 = owner_cta(qt * ntp + ntp - 1, U, G);
         const float base = exact ? k.qsq[i] : k.qbase[i];
         const float* qrow = k.queries + (int64_t)q * k.D;
@@ -596,17 +669,17 @@ __global__ void __launch_bounds__(32 * MERGE_WARPS) k_knn_merge(KnnSearch k) {
         uint32_t thr_i = 0;
         float minlast = INFINITY;   // smallest last bound over the full lists
         for (int c = c0; c <= c1; ++c) {
-            for (int h = 0; h < NH; ++h) {
-                const long long lst = ((long long)c + qt) * NH + h;
-                const int cnt = k.part_n[lst * KM + r];
+            {
+                const long long lst = (long long)c + qt;
+                const int cnt = k.part_n[lst * MQ + r];
                 const long long lb = lst * (long long)Kl;
                 if (!exact && cnt == Kl)
-                    minlast = fminf(minlast, __fadd_rd(k.part_key[(lb + Kl - 1) * KM + r], base));
+                    minlast = fminf(minlast, __fadd_rd(k.part_key[(lb + Kl - 1) * MQ + r], base));
                 for (int e0 = 0; e0 < cnt; e0 += 32) {
                     const int e = e0 + lane;
                     const bool valid = e < cnt;
-                    const float key = valid ? k.part_key[(lb + e) * KM + r] : INFINITY;
-                    const uint32_t id = valid ? k.part_id[(lb + e) * KM + r] : 0u;
+                    const float key = valid ? k.part_key[(lb + e) * MQ + r] : INFINITY;
+                    const uint32_t id = valid ? k.part_id[(lb + e) * MQ + r] : 0u;
                     const float low = exact ? __fadd_rn(key, base) : __fadd_rd(key, base);
                     // entries are in ascending key order: lane 0 holds the chunk's smallest
                     if (__shfl_sync(0xffffffffu, low, 0) > thr_d) break;
@@ -674,41 +747,43 @@ bool knn_map(CUtensorMap* m, const void* ptr, CUtensorMapDataType dt, int esize,
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-size_t knn_smem(int BN, bool exact, int Dp, int Kl, int ops, int eps) {
-    const int nepi = exact ? 8 : 4;
-    const size_t q = (size_t)KM * Dp * 2 * (exact ? 1 : 2);
-    const size_t op = (size_t)BN * Dp * 2 * (exact ? 1 : 2);
-    const size_t ep = (size_t)KM * (BN / 32) * 4 + (size_t)BN * 4;
-    const size_t lists = (size_t)32 * nepi * Kl * 8;
+size_t knn_smem(bool exact, int Dp, int Kl, int ops, int eps) {
+    const int MQ = exact ? kMqExact : kMqBound;
+    const size_t q = (size_t)MQ * Dp * 2 * (exact ? 1 : 2);
+    const size_t op = (size_t)kBn * Dp * 2 * (exact ? 1 : 2);
+    const size_t ep = (size_t)MQ * (kBn / 32) * 4 + (size_t)kBn * 4;
+    const size_t lists = (size_t)MQ * Kl * 8;
     const size_t bars = 8 * (7 + 2 * ops + 2 * eps) + 16;
     return 1024 + q + ops * op + eps * ep + lists + bars;
 }
 
-template <int BN, int NEPI, bool kExact>
-cudaError_t launch_knn_form(const KnnSearch& k, const CUtensorMap& mqh, const CUtensorMap& mql,
-                            const CUtensorMap& mxh, const CUtensorMap& mxl, cudaStream_t s) {
+template <int MQ, int NEPI, bool kExact>
+cudaError_t launch_knn_form(const KnnSearch& k, const CUtensorMap& mxh, const CUtensorMap& mxl, cudaStream_t s) {
     static std::atomic<size_t> cap{0};
     const size_t smem = kExact ? k.smem_exact : k.smem_bound;
     if (smem > cap.load()) {
-        const cudaError_t e = cudaFuncSetAttribute(k_knn_tc<BN, NEPI, kExact>,
+        const cudaError_t e = cudaFuncSetAttribute(k_knn_tc<kBn, MQ, NEPI, kExact>,
                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         cap = smem;
     }
-    CUtensorMap mbm;
-    if (!knn_map(&mbm, k.bm, CU_TENSOR_MAP_DATA_TYPE_UINT32, 4, (uint64_t)k.nwp, (uint64_t)k.Qcap, BN / 32, KM, false))
+    CUtensorMap mbm, mqh, mql;
+    if (!knn_map(&mbm, k.bm, CU_TENSOR_MAP_DATA_TYPE_UINT32, 4, (uint64_t)k.nwp, (uint64_t)k.Qcap, kBn / 32, MQ,
+                 false) ||
+        !knn_map(&mqh, k.qh, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (uint64_t)k.Dp, (uint64_t)k.Qcap, 64, MQ, true) ||
+        !knn_map(&mql, k.ql, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (uint64_t)k.Dp, (uint64_t)k.Qcap, 64, MQ, true))
         return cudaErrorNotSupported;
     KnnArgs a;
     a.N = k.N;
     a.D = k.D;
     a.Dp = k.Dp;
     a.exact_launched = k.exact_possible;
-    a.ntp_exact = (k.N + 255) / 256;
-    a.ntp_bound = (k.N + 127) / 128;
+    a.ntp_exact = (k.N + kBn - 1) / kBn;
+    a.ntp_bound = (k.N + kBn - 1) / kBn;
     a.kl_exact = k.kl_exact;
     a.kl_bound = k.kl_bound;
     a.op_stages = kExact ? k.ops_exact : k.ops_bound;
-    a.ep_stages = 4;
+    a.ep_stages = kEpStages;
     a.n_dense = k.n_dense;
     a.dstate = k.dstate;
     a.qstate = k.qstate;
@@ -718,7 +793,7 @@ cudaError_t launch_knn_form(const KnnSearch& k, const CUtensorMap& mqh, const CU
     a.part_id = k.part_id;
     a.part_n = k.part_n;
     a.err = k.err;
-    k_knn_tc<BN, NEPI, kExact><<<k.grid, 64 + 32 * NEPI, smem, s>>>(mqh, mql, mxh, mxl, mbm, a);
+    k_knn_tc<kBn, MQ, NEPI, kExact><<<k.grid, 64 + 32 * NEPI, smem, s>>>(mqh, mql, mxh, mxl, mbm, a);
     return cudaGetLastError();
 }
 
@@ -747,15 +822,16 @@ bool knn_plan(KnnSearch& k, int max_smem) {
     if (const char* e = getenv("CULSH_KNN_LIST_MARGIN")) margin = std::max(0, atoi(e));
     k.kl_bound = std::min(kMaxKnnK, k.K + margin);
     k.ops_exact = k.ops_bound = 0;
-    for (int ops = 2; ops >= 1 && !k.ops_exact; --ops) {
-        const size_t sm = knn_smem(256, true, k.Dp, k.kl_exact, ops, 4);
+    // the deepest point-tile ring (1 to 4 stages) that fits
+    for (int ops = 4; ops >= 1 && !k.ops_exact; --ops) {
+        const size_t sm = knn_smem(true, k.Dp, k.kl_exact, ops, kEpStages);
         if (sm <= (size_t)max_smem) {
             k.ops_exact = ops;
             k.smem_exact = sm;
         }
     }
-    for (int ops = 2; ops >= 1 && !k.ops_bound; --ops) {
-        const size_t sm = knn_smem(128, false, k.Dp, k.kl_bound, ops, 4);
+    for (int ops = 4; ops >= 1 && !k.ops_bound; --ops) {
+        const size_t sm = knn_smem(false, k.Dp, k.kl_bound, ops, kEpStages);
         if (sm <= (size_t)max_smem) {
             k.ops_bound = ops;
             k.smem_bound = sm;
@@ -769,8 +845,9 @@ bool knn_plan(KnnSearch& k, int max_smem) {
 }
 
 size_t knn_part_lists(const KnnSearch& k) {
-    // list sets blockIdx.x + query tile < grid + Qcap / 128; two halves in the exact form
-    return (size_t)(k.grid + k.Qcap / KM) * 2 * KM;
+    // list sets blockIdx.x + query tile < grid + Qcap / MQ, MQ rows each:
+    // at most (grid + Qcap / 128) * 256 in either form
+    return (size_t)(k.grid + k.Qcap / KM) * kMqExact;
 }
 size_t knn_part_entries(const KnnSearch& k) {
     return knn_part_lists(k) * (size_t)std::max(k.kl_exact, k.kl_bound);
@@ -789,25 +866,20 @@ int knn_launches(const KnnSearch& k) { return 3 + (k.exact_possible ? 1 : 0); }
 cudaError_t launch_knn_search(const KnnSearch& k, cudaStream_t s) {
     // query rows in dense-list order, zero rows up to the next tile
     const int qblocks = (int)std::min<int64_t>(((int64_t)k.Qcap * 32 + 255) / 256, 152 * 8);
-    k_knn_rows<<<qblocks, 256, 0, s>>>(k.queries, k.D, k.Dp, k.dense_q, k.n_dense, 0, 0, KM,
+    k_knn_rows<<<qblocks, 256, 0, s>>>(k.queries, k.D, k.Dp, k.dense_q, k.n_dense, 0, 0, kMqExact,
                                        static_cast<__nv_bfloat16*>(k.qh), static_cast<__nv_bfloat16*>(k.ql), k.qsq,
                                        k.qbase, k.C, k.qstate);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    CUtensorMap mqh, mql, mxh, mxl;
-    if (!knn_map(&mqh, k.qh, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (uint64_t)k.Dp, (uint64_t)k.Qcap, 64, KM, true) ||
-        !knn_map(&mql, k.ql, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (uint64_t)k.Dp, (uint64_t)k.Qcap, 64, KM, true))
+    CUtensorMap mxh, mxl;
+    if (!knn_map(&mxh, k.xh, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (uint64_t)k.Dp, (uint64_t)k.N, 64, kBn, true) ||
+        !knn_map(&mxl, k.xl, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (uint64_t)k.Dp, (uint64_t)k.N, 64, kBn, true))
         return cudaErrorNotSupported;
     if (k.exact_possible) {
-        if (!knn_map(&mxh, k.xh, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (uint64_t)k.Dp, (uint64_t)k.N, 64, 256, true))
-            return cudaErrorNotSupported;
-        e = launch_knn_form<256, 8, true>(k, mqh, mql, mxh, mxh, s);
+        e = launch_knn_form<kMqExact, 8, true>(k, mxh, mxh, s);
         if (e != cudaSuccess) return e;
     }
-    if (!knn_map(&mxh, k.xh, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (uint64_t)k.Dp, (uint64_t)k.N, 64, 128, true) ||
-        !knn_map(&mxl, k.xl, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (uint64_t)k.Dp, (uint64_t)k.N, 64, 128, true))
-        return cudaErrorNotSupported;
-    e = launch_knn_form<128, 4, false>(k, mqh, mql, mxh, mxl, s);
+    e = launch_knn_form<kMqBound, 4, false>(k, mxh, mxl, s);
     if (e != cudaSuccess) return e;
     const int mblocks = (int)std::min<int64_t>(((int64_t)k.Qcap + MERGE_WARPS - 1) / MERGE_WARPS, 152 * 16);
     k_knn_merge<<<mblocks, 32 * MERGE_WARPS, 0, s>>>(k);

@@ -108,7 +108,7 @@ def test_bf16_distance_form_is_exact(culsh, name):
     ht = build_index(culsh, c)
     st = culsh.SearchTables()
     st.reset(ht, int(c["K"]), int(c["T"]))
-    st.set_tuning(candidates_mode=1, distance_bf16=1)
+    st.set_tuning(candidates_mode=1, distance_bf16=1, dense_tc=0)   # dense queries: SIMT, not tensor cores
     st.search(c["queries"], dataset=c["X"])
     check_search(st, c)
     np.testing.assert_array_equal(st.getKnnDistances(), c["knn_dists"])
@@ -143,8 +143,10 @@ def test_bf16_form_extreme_magnitudes_and_ties(culsh):
     ref = oracle.search(oracle.build_index(X, A, b, W), X, queries, K, T)
     st = culsh.SearchTables()
     st.reset(ht, K, T)
-    for bf in (0, 1):
-        st.set_tuning(candidates_mode=1, distance_bf16=bf)
+    # the work-stealing forms (dense queries on the SIMT kernels), then the
+    # tensor-core path for the dense queries
+    for bf, tc in ((0, 0), (1, 0), (0, 1)):
+        st.set_tuning(candidates_mode=1, distance_bf16=bf, dense_tc=tc)
         st.search(queries, dataset=X)
         np.testing.assert_array_equal(st.getKnnIds(), ref["knn_ids"])
         np.testing.assert_array_equal(st.getKnnDistances(), ref["knn_dists"])

@@ -352,6 +352,7 @@ def test_work_stealing_partitions_and_overflow_reruns(culsh, monkeypatch):
     ht = build_index(culsh, c)
     st = culsh.SearchTables()
     st.reset(ht, int(c["K"]), int(c["T"]))
+    st.set_tuning(dense_tc=0)   # every query with candidates in work-stealing partitions
     st.search(c["queries"], dataset=c["X"])
     check_search(st, c)
     assert st.profile()["candidates_mode"] == 1
@@ -404,6 +405,12 @@ def test_work_stealing_large_candidate_sets(culsh):
     np.testing.assert_array_equal(st.getKnnDistances(), ref["knn_dists"])
     # the bitmap kernel computes FP32 distances; partitions stay for the rest
     assert st.profile()["dense_queries"] == 8
+    # dense queries on the SIMT bitmap kernel instead of the tensor cores
+    st.set_tuning(distance_bf16=0, dense_tc=0)
+    st.search(queries, dataset=X)
+    np.testing.assert_array_equal(st.getKnnIds(), ref["knn_ids"])
+    np.testing.assert_array_equal(st.getKnnDistances(), ref["knn_dists"])
+    assert st.profile()["dense_queries"] == 8 and st.profile()["knn_queries"] == 0
 
 
 @pytest.mark.parametrize("name", golden_cases())
@@ -415,6 +422,7 @@ def test_dense_bitmap_candidates_kernel(culsh, name, monkeypatch):
     ht = build_index(culsh, c)
     st = culsh.SearchTables()
     st.reset(ht, int(c["K"]), int(c["T"]))
+    st.set_tuning(dense_tc=0)   # the SIMT bitmap kernel (test_gpu_knn_tc.py covers the tensor cores)
     st.search(c["queries"], dataset=c["X"])
     check_search(st, c)
     np.testing.assert_array_equal(st.getKnnDistances(), c["knn_dists"])
