@@ -220,7 +220,8 @@ struct culsh_search {
     unsigned long long tot_unique = 0, tot_nonunique = 0;
     culsh_times times{};
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    // stage boundaries: [0..3] search stages, [4] host copy done, [5] membership rows done
+    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     int launches = 0, deferred_queries = 0;
     bool host_copy_timed = false;
     DevBuf<float> dq, vals, od;
@@ -864,7 +865,7 @@ struct SearchPlan {
     unsigned long long* stats;
     unsigned long long* h_stats;
     unsigned long long* cnu;
-    cudaEvent_t ev[4];
+    cudaEvent_t ev[5];  // stage boundaries; ev[4]: membership rows done (tensor-core path)
     int stage_events;   // 0: no stage events in the graph (they cost a few microseconds each)
 };
 
@@ -1202,6 +1203,7 @@ int plan_search(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* 
     P.h_stats = s->h_stats.p;
     P.cnu = s->cnu.p;
     for (int i = 0; i < 4; ++i) P.ev[i] = s->ev[i];
+    P.ev[4] = s->ev[5];
     P.stage_events = s->stage_events ? 1 : 0;
     return CULSH_OK;
 }
@@ -1229,6 +1231,7 @@ int enqueue_search(const SearchPlan& P, cudaStream_t st, bool capturing, int* la
         CU_TRY(launch_candidates_ws(P.wa, P.ws_grid, st));
         if (P.use_knn) {
             CU_TRY(launch_cand_bitmap(P.wa, P.kbm, P.kn.nwp, P.dense_grid, st));
+            if (P.stage_events) CU_TRY(cudaEventRecordWithFlags(P.ev[4], st, evf));
             CU_TRY(launch_knn_search(P.kn, st));
         } else if (P.use_dense) {
             CU_TRY(launch_candidates_dense(P.wa, P.dense_grid, st));
@@ -2287,6 +2290,10 @@ int culsh_search_profile_get(culsh_search* s, culsh_search_profile* out) {
         CU_TRY(cudaEventElapsedTime(&out->project_ms, s->ev[0], s->ev[1]));
         CU_TRY(cudaEventElapsedTime(&out->probe_ms, s->ev[1], s->ev[2]));
         CU_TRY(cudaEventElapsedTime(&out->candidates_ms, s->ev[2], s->ev[3]));
+        if (s->knn_queries > 0) {
+            CU_TRY(cudaEventElapsedTime(&out->membership_ms, s->ev[2], s->ev[5]));
+            CU_TRY(cudaEventElapsedTime(&out->knn_ms, s->ev[5], s->ev[3]));
+        }
     }
     out->launches = s->launches;
     out->deferred_queries = s->deferred_queries;

@@ -230,6 +230,10 @@ typedef struct culsh_search_profile {
     int knn_fallback;    /* of those, queries whose bound-form lists could not
                             prove the top-K, re-run by the exact per-query
                             kernel                                          */
+    float membership_ms; /* tensor-core path, stage times: planning and the
+                            candidate membership rows ...                   */
+    float knn_ms;        /* ... and the tensor-core distances, top-K lists
+                            and merge (0 unless measured)                   */
 } culsh_search_profile;
 int culsh_search_profile_get(culsh_search* s, culsh_search_profile* out);
 
