@@ -1,11 +1,17 @@
 #!/usr/bin/env python3
-"""Search throughput of the GB300 LSH engine on the integer-feature workload.
+"""k-NN search throughput of the GB300 LSH engine at recall@10 >= 0.90 on
+1M x 128 integer features.
 
 One step = one multiprobe k-NN search of Q queries against a resident index:
 query projection onto all L*M columns, multiprobe codes + bucket lookup, then
-candidate gather / dedup / distances / top-K. Default workload: N=1,000,000
-points of D=128 non-negative integer features stored as float32, L=16 tables,
-M=12 projections, W=16, Q=10,000 held-out queries, K=10, T=16 probes.
+candidate membership / distances / top-K. Default workload: N=1,000,000 points
+of D=128 non-negative integer features stored as float32, L=16 tables, M=12
+projections, T=16 probes, K=10, Q=10,000 held-out queries, and W=825: the
+width at which LSH reaches recall@10 >= 0.90 on these data (at the named
+W=16 no held-out query has a candidate). Each query's candidates then cover
+about half of the dataset; the candidate stage runs on the tensor cores
+(bf16 operands, exact distances for these integer data: the "BF16" form), and
+the FP32 SIMT form of the same search is timed beside it.
 
 value  : queries/s with queries already in HBM (device API), timed per step
          with CUDA events on the launching stream; L2 is flushed (256 MB
@@ -16,8 +22,9 @@ e2e    : queries/s through the reference-facing C ABI (culsh_search_run) with
          pageable copies is reported beside it) and the K x Q ids and
          distances out.
 --impl reference : the CPU oracle (C++/OpenMP restatement of the reference
-         algorithm, all host threads) on the same workload; the reference itself
-         is CUDA-only and cannot be built for the Arm host of the GPU machine.
+         algorithm, all host threads) on the same workload; the reference's
+         own search runs only on a GPU and is not run here (see the
+         reference_build note in the JSON line).
 Multi-GPU (torchrun): independent replicas, one per rank, no collective on the
 data path; the job value is world * Q * steps / max-over-ranks time.
 """
@@ -43,6 +50,13 @@ UNIT = "queries/s"
 FALLBACK_HBM_GBS = 6800.0
 
 
+# Width of the headline workload per configuration: the W at which LSH
+# reaches recall@10 >= 0.90 on the integer features (0.93 with the CPU oracle
+# over 150 held-out queries at 1M points; 0.905 at W=800); the named W=16
+# leaves every held-out query without a candidate.
+RECALL_W = {2: 825.0}
+
+
 def parse_args(argv=None):
     p = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     p.add_argument("--gpus", type=int, default=1)
@@ -54,19 +68,23 @@ def parse_args(argv=None):
     p.add_argument("--q", type=int, default=None, help="override Q")
     p.add_argument("--K", type=int, default=None)
     p.add_argument("--T", type=int, default=None)
+    p.add_argument("--W", type=float, default=None, help="override the bucket width")
+    p.add_argument("--named-w", action="store_true",
+                   help="use the configuration's named W instead of the recall operating point")
     p.add_argument("--recall-sample", type=int, default=200)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-fp32-form", action="store_true", help="skip timing the FP32 SIMT form beside the headline")
     p.add_argument("--no-autotune", action="store_true", help="search with the default tuning")
     p.add_argument("--serve-rates", default="1000,4000,16000",
                    help="Poisson request rates (requests/s) for the serving measurement; empty to skip")
     p.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per serving rate")
-    p.add_argument("--no-recall-point", action="store_true",
-                   help="skip the recall@10 >= 0.90 operating point (clustered 1M x 128, W chosen for recall)")
+    p.add_argument("--no-side", action="store_true",
+                   help="skip the side measurements (named W, Gaussian-mixture recall point, serving)")
     p.add_argument("--tuning", default=None,
                    help="with --recall-point-only: fixed search tuning key=value,... (no tuner, no per-form choice)")
     p.add_argument("--recall-point-only", action="store_true",
-                   help="run only the recall operating point and print its JSON (profiling)")
+                   help="run only the Gaussian-mixture recall operating point and print its JSON (profiling)")
     return p.parse_args(argv)
 
 
@@ -165,15 +183,30 @@ def hbm_peak():
         return FALLBACK_HBM_GBS, "fallback"
 
 
+def tensor_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 1900.0, "fallback"
+
+
 def ncu_traffic(kernel: str, workload: str):
-    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, if any."""
+    """DRAM bytes per launch of `kernel` on `workload` from the committed ncu
+    summary (profiles/ncu_traffic.json): not measured in this run; the entry
+    names the capture it was copied from."""
     path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     try:
         with open(path) as f:
             d = json.load(f)
         e = d.get(workload, {}).get(kernel)
-        return None if e is None else float(e)
-    except (OSError, ValueError):
+        if e is None:
+            return None
+        if isinstance(e, dict):
+            return {"bytes": float(e["bytes"]), "source": f"copied from profiles/ncu_traffic.json: {e['source']}"}
+        return {"bytes": float(e), "source": "copied from profiles/ncu_traffic.json"}
+    except (OSError, ValueError, KeyError):
         return None
 
 
@@ -187,7 +220,12 @@ def stage_bytes(cfg, Q, K, T, KW, hits, nonunique, unique):
     project = 4 * (Q * D + L * M * D + L * M + L * M * Q)
     probe = 4 * L * M * Q + Q * L * T * (8 + 4) + hits * (4 * KW + 4) + 8 * Q
     cand = 8 * Q + 4 * Q * L * T + 8 * hits + 4 * nonunique + 4 * D * unique + 4 * D * Q + 8 * K * Q
-    return {"project": project, "probe": probe, "candidates": cand}
+    # tensor-core path: the membership rows read every candidate id (4 C_nu)
+    # and write one N-bit row per query; the masked GEMM's work is 2 D N
+    # multiply-adds per query
+    membership = 4 * Q * L * T + 4 * nonunique + Q * ((cfg["N"] + 31) // 32) * 4
+    knn_flops = 2.0 * D * cfg["N"] * Q
+    return {"project": project, "probe": probe, "candidates": cand, "membership": membership, "knn_flops": knn_flops}
 
 
 def recall_at_k(found, X, queries, K):
@@ -216,25 +254,40 @@ def workload(args):
     X, Qm, A, b, cfg = synth.dataset(args.config, n=args.n, q=args.q)
     K = args.K or cfg.K
     T = args.T or cfg.T
-    d = dict(N=X.shape[0], D=cfg.D, L=cfg.L, M=cfg.M, W=cfg.W, Q=Qm.shape[0], K=K, T=T)
-    name = f"{cfg.name} N={d['N']} L={cfg.L} M={cfg.M} W={cfg.W:g} T={T} K={K} Q={d['Q']}"
+    W = args.W if args.W is not None else (cfg.W if args.named_w else RECALL_W.get(args.config, cfg.W))
+    if W != cfg.W:   # same seeded projection, b drawn for this width
+        A, b = synth.projection(cfg.L, cfg.M, cfg.D, W, 3000 + args.config)
+    d = dict(N=X.shape[0], D=cfg.D, L=cfg.L, M=cfg.M, W=W, Q=Qm.shape[0], K=K, T=T)
+    name = f"{cfg.name} N={d['N']} L={cfg.L} M={cfg.M} W={W:g} T={T} K={K} Q={d['Q']}"
     return X, Qm, A, b, d, name
 
 
-def cpu_baseline(X, Qm, A, b, d, min_seconds=8.0):
+def cpu_baseline(X, Qm, A, b, d, seconds=12.0):
+    """The oracle on the host cores over a bounded sample of the queries
+    (about `seconds` of search after an untimed CPU index build)."""
     import oracle
     t0 = time.perf_counter()
     idx = oracle.build_index(X, A, b, d["W"])
     t_index = time.perf_counter() - t0
-    reps, el = 0, 0.0
-    while el < min_seconds or reps < 1:
-        t0 = time.perf_counter()
-        oracle.search(idx, X, Qm, d["K"], d["T"])
-        el += time.perf_counter() - t0
-        reps += 1
-    return {"value": reps * Qm.shape[0] / el, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
-            "sample": f"{reps} x {Qm.shape[0]} queries of the same workload after a {t_index:.1f} s CPU index build",
+    t0 = time.perf_counter()
+    oracle.search(idx, X, Qm[:16], d["K"], d["T"])
+    per_q = max((time.perf_counter() - t0) / 16, 1e-7)
+    nq = int(min(Qm.shape[0], max(16, seconds / per_q)))
+    t0 = time.perf_counter()
+    oracle.search(idx, X, Qm[:nq], d["K"], d["T"])
+    el = time.perf_counter() - t0
+    return {"value": nq / el, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+            "sample": f"the first {nq} of the {Qm.shape[0]} queries of the same workload, after a "
+                      f"{t_index:.1f} s CPU index build",
             "index_build_s": round(t_index, 3)}
+
+
+REFERENCE_BUILD_NOTE = (
+    "the reference's own CUDA build is not run: its sources compile with this image's nvcc for sm_103a, "
+    "but the GPU machine is an Arm host without the reference tree, the reference sources may not be copied "
+    "into this repository, binaries built on the x86 development host do not run there, and no aarch64 cross "
+    "toolchain or CUDA aarch64 libraries exist on the development host; the '>= 3x the reference CUDA build' "
+    "target is therefore unmeasured, and the reference arm is the CPU oracle port")
 
 
 def run_reference(args):
@@ -246,11 +299,11 @@ def run_reference(args):
     t0 = time.perf_counter()
     idx = oracle.build_index(X, A, b, d["W"])
     t_index = time.perf_counter() - t0
-    # bounded sample per step: as many queries as take about half a second
+    # bounded sample per step: as many queries as take about one second
     t0 = time.perf_counter()
-    oracle.search(idx, X, Qm[:500], d["K"], d["T"])
-    per_q = max((time.perf_counter() - t0) / 500, 1e-7)
-    nq = int(min(Qm.shape[0], max(500, 0.5 / per_q)))
+    oracle.search(idx, X, Qm[:8], d["K"], d["T"])
+    per_q = max((time.perf_counter() - t0) / 8, 1e-7)
+    nq = int(min(Qm.shape[0], max(8, 1.0 / per_q)))
     sample = Qm[:nq]
     for _ in range(args.warmup):
         oracle.search(idx, X, sample, d["K"], d["T"])
@@ -267,8 +320,9 @@ def run_reference(args):
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
                              "sample": f"{nq} queries per step; CPU index build {t_index:.1f} s untimed"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "the reference (cuLSH) is CUDA + cuBLAS + Thrust only; its algorithm runs here as the "
-                    "C++/OpenMP oracle port on the host cores"}
+            "note": "the reference (cuLSH) has no CPU path; its algorithm runs here as the C++/OpenMP "
+                    "oracle port on the host cores",
+            "reference_build": REFERENCE_BUILD_NOTE}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -336,12 +390,30 @@ def parse_tuning(spec):
     return out
 
 
+def timed_searches(st, torch, stream, sp, qt, Q, ids, dists, flush, steps):
+    """Median device ms of `steps` searches (CUDA events on the launching
+    stream, L2 flushed before each, outside the events)."""
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for i in range(steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(i & 0xFF)
+        ev[i][0].record(stream)
+        st.search_device(qt.data_ptr(), Q, ids.data_ptr(), dists.data_ptr(), sp)
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    return statistics.median(e0.elapsed_time(e1) for e0, e1 in ev)
+
+
 def recall_point(culsh, torch, dev, steps, warmup, autotune=True, fixed=None):
-    """Search throughput where LSH reaches recall@10 >= 0.90: the Gaussian-
-    mixture generator (100 centres ~N(0,10^2), unit noise) at 1M x 128, L=8,
-    M=8, T=16, K=10, with W=32 (the named W=4 leaves every held-out query
-    without candidates). FP32 and BF16 distance forms return identical
-    results; both are timed (device events, inputs resident, L2 flushed)."""
+    """The Gaussian-mixture generator (100 centres ~N(0,10^2), unit noise) at
+    1M x 128, L=8, M=8, T=16, K=10, W=32, where LSH reaches recall@10 >= 0.90
+    with sparse candidate sets (about 0.7 % of the dataset per query; the
+    named W=4 leaves every held-out query without a candidate). Real-valued
+    data: the tensor-core form takes its bound form (three bf16 products,
+    certified bounds, exact FP32 recomputation). Three forms, identical
+    results: FP32 work-stealing gather, BF16 gather with certified FP32
+    rerank, tensor cores; each timed at its best settings (device events,
+    inputs resident, L2 flushed)."""
     from culsh_gb300 import synth
     X, Qm, _, _, cfg = synth.dataset(1, n=1_000_000, q=10_000)
     N, D = X.shape
@@ -363,95 +435,77 @@ def recall_point(culsh, torch, dev, steps, warmup, autotune=True, fixed=None):
     forms = {}
     ref = None
     tuned = None
-    if autotune and not fixed:   # untimed; the tuner may pick either distance form, both are timed below
+    if autotune and not fixed:   # untimed; the tuner may pick any form, all are timed below
         tuned = st.autotune(qt.data_ptr(), Q, ids.data_ptr(), dists.data_ptr(), sp)
     if fixed:
         st.set_tuning(**fixed)
         tuned = st.get_tuning()
-    for name, bf in (("fp32", 0), ("bf16_rerank", 1)):
-        if fixed and "distance_bf16" in fixed and fixed["distance_bf16"] != bf:
+    for name, bf, tc in (("fp32", 0, 0), ("bf16_rerank", 1, 0), ("tensor_cores", 0, 1)):
+        if fixed and ("distance_bf16" in fixed and fixed["distance_bf16"] != bf or
+                      "dense_tc" in fixed and fixed["dense_tc"] != tc):
             continue
-        # each form at its own best set size, partition size and item order
+        # each gather form at its own best set size, partition size and item order
         # (untimed selection among a few; the tuner's choice is one of them)
         t0 = st.get_tuning()
         best = (0.0, t0["ws_set_slots"], t0["ws_chunk"], t0["ws_order"])
-        for sl, ch in (() if fixed else ((4096, 2048), (8192, 4096), (16384, 8192))):
+        grid = () if (fixed or tc) else ((4096, 2048), (8192, 4096), (16384, 8192))
+        for sl, ch in grid:
             for order in (0, 1):
-                st.set_tuning(candidates_mode=1, distance_bf16=bf, ws_set_slots=sl, ws_chunk=ch, ws_order=order)
+                st.set_tuning(candidates_mode=1, distance_bf16=bf, dense_tc=tc, dense_min=0,
+                              ws_set_slots=sl, ws_chunk=ch, ws_order=order)
                 t = []
                 for _ in range(3):
                     st.search_device(qt.data_ptr(), Q, ids.data_ptr(), dists.data_ptr(), sp)
                     t.append(st.profile()["candidates_ms"])
                 if best[0] == 0.0 or statistics.median(t) < best[0]:
                     best = (statistics.median(t), sl, ch, order)
-        st.set_tuning(candidates_mode=1, distance_bf16=bf, ws_set_slots=best[1], ws_chunk=best[2], ws_order=best[3])
+        st.set_tuning(candidates_mode=1, distance_bf16=bf, dense_tc=tc, ws_set_slots=best[1], ws_chunk=best[2],
+                      ws_order=best[3], dense_min=(1024 if tc else 0))
         for _ in range(warmup):
             st.search_device(qt.data_ptr(), Q, ids.data_ptr(), dists.data_ptr(), sp)
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-        cand = []
-        for i in range(steps):
-            with torch.cuda.stream(stream):
-                flush.fill_(i & 0xFF)
-            ev[i][0].record(stream)
-            st.search_device(qt.data_ptr(), Q, ids.data_ptr(), dists.data_ptr(), sp)
-            ev[i][1].record(stream)
-            cand.append(st.profile()["candidates_ms"])
-        torch.cuda.synchronize()
-        ms = statistics.median(e0.elapsed_time(e1) for e0, e1 in ev)
+        ms = timed_searches(st, torch, stream, sp, qt, Q, ids, dists, flush, steps)
         out = ids.cpu().numpy()
         if ref is None:
             ref = out
         pr = st.profile()
         forms[name] = {"qps": round(Q / (ms / 1e3), 1), "ms_per_step": round(ms, 3),
-                       "set_slots": best[1], "chunk": best[2], "order": best[3],
-                       "candidates_ms": round(statistics.median(cand), 3), "rechecked_fp32": int(pr["rechecked"]),
+                       "candidates_ms": round(pr["candidates_ms"], 3), "rechecked_fp32": int(pr["rechecked"]),
+                       "tensor_core_queries": int(pr["knn_queries"]), "fallback_queries": int(pr["knn_fallback"]),
                        "identical_to_fp32": bool(np.array_equal(out, ref))}
+        if not tc:
+            forms[name].update({"set_slots": best[1], "chunk": best[2], "order": best[3]})
     uniq = st.getTotalCandidates_unique() / Q
-    # algorithmic gather bytes of the candidate stage: rows of the unique candidates
-    for name, f in forms.items():
-        row = 2 * D if name == "bf16_rerank" else 4 * D
-        f["candidate_gather_gbs"] = round(uniq * Q * row / (f["candidates_ms"] / 1e3) / 1e9, 1)
     rec = recall_at_k(ref[:200], X, Qm[:200], K)
     return {"workload": f"gauss-mixture-1m-d128 N={N} L={L} M={M} W={W} T={T} K={K} Q={Q}",
             "recall_at_k": rec, "recall_sample": 200, "candidates_unique_per_query": round(uniq, 1),
             "tuning": tuned, "forms": forms}
 
 
-def recall_point_same_data(culsh, torch, dev, Xt, X, Qm, d, steps, warmup, W=900.0, nq=2000):
-    """The integer-feature data themselves at recall@10 >= 0.90: same resident
-    1M x 128 dataset, L, M, T, K, held-out queries, with W = 900 (the features
-    have no neighbourhood structure, so recall needs near-exhaustive candidate
-    sets: about two thirds of the dataset per query, the bitmap kernel)."""
+def named_point(culsh, torch, dev, Xt, d, A, b, Qm, steps, warmup):
+    """The configuration exactly as named (W=16): no held-out query has a
+    candidate, so the search is projection + multiprobe lookups only."""
     N, D, L, M, T, K = d["N"], d["D"], d["L"], d["M"], d["T"], d["K"]
-    from culsh_gb300 import synth
-    A, b = synth.projection(L, M, D, W, 3002)
+    Q = Qm.shape[0]
     stream = torch.cuda.Stream(dev)
     sp = stream.cuda_stream
     ht = culsh.HashTables()
-    ht.reset(N, D, L, M, W, A=A, b=b)
+    ht.reset(N, D, L, M, d["W"], A=A, b=b)
     ht.index_device(Xt.data_ptr(), sp)
-    q = torch.from_numpy(np.ascontiguousarray(Qm[:nq])).to(dev)
+    qt = torch.from_numpy(Qm).to(dev)
     torch.cuda.synchronize()
-    ids = torch.empty((nq, K), dtype=torch.int32, device=dev)
-    dists = torch.empty((nq, K), dtype=torch.float32, device=dev)
+    ids = torch.empty((Q, K), dtype=torch.int32, device=dev)
+    dists = torch.empty((Q, K), dtype=torch.float32, device=dev)
     st = culsh.SearchTables()
     st.reset(ht, K, T)
+    st.autotune(qt.data_ptr(), Q, ids.data_ptr(), dists.data_ptr(), sp)
+    st.set_profiling(False)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     for _ in range(warmup):
-        st.search_device(q.data_ptr(), nq, ids.data_ptr(), dists.data_ptr(), sp)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-    for i in range(steps):
-        ev[i][0].record(stream)
-        st.search_device(q.data_ptr(), nq, ids.data_ptr(), dists.data_ptr(), sp)
-        ev[i][1].record(stream)
-    torch.cuda.synchronize()
-    ms = statistics.median(e0.elapsed_time(e1) for e0, e1 in ev)
-    pr = st.profile()
-    uniq = st.getTotalCandidates_unique() / nq
-    rec = recall_at_k(ids.cpu().numpy()[:100], X, Qm[:100], K)
-    return {"workload": f"int-features-1m-d128 N={N} L={L} M={M} W={W:g} T={T} K={K} Q={nq}",
-            "recall_at_k": rec, "recall_sample": 100, "qps": round(nq / (ms / 1e3), 1), "ms_per_step": round(ms, 3),
-            "candidates_unique_per_query": round(uniq, 1), "dense_bitmap_queries": int(pr["dense_queries"]),
-            "candidate_rows_gbs": round(uniq * nq * 4 * D / (pr["candidates_ms"] / 1e3) / 1e9, 1)}
+        st.search_device(qt.data_ptr(), Q, ids.data_ptr(), dists.data_ptr(), sp)
+    ms = timed_searches(st, torch, stream, sp, qt, Q, ids, dists, flush, steps)
+    return ht, {"workload": f"int-features-1m-d128 N={N} L={L} M={M} W={d['W']:g} T={T} K={K} Q={Q}",
+                "qps": round(Q / (ms / 1e3), 1), "ms_per_step": round(ms, 4),
+                "candidates_unique_per_query": st.getTotalCandidates_unique() / Q}
 
 
 def run_culsh(args):
@@ -495,7 +549,7 @@ def run_culsh(args):
     st.reset(ht, K, T)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     tuning = None
-    if not args.no_autotune:   # untimed: picks tiles, probe batch depth, candidate kernel shape
+    if not args.no_autotune:   # untimed: tilings, probe form, candidate-stage form (tensor cores or SIMT)
         tuning = st.autotune(qt.data_ptr(), Q, ids.data_ptr(), dists.data_ptr(), sp)
 
     for _ in range(args.warmup):
@@ -511,7 +565,6 @@ def run_culsh(args):
     clocks = ClockSampler(gpu_id)
     clocks.start()
     events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    stages = {"project": [], "probe": [], "candidates": []}
     launches = 0
     if dist is not None:
         dist.barrier()
@@ -536,43 +589,79 @@ def run_culsh(args):
         dist.barrier()
     clk = clocks.stop()
     step_ms = [e0.elapsed_time(e1) for e0, e1 in events]
+    total_s = sum(step_ms) / 1e3
+    max_s = reduce_max(dist, total_s, dev)
+    value = aggregate_throughput(Q * args.steps, world, max_s)
+    found = ids.cpu().numpy()
+    found_d = dists.cpu().numpy()
+    prof_run = st.profile()
+
+    # Stage breakdown from separate searches with the stage events on.
     st.set_profiling(True)
+    stages = {k: [] for k in ("project", "probe", "candidates", "membership", "knn")}
     for i in range(max(3, min(args.steps, 10))):
         with torch.cuda.stream(stream):
             flush.fill_(i & 0xFF)
         st.search_device(qt.data_ptr(), Q, ids.data_ptr(), dists.data_ptr(), sp)
         pr = st.profile()
-        stages["project"].append(pr["project_ms"])
-        stages["probe"].append(pr["probe_ms"])
-        stages["candidates"].append(pr["candidates_ms"])
-    total_s = sum(step_ms) / 1e3
-    max_s = reduce_max(dist, total_s, dev)
-    value = aggregate_throughput(Q * args.steps, world, max_s)
+        for k, f in (("project", "project_ms"), ("probe", "probe_ms"), ("candidates", "candidates_ms"),
+                     ("membership", "membership_ms"), ("knn", "knn_ms")):
+            stages[k].append(pr[f])
+    med = {k: statistics.median(v) for k, v in stages.items()}
 
     # Totals for the algorithmic byte counts (outside the timed region).
     uniq, nonuniq = st.getTotalCandidates_unique(), st.getTotalCandidates_nonUnique()
     hits = sum(int((st.getQueryBuckets(l) >= 0).sum()) for l in range(L))
     KW = st.profile()["key_words"]
     sb = stage_bytes(d, Q, K, T, KW, hits, nonuniq, uniq)
-    med = {k: statistics.median(v) for k, v in stages.items()}
-    dom = max(med, key=med.get)
     peak, peak_kind = hbm_peak()
-    achieved = sb[dom] / (med[dom] / 1e3) / 1e9
-    kernel_name = {"project": "k_project", "probe": "k_probe", "candidates": "k_candidates"}[dom]
-    kernel_label = kernel_name
-    if dom == "probe":
-        # the probe stage is one fused kernel or (M <= 16) the enumeration
-        # kernel plus the lookup kernel (split form), or one kernel that looks
-        # its probes up at the end (tail form)
-        env = os.environ.get("CULSH_PROBE_SPLIT")
-        form = (int(env) if env is not None else int(st.get_tuning().get("probe_split", 0))) if M <= 16 else 0
-        kernel_name = {1: "k_probe_split", 2: "k_probe_tail"}.get(form, "k_probe_fused")
-        kernel_label = {1: "k_probe_fast (enumeration) + k_probe_resolve",
-                        2: "k_probe_fast (enumeration + lookups at its end)"}.get(form, "k_probe_fast")
-    roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 5), "traffic": ncu_traffic(kernel_name, name),
-                "kernel": kernel_label, "algorithmic_bytes": sb[dom], "peak_source": f"{peak_kind} hbm_gbs",
-                "stage_ms_median": {k: round(v, 4) for k, v in med.items()}}
+    tpeak, tpeak_kind = tensor_peak()
+    rooflines = {}
+    for k in ("project", "probe"):
+        if med[k] > 0:
+            rooflines[k] = {"bound": "hbm", "achieved": sb[k] / (med[k] / 1e3) / 1e9, "unit": "GB/s", "peak": peak}
+    if prof_run["knn_queries"] > 0 and med["knn"] > 0:
+        rooflines["membership"] = {"bound": "hbm", "achieved": sb["membership"] / (med["membership"] / 1e3) / 1e9,
+                                   "unit": "GB/s", "peak": peak}
+        rooflines["knn"] = {"bound": "tensor", "achieved": sb["knn_flops"] / (med["knn"] / 1e3) / 1e12,
+                            "unit": "TFLOP/s", "peak": tpeak}
+    else:
+        rooflines["candidates"] = {"bound": "hbm", "achieved": sb["candidates"] / (med["candidates"] / 1e3) / 1e9,
+                                   "unit": "GB/s", "peak": peak}
+    times = {"project": med["project"], "probe": med["probe"], "membership": med["membership"],
+             "knn": med["knn"], "candidates": med["candidates"]}
+    dom = max(rooflines, key=lambda k: times[k])
+    kernel_of = {"project": "k_project", "probe": "k_probe_fast", "membership": "k_cand_bitmap",
+                 "knn": "k_knn_tc", "candidates": "k_candidates_ws"}
+    rf = rooflines[dom]
+    traffic = ncu_traffic(kernel_of[dom], name)
+    roofline = {"bound": rf["bound"], "achieved": round(rf["achieved"], 2), "peak": rf["peak"], "unit": rf["unit"],
+                "frac": round(rf["achieved"] / rf["peak"], 5),
+                "traffic": None if traffic is None else traffic["bytes"],
+                "traffic_source": None if traffic is None else traffic["source"],
+                "kernel": kernel_of[dom], "stage": dom,
+                "algorithmic": {"membership_bytes": sb["membership"], "knn_flops": sb["knn_flops"],
+                                "probe_bytes": sb["probe"], "project_bytes": sb["project"],
+                                "candidates_bytes": sb["candidates"]},
+                "peak_source": f"{peak_kind} hbm_gbs" if rf["bound"] == "hbm" else f"{tpeak_kind} bf16_tflops (burst)",
+                "stage_ms_median": {k: round(v, 4) for k, v in med.items()},
+                "all_stages": {k: {"achieved": round(v["achieved"], 2), "unit": v["unit"],
+                                   "frac": round(v["achieved"] / v["peak"], 5)} for k, v in rooflines.items()}}
+
+    # The FP32 form of the same search (dense queries on the SIMT bitmap
+    # kernel, FP32 lane-order distances): same results, timed beside it.
+    fp32 = None
+    if not args.no_fp32_form and prof_run["knn_queries"] > 0 and rank == 0:
+        saved = st.get_tuning()
+        st.set_tuning(dense_tc=0, dense_min=0)
+        st.set_profiling(False)
+        st.search_device(qt.data_ptr(), Q, ids.data_ptr(), dists.data_ptr(), sp)
+        ms = timed_searches(st, torch, stream, sp, qt, Q, ids, dists, flush, 3)
+        fp32 = {"qps": round(Q / (ms / 1e3), 1), "ms_per_step": round(ms, 3), "form": "SIMT bitmap kernel, FP32",
+                "identical": bool(np.array_equal(ids.cpu().numpy(), found) and
+                                  np.array_equal(dists.cpu().numpy(), found_d)),
+                "tensor_cores_over_fp32": round(value / (Q / (ms / 1e3)), 2)}
+        st.set_tuning(**{k: v for k, v in saved.items() if k not in ("search_ms", "configs_tried")})
 
     # End to end through the reference-facing C ABI with host buffers.
     e2e = None
@@ -595,9 +684,10 @@ def run_culsh(args):
         for a in q_pin:
             a[...] = Qm
 
-        # host wall-clock timing: at least 200 calls (tens of milliseconds),
-        # so that host jitter averages out
-        e2e_steps = max(args.steps, 200)
+        # host wall-clock timing over at least 0.5 s of calls, so that host
+        # jitter averages out
+        per_call = max(1e-4, max_s / args.steps)
+        e2e_steps = max(args.steps, int(0.5 / per_call))
 
         def host_loop(bufs):
             # the warm-up touches every buffer once (as a serving loop's
@@ -612,7 +702,7 @@ def run_culsh(args):
             for i in range(e2e_steps):
                 st_h.search(bufs[(w + i) % n_rot], Q, X)
             el_max = reduce_max(dist, time.perf_counter() - t0, dev)
-            assert np.array_equal(st_h.getKnnIds(), ids.cpu().numpy()), "host and device API results differ"
+            assert np.array_equal(st_h.getKnnIds(), found), "host and device API results differ"
             return aggregate_throughput(Q * e2e_steps, world, el_max), st_h.profile()["host_path"]
 
         v_page, hp_page = host_loop([Qm.copy() for _ in range(n_rot)])
@@ -628,51 +718,62 @@ def run_culsh(args):
                "pageable": {"value": v_page, "host_path": hp_page}}
         del st_h, ht_h, q_pin, pinned
 
-    rpoint = rpoint_int = None
-    if not args.no_recall_point and rank == 0:
-        rpoint = recall_point(culsh, torch, dev, max(3, min(args.steps, 10)), max(args.warmup, 3))
-        if args.config == 2:
-            rpoint_int = recall_point_same_data(culsh, torch, dev, Xt, X, Qm, d, max(3, min(args.steps, 5)),
-                                                max(args.warmup, 3))
-
-    serving = None
-    rates = [float(r) for r in args.serve_rates.split(",") if r.strip()]
-    if rates and rank == 0:
-        from culsh_gb300 import synth
-        pool = synth.dataset(args.config, n=16, q=max(65536, Q))[1]
-        Ks = sorted({K, 10, 100})
-        Ts = [1, 8, 32] if args.config == 5 else sorted({1, T})   # the serving workload's T mix
-        serving = {"arrivals": "Poisson", "request_queries": "log-uniform 1..4096", "K": Ks, "T": Ts,
-                   "slots": 4, "index": "the resident index above",
-                   "runs": [serve_run(culsh, ht, pool, r, args.serve_seconds, Ks, Ts, seed=17 + i)
-                            for i, r in enumerate(rates)]}
-
-    found = ids.cpu().numpy()
     ns = min(args.recall_sample, Q)
     rec = recall_at_k(found[:ns], X, Qm[:ns], K) if ns > 0 else None
+
+    named = rpoint = serving = None
+    if not args.no_side and rank == 0:
+        from culsh_gb300 import synth
+        cfg = synth.CONFIGS[args.config]
+        ht_named = ht
+        if args.config in RECALL_W and d["W"] != cfg.W:
+            An, bn = synth.projection(cfg.L, cfg.M, cfg.D, cfg.W, 3000 + args.config)
+            ht_named, named = named_point(culsh, torch, dev, Xt, dict(d, W=cfg.W), An, bn, Qm,
+                                          max(3, min(args.steps, 10)), max(args.warmup, 3))
+        rpoint = recall_point(culsh, torch, dev, max(3, min(args.steps, 10)), max(args.warmup, 3))
+        rates = [float(r) for r in args.serve_rates.split(",") if r.strip()]
+        if rates:
+            pool = synth.dataset(args.config, n=16, q=max(65536, Q))[1]
+            Ks = sorted({K, 10, 100})
+            Ts = [1, 8, 32] if args.config == 5 else sorted({1, T})   # the serving workload's T mix
+            serving = {"arrivals": "Poisson", "request_queries": "log-uniform 1..4096", "K": Ks, "T": Ts,
+                       "slots": 4, "index": f"{cfg.name} at W={cfg.W:g} (the named configuration)",
+                       "runs": [serve_run(culsh, ht_named, pool, r, args.serve_seconds, Ks, Ts, seed=17 + i)
+                                for i, r in enumerate(rates)]}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(X, Qm, A, b, d)
 
     if rank == 0:
+        from culsh_gb300 import synth
+        tc = prof_run["knn_queries"] > 0
+        named_w = synth.CONFIGS[args.config].W
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * max_s / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "scaling": "weak", "vs_baseline": None, "dtype": "bf16" if tc else "f32",
                 "data": "synthetic (seeded generator of the workload's distribution)",
-                "config": {"workload": name, **d, "form": "fp32 (canonical order, bit-exact)",
+                "config": {"workload": name, **d,
+                           "form": ("tensor cores: bf16 operands, exact distances (integer data), "
+                                    "results bit-identical to the FP32 form") if tc else
+                                   "fp32 (canonical order, bit-exact)",
+                           "operating_point": (f"W={d['W']:g} for recall@10 >= 0.90 (the named W={named_w:g} "
+                                               "leaves held-out queries without candidates)")
+                                              if d["W"] != named_w else "the named W",
                            "l2": "flushed by a 256 MB write between timed steps", "parallelism": "replicas",
-                           "search": "captured CUDA graph, persistent work-stealing candidate kernel",
+                           "search": "captured CUDA graph",
                            "stage_events": "off in the timed loops (instrumentation); stage times from separate searches",
                            "tuning": tuning},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-                "clocks": clk, "index_build_ms": round(statistics.median(build_ms), 3),
+                "clocks": clk, "recall_at_k": rec, "recall_sample": ns,
+                "selectivity": st.getSelectivity(), "candidates_unique_per_query": uniq / Q,
+                "candidates_nonunique_per_query": nonuniq / Q,
+                "tensor_core_queries": prof_run["knn_queries"], "fallback_queries": prof_run["knn_fallback"],
+                "fp32_form": fp32, "index_build_ms": round(statistics.median(build_ms), 3),
                 "index_build_stages_ms": {k: (round(v, 4) if isinstance(v, float) else v)
                                           for k, v in build_profile.items()},
-                "recall_at_k": rec, "recall_sample": ns, "recall_point": rpoint,
-                "recall_point_same_data": rpoint_int, "serving": serving,
-                "selectivity": st.getSelectivity(), "candidates_unique_per_query": uniq / Q,
-                "candidates_nonunique_per_query": nonuniq / Q}
+                "named_w": named, "recall_point_gauss": rpoint, "serving": serving,
+                "reference_build": REFERENCE_BUILD_NOTE}
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.barrier()
@@ -689,9 +790,9 @@ def main(argv=None):
         import culsh_gb300 as culsh
         dev = torch.device("cuda", 0)
         torch.cuda.set_device(dev)
-        print(json.dumps({"recall_point": recall_point(culsh, torch, dev, args.steps, args.warmup,
-                                                       autotune=not args.no_autotune,
-                                                       fixed=parse_tuning(args.tuning))}), flush=True)
+        print(json.dumps({"recall_point_gauss": recall_point(culsh, torch, dev, args.steps, args.warmup,
+                                                             autotune=not args.no_autotune,
+                                                             fixed=parse_tuning(args.tuning))}), flush=True)
         return 0
     return run_culsh(args)
 
