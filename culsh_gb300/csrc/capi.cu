@@ -243,6 +243,7 @@ struct culsh_search {
     DevBuf<uint32_t> kbm;
     DevBuf<uint16_t> kq_h, kq_l;
     DevBuf<float> kq_sq, kq_base, kpart_key;
+    DevBuf<unsigned int> kq_bound;
     DevBuf<uint32_t> kpart_id;
     DevBuf<int> kpart_n, kfallback;
     int knn_queries = 0, knn_fallback = 0;   // last search: dense queries on the tensor cores, re-run
@@ -931,6 +932,7 @@ int plan_knn(culsh_search* s, SearchPlan& P, int Q, int32_t* d_ids, float* d_d, 
     CU_TRY(s->kq_l.reserve((size_t)k.Qcap * k.Dp));
     CU_TRY(s->kq_sq.reserve(k.Qcap));
     CU_TRY(s->kq_base.reserve(k.Qcap));
+    CU_TRY(s->kq_bound.reserve(k.Qcap));
     CU_TRY(s->kpart_key.reserve(knn_part_entries(k)));
     CU_TRY(s->kpart_id.reserve(knn_part_entries(k)));
     CU_TRY(s->kpart_n.reserve(knn_part_lists(k)));
@@ -948,6 +950,7 @@ int plan_knn(culsh_search* s, SearchPlan& P, int Q, int32_t* d_ids, float* d_d, 
     k.ql = s->kq_l.p;
     k.qsq = s->kq_sq.p;
     k.qbase = s->kq_base.p;
+    k.qbound = s->kq_bound.p;
     k.qstate = reinterpret_cast<KnnState*>(s->stats.p + 8);
     k.bm = s->kbm.p;
     k.part_key = s->kpart_key.p;
@@ -1927,6 +1930,7 @@ long long culsh_search_device_bytes(culsh_search* s) {
     add(s->kq_l);
     add(s->kq_sq);
     add(s->kq_base);
+    add(s->kq_bound);
     add(s->kpart_key);
     add(s->kpart_id);
     add(s->kpart_n);
@@ -1990,6 +1994,7 @@ int culsh_search_release(culsh_search* s) {
     s->kq_l.release();
     s->kq_sq.release();
     s->kq_base.release();
+    s->kq_bound.release();
     s->kpart_key.release();
     s->kpart_id.release();
     s->kpart_n.release();
@@ -2400,7 +2405,12 @@ extern "C" int culsh_search_run_device_noalloc(culsh_search* s, const float* d_q
     unsigned long long* stats = reinterpret_cast<unsigned long long*>(base + o_stats);
     int* deferred = reinterpret_cast<int*>(base + o_def);
     uint32_t* arena = reinterpret_cast<uint32_t*>(base + o_arena);
-    const unsigned long long arena_words = (kNoAllocScratchBytes - o_arena) / 4;
+    unsigned long long arena_words = (kNoAllocScratchBytes - o_arena) / 4;
+    // CULSH_NOALLOC_ARENA_WORDS lowers the overflow arena below what the
+    // fixed array leaves for it (never raises it); the tests use it to reach
+    // the deferred rounds and the capacity error with small cases.
+    if (const char* e = getenv("CULSH_NOALLOC_ARENA_WORDS"))
+        arena_words = std::min<unsigned long long>(arena_words, std::max(1ll, atoll(e)));
 
     CU_TRY(cudaMemsetAsync(cnu, 0, 8 * (size_t)Q, st));
     CU_TRY(cudaMemsetAsync(stats, 0, 8 * 4, st));

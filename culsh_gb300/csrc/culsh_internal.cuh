@@ -403,6 +403,7 @@ struct KnnSearch {
     float* qsq;                        // [Qcap]
     float* qbase;                      // [Qcap]
     KnnState* qstate;                  // cleared before the search
+    unsigned int* qbound;              // [Qcap] exact form: per-query shared key bound
     const uint32_t* bm;                // [Qcap][nwp] membership rows (k_cand_bitmap)
     float* part_key;                   // partial lists, see k_knn_tc
     uint32_t* part_id;

@@ -60,6 +60,7 @@
 #include <climits>
 #include <cmath>
 #include <cstdlib>
+#include <cstring>
 
 #include "culsh_internal.cuh"
 #include "topk_common.cuh"
@@ -68,10 +69,16 @@ namespace culsh {
 namespace {
 
 constexpr int KM = 128;                 // rows of one MMA (TMEM lanes)
-constexpr int kBn = 128;                // points per tile
-constexpr int kMqExact = 256;           // queries per tile, exact form (two MMAs share a point tile)
-constexpr int kMqBound = 128;           // queries per tile, bound form (three products per element)
-constexpr uint32_t kKnnPoll = 1u << 26;
+// Tile shapes: MQ queries (MQ / 128 MMAs of M = 128) x BN points per tile,
+// NEPI epilogue warps, NCH = 32 NEPI / MQ column slices of 64 per query.
+constexpr int kBnExact = 128, kMqExact = 256, kNepiExact = 16;   // exact form: two MMAs share a point tile
+constexpr int kBnBound = 128, kMqBound = 128, kNepiBound = 8;    // bound form: three products per element
+constexpr int kNchExact = 32 * kNepiExact / kMqExact, kNchBound = 32 * kNepiBound / kMqBound;
+// Bounded waits: each poll suspends the thread in hardware for up to
+// kKnnSuspendNs (it resumes as soon as the phase completes, and takes no issue
+// slots meanwhile), at most kKnnPoll polls (a few seconds) in all.
+constexpr uint32_t kKnnPoll = 1u << 18;
+constexpr uint32_t kKnnSuspendNs = 16384;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -88,20 +95,18 @@ __device__ __forceinline__ void bar_arrive(uint64_t* bar) {
 __device__ __forceinline__ bool bar_try_wait(uint64_t* bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
         : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(parity)
+        : "r"(smem_addr(bar)), "r"(parity), "r"(kKnnSuspendNs)
         : "memory");
     return ok != 0;
 }
 // Bounded wait for the phase of the given parity; on timeout raises the
-// block's abort flag and kErrSpin. Single-thread roles back off between polls.
-__device__ __forceinline__ bool bar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag, int* err,
-                                         bool backoff) {
+// block's abort flag and kErrSpin.
+__device__ __forceinline__ bool bar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag, int* err) {
     for (uint32_t i = 0; i < kKnnPoll; ++i) {
         if (bar_try_wait(bar, parity)) return true;
         if (*abort_flag) return false;
-        if (backoff) __nanosleep(64);
     }
     *abort_flag = 1;
     atomicOr(err, kErrSpin);
@@ -109,10 +114,8 @@ __device__ __forceinline__ bool bar_wait(uint64_t* bar, uint32_t parity, volatil
 }
 // Bounded wait that ignores the abort flag (draining at exit).
 __device__ __forceinline__ void bar_drain(uint64_t* bar, uint32_t parity, int* err) {
-    for (uint32_t i = 0; i < kKnnPoll; ++i) {
+    for (uint32_t i = 0; i < kKnnPoll; ++i)
         if (bar_try_wait(bar, parity)) return;
-        __nanosleep(64);
-    }
     atomicOr(err, kErrSpin);
 }
 
@@ -163,20 +166,15 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// The 128 accumulator columns [taddr, taddr + 128) of this thread's TMEM lane,
+// The 64 accumulator columns [taddr, taddr + 64) of this thread's TMEM lane,
 // loaded and waited for in one statement, so that no use of r can be
 // scheduled before the wait.
-__device__ __forceinline__ void tmem_ld128(uint32_t taddr, uint32_t (&r)[128]) {
+__device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t (&r)[64]) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%128];\n\t"
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%64];\n\t"
         "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%32, %33, %34, %35, %36, %37, %38, %39, %40, %41, %42, %43, %44, "
-        "%45, %46, %47, %48, %49, %50, %51, %52, %53, %54, %55, %56, %57, %58, %59, %60, %61, %62, %63}, [%128+32];\n\t"
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%64, %65, %66, %67, %68, %69, %70, %71, %72, %73, %74, %75, %76, "
-        "%77, %78, %79, %80, %81, %82, %83, %84, %85, %86, %87, %88, %89, %90, %91, %92, %93, %94, %95}, [%128+64];\n\t"
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%96, %97, %98, %99, %100, %101, %102, %103, %104, %105, %106, %107, "
-        "%108, %109, %110, %111, %112, %113, %114, %115, %116, %117, %118, %119, %120, %121, %122, %123, %124, %125, "
-        "%126, %127}, [%128+96];\n\t"
+        "%45, %46, %47, %48, %49, %50, %51, %52, %53, %54, %55, %56, %57, %58, %59, %60, %61, %62, %63}, [%64+32];\n\t"
         "tcgen05.wait::ld.sync.aligned;"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
           "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
@@ -185,16 +183,7 @@ __device__ __forceinline__ void tmem_ld128(uint32_t taddr, uint32_t (&r)[128]) {
           "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]),
           "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]),
           "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]), "=r"(r[56]),
-          "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63]), "=r"(r[64]),
-          "=r"(r[65]), "=r"(r[66]), "=r"(r[67]), "=r"(r[68]), "=r"(r[69]), "=r"(r[70]), "=r"(r[71]), "=r"(r[72]),
-          "=r"(r[73]), "=r"(r[74]), "=r"(r[75]), "=r"(r[76]), "=r"(r[77]), "=r"(r[78]), "=r"(r[79]), "=r"(r[80]),
-          "=r"(r[81]), "=r"(r[82]), "=r"(r[83]), "=r"(r[84]), "=r"(r[85]), "=r"(r[86]), "=r"(r[87]), "=r"(r[88]),
-          "=r"(r[89]), "=r"(r[90]), "=r"(r[91]), "=r"(r[92]), "=r"(r[93]), "=r"(r[94]), "=r"(r[95]), "=r"(r[96]),
-          "=r"(r[97]), "=r"(r[98]), "=r"(r[99]), "=r"(r[100]), "=r"(r[101]), "=r"(r[102]), "=r"(r[103]),
-          "=r"(r[104]), "=r"(r[105]), "=r"(r[106]), "=r"(r[107]), "=r"(r[108]), "=r"(r[109]), "=r"(r[110]),
-          "=r"(r[111]), "=r"(r[112]), "=r"(r[113]), "=r"(r[114]), "=r"(r[115]), "=r"(r[116]), "=r"(r[117]),
-          "=r"(r[118]), "=r"(r[119]), "=r"(r[120]), "=r"(r[121]), "=r"(r[122]), "=r"(r[123]), "=r"(r[124]),
-          "=r"(r[125]), "=r"(r[126]), "=r"(r[127])
+          "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
         : "r"(taddr)
         : "memory");
 }
@@ -221,6 +210,19 @@ __device__ __forceinline__ float fmin3(float a, float b, float c) {
     return d;
 }
 
+// Order-preserving encoding of a float key as an unsigned word (unsigned
+// comparison of encodings = float comparison of keys), so that a shared bound
+// can be lowered with atomicMin.
+__host__ __device__ __forceinline__ uint32_t key_enc(float f) {
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float key_dec(uint32_t e) {
+    return __uint_as_float((e & 0x80000000u) ? (e & 0x7FFFFFFFu) : ~e);
+}
+constexpr uint32_t kNoBound = 0xFF800000u;   // key_enc(+infinity)
+
 // Exact form of the search (see the file comment), from the flags and value
 // ranges of the dataset and of the dense queries.
 __device__ __forceinline__ bool exact_form(const KnnState* ds, const KnnState* qs, int D) {
@@ -241,6 +243,7 @@ struct KnnArgs {
     const unsigned int* n_dense;
     const KnnState* dstate;
     const KnnState* qstate;
+    unsigned int* qbound;             // [dense position] shared key bound of the exact form (key_enc)
     const float* w_exact;
     const float* w_bound;
     float* part_key;
@@ -256,17 +259,20 @@ __device__ __forceinline__ int owner_cta(long long p, long long U, int G) {
 }
 
 // MQ queries per tile (MQ / 128 MMAs of M = 128 share each point tile of BN
-// points), NEPI epilogue warps (one query each per lane: 32 * NEPI == MQ).
+// points), NEPI epilogue warps: each lane keeps one query's list over one of
+// the NCH column slices of the tile (32 * NEPI == MQ * NCH).
 template <int BN, int MQ, int NEPI, bool kExact>
 __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
     k_knn_tc(const __grid_constant__ CUtensorMap tm_qh, const __grid_constant__ CUtensorMap tm_ql,
              const __grid_constant__ CUtensorMap tm_xh, const __grid_constant__ CUtensorMap tm_xl,
              const __grid_constant__ CUtensorMap tm_bm, KnnArgs a) {
-    constexpr int NT = 32 * NEPI;          // list-keeping threads, one query each
+    constexpr int NT = 32 * NEPI;          // list-keeping threads: one (query, column slice) each
     constexpr int MH = MQ / KM;            // M = 128 halves of the query tile
+    constexpr int NCH = NT / MQ;           // column slices of a tile
+    constexpr int CW = BN / NCH;           // columns per slice
     constexpr int BW = BN / 32;            // membership words per query row and point tile
     constexpr uint32_t kTmemCols = 2 * MH * BN;
-    static_assert(NT == MQ && BW == 4, "one list per query; four membership words per tile row");
+    static_assert(NCH * MQ == NT && CW == 64, "64-column slices, one list per (query, slice)");
     // the other form's kernel runs (the exact one only where it was launched)
     if ((a.exact_launched && exact_form(a.dstate, a.qstate, a.D)) != kExact) return;
     const unsigned int nd = *a.n_dense;
@@ -348,7 +354,7 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
             if (qt != cur_qt) {
                 ++j;
                 cur_qt = qt;
-                if (j >= 1 && !bar_wait(a_empty, (uint32_t)((j - 1) & 1), abort_flag, a.err, true)) break;
+                if (j >= 1 && !bar_wait(a_empty, (uint32_t)((j - 1) & 1), abort_flag, a.err)) break;
                 bar_expect_tx(a_full, qbytes * (need_ql ? 2u : 1u));
                 for (int k = 0; k < atoms; ++k) {
                     tma_2d(sQh + (size_t)k * MQ * 128, &tm_qh, a_full, k * 64, (int)(qt * MQ));
@@ -356,7 +362,7 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
                 }
             }
             const int s = (int)(i % ops);
-            if (i >= ops && !bar_wait(empty_op + s, (uint32_t)((i / ops - 1) & 1), abort_flag, a.err, true)) break;
+            if (i >= ops && !bar_wait(empty_op + s, (uint32_t)((i / ops - 1) & 1), abort_flag, a.err)) break;
             unsigned char* xs = sX + (size_t)s * op_stride;
             bar_expect_tx(full_op + s, xbytes * (need_xl ? 2u : 1u));
             for (int k = 0; k < atoms; ++k) {
@@ -364,7 +370,7 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
                 if (need_xl) tma_2d(xs + xbytes + (size_t)k * BN * 128, &tm_xl, full_op + s, k * 64, (int)(pt * BN));
             }
             const int e = (int)(i % eps);
-            if (i >= eps && !bar_wait(empty_ep + e, (uint32_t)((i / eps - 1) & 1), abort_flag, a.err, true)) break;
+            if (i >= eps && !bar_wait(empty_ep + e, (uint32_t)((i / eps - 1) & 1), abort_flag, a.err)) break;
             unsigned char* es = sE + (size_t)e * ep_stride;
             bar_expect_tx(full_ep + e, ep_stride);
             tma_2d(es, &tm_bm, full_ep + e, (int)(pt * BW), (int)(qt * MQ));
@@ -386,6 +392,8 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
         // kind::f16: FP32 accumulator, bf16 A and B, both K-major, N = BN, M = 128.
         const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
                                ((uint32_t)(KM >> 4) << 24);
+        const uint64_t qhdesc = desc_sw128(smem_addr(sQh)), qldesc = desc_sw128(smem_addr(sQl));
+        const uint64_t xdesc = desc_sw128(smem_addr(sX));
         long long cur_qt = -1;
         int j = -1;
         long long i = 0;
@@ -395,24 +403,26 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
                 if (j >= 0) mma_commit(a_empty);
                 ++j;
                 cur_qt = qt;
-                if (!bar_wait(a_full, (uint32_t)(j & 1), abort_flag, a.err, true)) break;
+                if (!bar_wait(a_full, (uint32_t)(j & 1), abort_flag, a.err)) break;
             }
             const int acc = (int)(i & 1);
-            if (i >= 2 && !bar_wait(tempty + acc, (uint32_t)(((i >> 1) - 1) & 1), abort_flag, a.err, true)) break;
+            if (i >= 2 && !bar_wait(tempty + acc, (uint32_t)(((i >> 1) - 1) & 1), abort_flag, a.err)) break;
             const int s = (int)(i % ops);
-            if (!bar_wait(full_op + s, (uint32_t)((i / ops) & 1), abort_flag, a.err, true)) break;
+            if (!bar_wait(full_op + s, (uint32_t)((i / ops) & 1), abort_flag, a.err)) break;
             fence_after();
-            const uint32_t qh = smem_addr(sQh), ql = smem_addr(sQl);
-            const uint32_t xh = smem_addr(sX + (size_t)s * op_stride), xl = xh + xbytes;
+            // descriptors advance by adding the byte offset / 16 to their
+            // start-address field (shared addresses stay below 2^18: no carry)
+            const uint64_t dxh = xdesc + (uint64_t)(s * (op_stride >> 4)), dxl = dxh + (xbytes >> 4);
             for (int hq = 0; hq < MH; ++hq) {
                 const uint32_t d = tmem + (uint32_t)((acc * MH + hq) * BN);
+#pragma unroll 4
                 for (int ks = 0; ks < ksteps; ++ks) {
-                    const uint32_t ao = (uint32_t)((ks >> 2) * MQ * 128 + hq * KM * 128 + (ks & 3) * 32);
-                    const uint32_t bo = (uint32_t)((ks >> 2) * BN * 128 + (ks & 3) * 32);
-                    mma_bf16(d, desc_sw128(qh + ao), desc_sw128(xh + bo), idesc, ks > 0 ? 1u : 0u);
+                    const uint64_t ao = (uint64_t)(((ks >> 2) * MQ * 128 + hq * KM * 128 + (ks & 3) * 32) >> 4);
+                    const uint64_t bo = (uint64_t)(((ks >> 2) * BN * 128 + (ks & 3) * 32) >> 4);
+                    mma_bf16(d, qhdesc + ao, dxh + bo, idesc, ks > 0 ? 1u : 0u);
                     if (!kExact) {
-                        if (need_xl) mma_bf16(d, desc_sw128(qh + ao), desc_sw128(xl + bo), idesc, 1u);
-                        if (need_ql) mma_bf16(d, desc_sw128(ql + ao), desc_sw128(xh + bo), idesc, 1u);
+                        if (need_xl) mma_bf16(d, qhdesc + ao, dxl + bo, idesc, 1u);
+                        if (need_ql) mma_bf16(d, qldesc + ao, dxh + bo, idesc, 1u);
                     }
                 }
             }
@@ -425,8 +435,9 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
     } else if (warp >= 2) {
         // ---- epilogue: ranking keys, per-query lists ----
         const int ew = warp - 2;
-        const int quad = warp & 3;
-        const int hq = ew >> 2;                       // query half (its own accumulator)
+        const int quad = warp & 3;                    // TMEM lanes this warp may read
+        const int hq = (ew >> 2) % MH;                // query half (its own accumulator)
+        const int ch = (ew >> 2) / MH;                // column slice
         const int row = hq * KM + quad * 32 + lane;   // query of the tile
         const int lt = ew * 32 + lane;
         float* mk = lkey + lt;
@@ -435,14 +446,19 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
         float thr = INFINITY;
         long long cur_qt = -1;
         long long i = 0;
+        // Exact form: the lists of one query (column slices, CTAs) share a
+        // bound in global memory, the smallest K-th key of any full list (an
+        // upper bound of the query's K-th key: that list holds K candidates at
+        // or below it). A candidate above it cannot be in the top-K; one equal
+        // to it still enters (it may win the tie on its id).
         auto flush = [&](long long qt) {
-            const long long set = (long long)blockIdx.x + qt;
-            const long long lb = set * (long long)Kl;
+            const long long lst = ((long long)blockIdx.x + qt) * NCH + ch;
+            const long long lb = lst * (long long)Kl;
             for (int k = 0; k < n; ++k) {
                 a.part_key[(lb + k) * MQ + row] = mk[k * NT];
                 a.part_id[(lb + k) * MQ + row] = mi[k * NT];
             }
-            a.part_n[set * MQ + row] = n;
+            a.part_n[lst * MQ + row] = n;
         };
         for (long long p = p0; p < p1; ++p, ++i) {
             const long long qt = p / ntp, pt = p - qt * ntp;
@@ -456,20 +472,23 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
             const int e = (int)(i % eps);
             // every lane waits (and so sees the copied data); the warp leaves
             // together if any lane gave up, since tcgen05.ld is warp-wide
-            const bool ok = bar_wait(tfull + acc, (uint32_t)((i >> 1) & 1), abort_flag, a.err, false) &&
-                            bar_wait(full_ep + e, (uint32_t)((i / eps) & 1), abort_flag, a.err, false);
+            const bool ok = bar_wait(tfull + acc, (uint32_t)((i >> 1) & 1), abort_flag, a.err) &&
+                            bar_wait(full_ep + e, (uint32_t)((i / eps) & 1), abort_flag, a.err);
             if (!__all_sync(0xffffffffu, ok)) break;
             fence_after();
             const unsigned char* es = sE + (size_t)e * ep_stride;
-            const uint4 mw = *reinterpret_cast<const uint4*>(es + (size_t)row * BW * 4);
-            const float* wv = reinterpret_cast<const float*>(es + bm_bytes);
-            const uint32_t id0 = (uint32_t)(pt * BN);
-            const uint32_t tbase = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)((acc * MH + hq) * BN);
-            uint32_t r[128];
-            tmem_ld128(tbase, r);
+            const int gq = (int)qt * MQ + row;   // dense position of this lane's query
+            const float ext = kExact ? key_dec(__ldcg(a.qbound + gq)) : INFINITY;
+            const uint2 mw = *reinterpret_cast<const uint2*>(es + (size_t)row * BW * 4 + ch * 8);   // 2 words: 64 columns
+            const float* wv = reinterpret_cast<const float*>(es + bm_bytes) + ch * CW;
+            const uint32_t id0 = (uint32_t)(pt * BN + ch * CW);
+            const uint32_t tbase =
+                tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)((acc * MH + hq) * BN + ch * CW);
+            uint32_t r[64];
+            tmem_ld64(tbase, r);
             // keys t = w - 2 q.x (packed FMA, in place)
 #pragma unroll
-            for (int j = 0; j < 128; j += 4) {
+            for (int j = 0; j < 64; j += 4) {
                 const float4 w4 = *reinterpret_cast<const float4*>(wv + j);
                 const float2 a = __ffma2_rn(make_float2(-2.0f, -2.0f),
                                             make_float2(__uint_as_float(r[j]), __uint_as_float(r[j + 1])),
@@ -483,8 +502,8 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
                 r[j + 3] = __float_as_uint(b.y);
             }
 #pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                const uint32_t mbits = c == 0 ? mw.x : c == 1 ? mw.y : c == 2 ? mw.z : mw.w;
+            for (int c = 0; c < 2; ++c) {
+                const uint32_t mbits = c == 0 ? mw.x : mw.y;
                 const uint32_t* rc = r + c * 32;
                 float mm[11];
 #pragma unroll
@@ -493,17 +512,20 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
                 mm[10] = fminf(__uint_as_float(rc[30]), __uint_as_float(rc[31]));
                 const float m = fmin3(fmin3(mm[0], mm[1], mm[2]), fmin3(mm[3], mm[4], mm[5]),
                                       fmin3(fmin3(mm[6], mm[7], mm[8]), mm[9], mm[10]));
-                if (m < thr && mbits) {
+                if (m < thr && !(m > ext) && mbits) {
                     // this lane's candidate columns whose key beats its list;
                     // lanes insert in parallel, each into its own sorted list
                     uint32_t pm = 0;
 #pragma unroll
-                    for (int k = 0; k < 32; ++k) pm |= (__uint_as_float(rc[k]) < thr ? 1u : 0u) << k;
+                    for (int k = 0; k < 32; ++k) {
+                        const float v = __uint_as_float(rc[k]);
+                        pm |= (v < thr && !(v > ext) ? 1u : 0u) << k;
+                    }
                     pm &= mbits;
                     for (; pm; pm &= pm - 1) {
                         const int k = __ffs((int)pm) - 1;
                         const float key = select32(rc, k);
-                        if (!(key < thr)) continue;
+                        if (!(key < thr) || key > ext) continue;
                         // ids arrive in ascending order, so a key equal to a
                         // listed one goes after it
                         int pos = n < Kl ? n : Kl - 1;
@@ -519,6 +541,7 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
                     }
                 }
             }
+            if (kExact && n == Kl && thr < ext) atomicMin(a.qbound + gq, key_enc(thr));
             fence_before();
             __syncwarp();
             if (lane == 0) {
@@ -545,7 +568,8 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
 __global__ void k_knn_rows(const float* __restrict__ src, int D, int Dp, const int* __restrict__ list,
                            const unsigned int* __restrict__ count, int64_t n, int64_t pad, int pad_to,
                            __nv_bfloat16* __restrict__ xh, __nv_bfloat16* __restrict__ xl, float* __restrict__ sq,
-                           float* __restrict__ wb, float C, KnnState* __restrict__ st) {
+                           float* __restrict__ wb, float C, KnnState* __restrict__ st,
+                           unsigned int* __restrict__ bound) {
     const int lane = threadIdx.x & 31;
     const int64_t nrows = count ? (int64_t)*count : n;
     const int64_t npad = count ? ((nrows + pad_to - 1) / pad_to) * pad_to : pad;
@@ -553,6 +577,7 @@ __global__ void k_knn_rows(const float* __restrict__ src, int D, int Dp, const i
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     int flags = 0, mneg = 0, mpos = 0;
     for (int64_t r = w0; r < npad; r += nw) {
+        if (bound && lane == 0) bound[r] = kNoBound;
         if (r >= nrows) {
             if (r < n || count) {   // operand rows exist only up to the buffer's rows
                 for (int d = lane; d < Dp; d += 32) {
@@ -651,7 +676,9 @@ __global__ void __launch_bounds__(32 * MERGE_WARPS) k_knn_merge(KnnSearch k) {
     const int K = k.K;
     const int Kl = exact ? k.kl_exact : k.kl_bound;
     const int MQ = exact ? kMqExact : kMqBound;
-    const long long ntp = (k.N + kBn - 1) / kBn;
+    const int NCH = exact ? kNchExact : kNchBound;
+    const int BN = exact ? kBnExact : kBnBound;
+    const long long ntp = (k.N + BN - 1) / BN;
     const long long nqt = ((long long)nd + MQ - 1) / MQ;
     const long long U = nqt * ntp;
     const int G = (int)min((long long)k.grid, U);
@@ -669,8 +696,8 @@ __global__ void __launch_bounds__(32 * MERGE_WARPS) k_knn_merge(KnnSearch k) {
         uint32_t thr_i = 0;
         float minlast = INFINITY;   // smallest last bound over the full lists
         for (int c = c0; c <= c1; ++c) {
-            {
-                const long long lst = (long long)c + qt;
+            for (int h = 0; h < NCH; ++h) {   // the column slices
+                const long long lst = ((long long)c + qt) * NCH + h;
                 const int cnt = k.part_n[lst * MQ + r];
                 const long long lb = lst * (long long)Kl;
                 if (!exact && cnt == Kl)
@@ -748,27 +775,28 @@ bool knn_map(CUtensorMap* m, const void* ptr, CUtensorMapDataType dt, int esize,
 }
 
 size_t knn_smem(bool exact, int Dp, int Kl, int ops, int eps) {
-    const int MQ = exact ? kMqExact : kMqBound;
+    const int MQ = exact ? kMqExact : kMqBound, BN = exact ? kBnExact : kBnBound;
+    const int nepi = exact ? kNepiExact : kNepiBound;
     const size_t q = (size_t)MQ * Dp * 2 * (exact ? 1 : 2);
-    const size_t op = (size_t)kBn * Dp * 2 * (exact ? 1 : 2);
-    const size_t ep = (size_t)MQ * (kBn / 32) * 4 + (size_t)kBn * 4;
-    const size_t lists = (size_t)MQ * Kl * 8;
+    const size_t op = (size_t)BN * Dp * 2 * (exact ? 1 : 2);
+    const size_t ep = (size_t)MQ * (BN / 32) * 4 + (size_t)BN * 4;
+    const size_t lists = (size_t)32 * nepi * Kl * 8;   // one list per (query, column slice)
     const size_t bars = 8 * (7 + 2 * ops + 2 * eps) + 16;
     return 1024 + q + ops * op + eps * ep + lists + bars;
 }
 
-template <int MQ, int NEPI, bool kExact>
+template <int BN, int MQ, int NEPI, bool kExact>
 cudaError_t launch_knn_form(const KnnSearch& k, const CUtensorMap& mxh, const CUtensorMap& mxl, cudaStream_t s) {
     static std::atomic<size_t> cap{0};
     const size_t smem = kExact ? k.smem_exact : k.smem_bound;
     if (smem > cap.load()) {
-        const cudaError_t e = cudaFuncSetAttribute(k_knn_tc<kBn, MQ, NEPI, kExact>,
+        const cudaError_t e = cudaFuncSetAttribute(k_knn_tc<BN, MQ, NEPI, kExact>,
                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         cap = smem;
     }
     CUtensorMap mbm, mqh, mql;
-    if (!knn_map(&mbm, k.bm, CU_TENSOR_MAP_DATA_TYPE_UINT32, 4, (uint64_t)k.nwp, (uint64_t)k.Qcap, kBn / 32, MQ,
+    if (!knn_map(&mbm, k.bm, CU_TENSOR_MAP_DATA_TYPE_UINT32, 4, (uint64_t)k.nwp, (uint64_t)k.Qcap, BN / 32, MQ,
                  false) ||
         !knn_map(&mqh, k.qh, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (uint64_t)k.Dp, (uint64_t)k.Qcap, 64, MQ, true) ||
         !knn_map(&mql, k.ql, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (uint64_t)k.Dp, (uint64_t)k.Qcap, 64, MQ, true))
@@ -778,8 +806,8 @@ cudaError_t launch_knn_form(const KnnSearch& k, const CUtensorMap& mxh, const CU
     a.D = k.D;
     a.Dp = k.Dp;
     a.exact_launched = k.exact_possible;
-    a.ntp_exact = (k.N + kBn - 1) / kBn;
-    a.ntp_bound = (k.N + kBn - 1) / kBn;
+    a.ntp_exact = (k.N + kBnExact - 1) / kBnExact;
+    a.ntp_bound = (k.N + kBnBound - 1) / kBnBound;
     a.kl_exact = k.kl_exact;
     a.kl_bound = k.kl_bound;
     a.op_stages = kExact ? k.ops_exact : k.ops_bound;
@@ -787,13 +815,14 @@ cudaError_t launch_knn_form(const KnnSearch& k, const CUtensorMap& mxh, const CU
     a.n_dense = k.n_dense;
     a.dstate = k.dstate;
     a.qstate = k.qstate;
+    a.qbound = k.qbound;
     a.w_exact = k.w_exact;
     a.w_bound = k.w_bound;
     a.part_key = k.part_key;
     a.part_id = k.part_id;
     a.part_n = k.part_n;
     a.err = k.err;
-    k_knn_tc<kBn, MQ, NEPI, kExact><<<k.grid, 64 + 32 * NEPI, smem, s>>>(mqh, mql, mxh, mxl, mbm, a);
+    k_knn_tc<BN, MQ, NEPI, kExact><<<k.grid, 64 + 32 * NEPI, smem, s>>>(mqh, mql, mxh, mxl, mbm, a);
     return cudaGetLastError();
 }
 
@@ -845,9 +874,11 @@ bool knn_plan(KnnSearch& k, int max_smem) {
 }
 
 size_t knn_part_lists(const KnnSearch& k) {
-    // list sets blockIdx.x + query tile < grid + Qcap / MQ, MQ rows each:
-    // at most (grid + Qcap / 128) * 256 in either form
-    return (size_t)(k.grid + k.Qcap / KM) * kMqExact;
+    // list sets blockIdx.x + query tile < grid + Qcap / MQ, with MQ rows and
+    // NCH column slices each
+    const size_t e = (size_t)(k.grid + k.Qcap / kMqExact) * kMqExact * kNchExact;
+    const size_t b = (size_t)(k.grid + k.Qcap / kMqBound) * kMqBound * kNchBound;
+    return std::max(e, b);
 }
 size_t knn_part_entries(const KnnSearch& k) {
     return knn_part_lists(k) * (size_t)std::max(k.kl_exact, k.kl_bound);
@@ -857,7 +888,7 @@ cudaError_t launch_knn_rows_dataset(const float* X, int64_t N, int D, int Dp, vo
                                     float* w_bound, int64_t pad, float C, KnnState* st, cudaStream_t s) {
     const int blocks = (int)std::min<int64_t>((pad * 32 + 255) / 256, 152 * 16);
     k_knn_rows<<<blocks, 256, 0, s>>>(X, D, Dp, nullptr, nullptr, N, pad, 1, static_cast<__nv_bfloat16*>(xh),
-                                      static_cast<__nv_bfloat16*>(xl), w_exact, w_bound, C, st);
+                                      static_cast<__nv_bfloat16*>(xl), w_exact, w_bound, C, st, nullptr);
     return cudaGetLastError();
 }
 
@@ -866,20 +897,24 @@ int knn_launches(const KnnSearch& k) { return 3 + (k.exact_possible ? 1 : 0); }
 cudaError_t launch_knn_search(const KnnSearch& k, cudaStream_t s) {
     // query rows in dense-list order, zero rows up to the next tile
     const int qblocks = (int)std::min<int64_t>(((int64_t)k.Qcap * 32 + 255) / 256, 152 * 8);
-    k_knn_rows<<<qblocks, 256, 0, s>>>(k.queries, k.D, k.Dp, k.dense_q, k.n_dense, 0, 0, kMqExact,
+    k_knn_rows<<<qblocks, 256, 0, s>>>(k.queries, k.D, k.Dp, k.dense_q, k.n_dense, 0, 0, std::max(kMqExact, kMqBound),
                                        static_cast<__nv_bfloat16*>(k.qh), static_cast<__nv_bfloat16*>(k.ql), k.qsq,
-                                       k.qbase, k.C, k.qstate);
+                                       k.qbase, k.C, k.qstate, k.qbound);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    CUtensorMap mxh, mxl;
-    if (!knn_map(&mxh, k.xh, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (uint64_t)k.Dp, (uint64_t)k.N, 64, kBn, true) ||
-        !knn_map(&mxl, k.xl, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (uint64_t)k.Dp, (uint64_t)k.N, 64, kBn, true))
-        return cudaErrorNotSupported;
     if (k.exact_possible) {
-        e = launch_knn_form<kMqExact, 8, true>(k, mxh, mxh, s);
+        CUtensorMap mxh;
+        if (!knn_map(&mxh, k.xh, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (uint64_t)k.Dp, (uint64_t)k.N, 64, kBnExact,
+                     true))
+            return cudaErrorNotSupported;
+        e = launch_knn_form<kBnExact, kMqExact, kNepiExact, true>(k, mxh, mxh, s);
         if (e != cudaSuccess) return e;
     }
-    e = launch_knn_form<kMqBound, 4, false>(k, mxh, mxl, s);
+    CUtensorMap mxh, mxl;
+    if (!knn_map(&mxh, k.xh, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (uint64_t)k.Dp, (uint64_t)k.N, 64, kBnBound, true) ||
+        !knn_map(&mxl, k.xl, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (uint64_t)k.Dp, (uint64_t)k.N, 64, kBnBound, true))
+        return cudaErrorNotSupported;
+    e = launch_knn_form<kBnBound, kMqBound, kNepiBound, false>(k, mxh, mxl, s);
     if (e != cudaSuccess) return e;
     const int mblocks = (int)std::min<int64_t>(((int64_t)k.Qcap + MERGE_WARPS - 1) / MERGE_WARPS, 152 * 16);
     k_knn_merge<<<mblocks, 32 * MERGE_WARPS, 0, s>>>(k);

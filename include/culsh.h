@@ -249,7 +249,10 @@ int culsh_search_profile_get(culsh_search* s, culsh_search_profile* out);
  *    64 MiB (Q = 10,000 with L=16, M=12, T=16 uses 18 MB), else
  *    CULSH_ERR_CAPACITY; a single query's candidate set must fit the arena;
  *  - the first call on a device looks up the array's address: make it before
- *    any stream capture;
+ *    any stream capture; the address is kept for the process, so a
+ *    cudaDeviceReset while the library is loaded is not supported;
+ *  - the call synchronises `stream` and returns when d_ids / d_dists hold the
+ *    results (it reads counters back to admit large candidate sets in rounds);
  *  - calls share the array: calls that overlap on the GPU race, serialise them;
  *  - stream NULL is the legacy default stream; the search object's getters
  *    are not updated (results go only to d_ids / d_dists). */

@@ -50,13 +50,18 @@ def build() -> str:
     return _LIB_PATH
 
 
+# Where the reference tree is read from by the `ref` recipe (the only place
+# that reads it); CULSH_REFERENCE_TREE overrides it.
+REFERENCE_TREE = os.environ.get("CULSH_REFERENCE_TREE", "/root/reference")
+
+
 def build_ref() -> str | None:
     """Compile the reference's kernel file for the host into oracle/_ref when
     the reference tree is present (the Makefile's `ref` target); returns the
     library path, or None when it was not built."""
     srcs = [os.path.join(_HERE, f) for f in ("ref_kernels_host.cpp", "ref_shim.h")]
     if not os.path.exists(_REF_PATH) or os.path.getmtime(_REF_PATH) < max(os.path.getmtime(f) for f in srcs):
-        subprocess.run(["make", "-s", "-C", _HERE, "ref"], check=True)
+        subprocess.run(["make", "-s", "-C", _HERE, "ref", f"REF={REFERENCE_TREE}"], check=True)
     return _REF_PATH if os.path.exists(_REF_PATH) else None
 
 
