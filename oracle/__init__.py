@@ -12,7 +12,9 @@ Parity status: the reference ships no tests, fixtures or CPU path, and its
 build needs a GPU. The oracle is pinned against the reference's own kernel
 file compiled for the host (``make -C oracle ref`` into ``oracle/_ref``, run
 by ``ref_kernels()``: projection epilogue, multiprobe enumeration, top-K
-heap, distances), where the reference tree is present, and by hand-traced known answers
+heap, distances), against the reference's index-side host code built on
+Thrust's CPP backend (``ref_index()``: row sort, bucket boundaries, index
+file load/save), where the reference tree is present, and by hand-traced known answers
 and an independent transliteration (tests/refsim.py).
 """
 
@@ -28,9 +30,11 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "build", "liboracle.so")
 _REF_PATH = os.path.join(_HERE, "_ref", "libref_kernels.so")
+_REF_INDEX_PATH = os.path.join(_HERE, "_ref", "libref_index.so")
 _lock = threading.Lock()
 _lib = None
 _ref = None
+_ref_index = None
 
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 _f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
@@ -56,11 +60,14 @@ REFERENCE_TREE = os.environ.get("CULSH_REFERENCE_TREE", "/root/reference")
 
 
 def build_ref() -> str | None:
-    """Compile the reference's kernel file for the host into oracle/_ref when
-    the reference tree is present (the Makefile's `ref` target); returns the
-    library path, or None when it was not built."""
-    srcs = [os.path.join(_HERE, f) for f in ("ref_kernels_host.cpp", "ref_shim.h")]
-    if not os.path.exists(_REF_PATH) or os.path.getmtime(_REF_PATH) < max(os.path.getmtime(f) for f in srcs):
+    """Compile the reference's kernel file and its index-side host code for the
+    host into oracle/_ref when the reference tree is present (the Makefile's
+    `ref` target); returns the kernel library's path, or None when it was not
+    built."""
+    srcs = [os.path.join(_HERE, f) for f in ("ref_kernels_host.cpp", "ref_shim.h", "ref_index_host.cpp",
+                                               "ref_index_shim.h", "Makefile")]
+    newest = max(os.path.getmtime(f) for f in srcs)
+    if any(not os.path.exists(p) or os.path.getmtime(p) < newest for p in (_REF_PATH, _REF_INDEX_PATH)):
         subprocess.run(["make", "-s", "-C", _HERE, "ref", f"REF={REFERENCE_TREE}"], check=True)
     return _REF_PATH if os.path.exists(_REF_PATH) else None
 
@@ -84,6 +91,25 @@ def ref_kernels():
             R.ref_distances.argtypes = [_f32p, _int, _int, _f32p, _int, _u32p, _u32p, ctypes.c_uint, _f32p]
             _ref = R
     return _ref
+
+
+def ref_index():
+    """The reference's index-side host code (row sort, bucket boundaries,
+    HashTables load/save) built on Thrust's CPP backend (oracle/_ref), or
+    None when it was not built here or does not load on this machine."""
+    global _ref_index
+    with _lock:
+        if _ref_index is None:
+            if not os.path.exists(_REF_INDEX_PATH):
+                return None
+            try:
+                R = ctypes.CDLL(_REF_INDEX_PATH)
+            except OSError:
+                return None
+            R.ref_sort_buckets.argtypes = [_f32p, _int, _int, _u32p, _u32p, _u32p, _u32p]
+            R.ref_load_save.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
+            _ref_index = R
+    return _ref_index
 
 
 def lib():

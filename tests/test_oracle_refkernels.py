@@ -128,3 +128,111 @@ def test_distances():
         np.testing.assert_array_equal(want, out, err_msg=f"D={D}")
         pairs += total
     assert pairs > 1000
+
+
+# --- index side: the reference's row sort, bucket boundaries and index file,
+# built on Thrust's CPP backend (oracle/_ref/libref_index.so) ---
+
+ref_idx = oracle.ref_index()
+needs_ref_index = pytest.mark.skipif(ref_idx is None, reason="oracle/_ref index library not built")
+
+
+def ref_buckets(P):
+    """P: one table's floored codes [M, N] (the reference's N x M column-major)
+    -> (ids, starts, sizes) from radixSortRows_1matrix + calculateBuckets."""
+    M, N = P.shape
+    perm = np.zeros(N, np.uint32)
+    starts = np.zeros(N, np.uint32)
+    sizes = np.zeros(N, np.uint32)
+    nb = np.zeros(1, np.uint32)
+    assert ref_idx.ref_sort_buckets(np.ascontiguousarray(P, np.float32), N, M, perm, starts, sizes, nb) == 0
+    B = int(nb[0])
+    return perm, starts[:B], sizes[:B]
+
+
+def oracle_buckets(P):
+    M, N = P.shape
+    ids, starts, sizes = (np.zeros(N, np.uint32) for _ in range(3))
+    codes = np.zeros(N * M, np.float32)
+    B = oracle.lib().oracle_bucket_table(np.ascontiguousarray(P, np.float32), N, M, ids, starts, sizes, codes)
+    return ids, starts[:B], sizes[:B], codes[:B * M].reshape(M, B)
+
+
+@needs_ref_index
+@pytest.mark.parametrize("name", golden_cases())
+def test_golden_tables_against_reference_sort(name):
+    """Every table of every golden index: the reference's own row sort and
+    bucket boundaries, run on the oracle's floored projection, give the
+    golden ids, starts and sizes, and the codes the golden file holds are
+    the rows those ids point at."""
+    c = load_case(name)
+    L, M, _ = c["A"].shape
+    v = np.floor(oracle.project(c["X"], c["A"], c["b"], float(c["W"])))
+    for l in range(L):
+        P = v[l * M:(l + 1) * M]
+        ids, starts, sizes = ref_buckets(P)
+        np.testing.assert_array_equal(ids, c[f"ids_{l}"], err_msg=f"table {l}")
+        np.testing.assert_array_equal(starts, c[f"starts_{l}"], err_msg=f"table {l}")
+        np.testing.assert_array_equal(sizes, c[f"sizes_{l}"], err_msg=f"table {l}")
+        np.testing.assert_array_equal(P[:, ids[starts]], c[f"codes_{l}"], err_msg=f"table {l}")
+
+
+@needs_ref_index
+def test_sort_buckets_random():
+    """The oracle's bucket table equals the reference's sort and boundaries
+    on random code matrices: N from 1 to 5000, M from 1 to 40, codes drawn
+    from a few values (large buckets), a wide range (mostly singletons) or
+    mixed signs with zeros, all rows equal, and the values of float32 near
+    the integer limits."""
+    rng = np.random.default_rng(21)
+    cases = 0
+    for trial in range(120):
+        N, M = int(rng.integers(1, 5000)), int(rng.integers(1, 41))
+        kind = trial % 5
+        if kind == 0:
+            P = rng.integers(-2, 2, (M, N))
+        elif kind == 1:
+            P = rng.integers(-10**6, 10**6, (M, N))
+        elif kind == 2:
+            P = rng.integers(-3, 4, (M, N)) * rng.integers(0, 2, (M, N))
+        elif kind == 3:
+            P = np.full((M, N), float(rng.integers(-5, 5)))
+        else:
+            P = rng.choice([-2.0**24, -1.0, 0.0, 1.0, 2.0**24, 2.0**31], (M, N))
+        P = P.astype(np.float32)
+        ids, starts, sizes = ref_buckets(P)
+        oids, ostarts, osizes, ocodes = oracle_buckets(P)
+        np.testing.assert_array_equal(oids, ids, err_msg=f"N={N} M={M} kind={kind}")
+        np.testing.assert_array_equal(ostarts, starts, err_msg=f"N={N} M={M} kind={kind}")
+        np.testing.assert_array_equal(osizes, sizes, err_msg=f"N={N} M={M} kind={kind}")
+        np.testing.assert_array_equal(ocodes, P[:, ids[starts]], err_msg=f"N={N} M={M} kind={kind}")
+        cases += 1
+    assert cases == 120
+
+
+@needs_ref_index
+@pytest.mark.parametrize("name", golden_cases())
+def test_index_file_through_reference_load_save(name, tmp_path):
+    """An index file the oracle writes is read by the reference's
+    HashTables::load and written back by its HashTables::save byte for
+    byte: the file layout (header, A, b, per-table buckets, ids, starts,
+    sizes, codes) is the reference's."""
+    c = load_case(name)
+    idx = oracle.build_index(c["X"], c["A"], c["b"], float(c["W"]))
+    src, out = tmp_path / "oracle.bin", tmp_path / "reference.bin"
+    idx.save(str(src))
+    assert ref_idx.ref_load_save(str(src).encode(), str(out).encode()) == 0
+    assert src.read_bytes() == out.read_bytes()
+
+
+@needs_ref_index
+def test_golden_index_file_through_reference_load_save(tmp_path):
+    """The committed golden index file (odd_d13.index.bin) survives the
+    reference's load and save unchanged."""
+    import os
+    from conftest import GOLDEN
+    src = os.path.join(GOLDEN, "odd_d13.index.bin")
+    out = tmp_path / "reference.bin"
+    assert ref_idx.ref_load_save(src.encode(), str(out).encode()) == 0
+    with open(src, "rb") as f:
+        assert f.read() == out.read_bytes()
