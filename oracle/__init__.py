@@ -14,7 +14,9 @@ file compiled for the host (``make -C oracle ref`` into ``oracle/_ref``, run
 by ``ref_kernels()``: projection epilogue, multiprobe enumeration, top-K
 heap, distances), against the reference's index-side host code built on
 Thrust's CPP backend (``ref_index()``: row sort, bucket boundaries, index
-file load/save), where the reference tree is present, and by hand-traced known answers
+file load/save), against the reference's whole index and search path built
+the same way (``ref_pipeline()``), where the reference tree is present, and
+by hand-traced known answers
 and an independent transliteration (tests/refsim.py).
 """
 
@@ -31,10 +33,12 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "build", "liboracle.so")
 _REF_PATH = os.path.join(_HERE, "_ref", "libref_kernels.so")
 _REF_INDEX_PATH = os.path.join(_HERE, "_ref", "libref_index.so")
+_REF_PIPELINE_PATH = os.path.join(_HERE, "_ref", "libref_pipeline.so")
 _lock = threading.Lock()
 _lib = None
 _ref = None
 _ref_index = None
+_ref_pipeline = None
 
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 _f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
@@ -65,9 +69,11 @@ def build_ref() -> str | None:
     `ref` target); returns the kernel library's path, or None when it was not
     built."""
     srcs = [os.path.join(_HERE, f) for f in ("ref_kernels_host.cpp", "ref_shim.h", "ref_index_host.cpp",
-                                               "ref_index_shim.h", "Makefile")]
+                                               "ref_index_shim.h", "ref_pipeline_host.cpp", "ref_pipeline_shim.h",
+                                               "Makefile", "oracle.cpp")]
     newest = max(os.path.getmtime(f) for f in srcs)
-    if any(not os.path.exists(p) or os.path.getmtime(p) < newest for p in (_REF_PATH, _REF_INDEX_PATH)):
+    outs = (_REF_PATH, _REF_INDEX_PATH, _REF_PIPELINE_PATH)
+    if any(not os.path.exists(p) or os.path.getmtime(p) < newest for p in outs):
         subprocess.run(["make", "-s", "-C", _HERE, "ref", f"REF={REFERENCE_TREE}"], check=True)
     return _REF_PATH if os.path.exists(_REF_PATH) else None
 
@@ -110,6 +116,58 @@ def ref_index():
             R.ref_load_save.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
             _ref_index = R
     return _ref_index
+
+
+def ref_pipeline_lib():
+    """The reference's whole index and search path built for the host
+    (oracle/_ref/libref_pipeline.so: Thrust's CPP backend, its kernels run as
+    host loops, the oracle's chain for its one GEMM), or None when it was not
+    built here or does not load on this machine."""
+    global _ref_pipeline
+    with _lock:
+        if _ref_pipeline is None:
+            if not os.path.exists(_REF_PIPELINE_PATH):
+                return None
+            try:
+                R = ctypes.CDLL(_REF_PIPELINE_PATH)
+            except OSError:
+                return None
+            R.ref_pipeline.argtypes = [_f32p, _int, _int, _int, _int, _flt, _f32p, _f32p, _f32p, _int, _int, _int,
+                                       ctypes.c_ulonglong, _u32p, _u32p, _u32p, _u32p, _f32p, _i32p, _i32p, _f32p,
+                                       _u32p]
+            _ref_pipeline = R
+    return _ref_pipeline
+
+
+def ref_pipeline(X, A, b, W, queries, K, T, free_bytes=0):
+    """Index X and search the queries with the reference's own host-built
+    code. Returns a dict shaped like search() (plus the index arrays and
+    totals), or raises RuntimeError with the stage that failed."""
+    R = ref_pipeline_lib()
+    if R is None:
+        raise RuntimeError("oracle/_ref/libref_pipeline.so is not built")
+    X = _c(X, np.float32)
+    A = _c(A, np.float32)
+    b = _c(b, np.float32)
+    queries = _c(queries, np.float32)
+    L, M, D = A.shape
+    N, Q = X.shape[0], queries.shape[0]
+    buckets = np.zeros(L, np.uint32)
+    ids = np.zeros((L, N), np.uint32)
+    starts = np.zeros((L, N), np.uint32)
+    sizes = np.zeros((L, N), np.uint32)
+    codes = np.zeros((L, N * M), np.float32)
+    qb = np.zeros((L, Q * T), np.int32)
+    kid = np.zeros((Q, K), np.int32)
+    kd = np.zeros((Q, K), np.float32)
+    totals = np.zeros(2, np.uint32)
+    rc = R.ref_pipeline(X, N, D, L, M, float(W), A, b, queries, Q, int(K), int(T), int(free_bytes),
+                        buckets, ids, starts, sizes, codes, qb, kid, kd, totals)
+    if rc != 0:
+        raise RuntimeError(f"reference pipeline failed at stage {rc} (1 reset, 2 index, 3 search)")
+    return {"index": Index(N, D, L, M, W, A, b, buckets, ids, starts, sizes, codes),
+            "qbuckets": qb, "knn_ids": kid, "knn_dists": kd,
+            "nonunique_total": int(totals[0]), "unique_total": int(totals[1])}
 
 
 def lib():
