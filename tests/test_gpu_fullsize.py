@@ -1,6 +1,8 @@
 """Full-size parity: the 100k x 128 Gaussian-mixture workload and the
 1M x 128 integer-feature workload, index and search compared bit for bit
-against the CPU oracle, plus size-independent properties of the index."""
+against the CPU oracle, plus size-independent properties of the index; the
+4M x 128 Zipf-cluster and 10M x 96 serving workloads through whole-table,
+sampled-point and search comparisons."""
 
 import numpy as np
 import pytest
@@ -67,4 +69,83 @@ def test_full_size_against_oracle(culsh, config):
         assert st.getTotalCandidates_nonUnique() == int(want["nonunique"].sum())
     # every near-data query of the mixture workload finds candidates
     if config == 1:
+        assert st.getTotalCandidates_unique() > 0
+
+
+def gpu_index_arrays(ht, N, L, M):
+    """The index the GPU built, packed as the oracle packs its own."""
+    buckets = np.asarray(ht.getBuckets(), np.uint32)
+    ids = np.zeros((L, N), np.uint32)
+    starts = np.zeros((L, N), np.uint32)
+    sizes = np.zeros((L, N), np.uint32)
+    codes = np.zeros((L, N * M), np.float32)
+    for l in range(L):
+        B = int(buckets[l])
+        ids[l] = ht.getBuckets_totalIndices(l)
+        starts[l, :B] = ht.getBuckets_startingIndices(l)
+        sizes[l, :B] = ht.getBuckets_sizes(l)
+        codes[l, :B * M] = ht.getBuckets_codes(l).reshape(-1)
+    return buckets, ids, starts, sizes, codes
+
+
+@pytest.mark.parametrize("config", [4, 5])
+def test_full_size_large_configs(culsh, config):
+    """The 4M x 128 Zipf-cluster workload (heavy-tailed candidate counts:
+    work stealing, dense candidates, overflow) and the 10M x 96 serving
+    mixture at full size. Two whole tables are compared with the oracle's;
+    in every table the bucket of 20,000 sampled points carries the oracle's
+    floored projection of that point; every table passes the index
+    properties; and 500 queries (300 held out, 200 near data points, which
+    find candidates) are
+    searched at the workload's K and T, compared bit for bit with the
+    oracle's search over the same index."""
+    X, Qm, A, b, cfg = synth.dataset(config)
+    N, D, L, M, W = X.shape[0], cfg.D, cfg.L, cfg.M, cfg.W
+    ht = culsh.HashTables()
+    ht.reset(N, D, L, M, W, A=A, b=b)
+    ht.index(X)
+    index_properties(ht, N, M)
+    buckets, ids, starts, sizes, codes = gpu_index_arrays(ht, N, L, M)
+
+    pick = [0, L - 1]
+    ref = oracle.build_index(X, A[pick], b[pick], W)
+    for j, l in enumerate(pick):
+        B = int(buckets[l])
+        assert B == int(ref.buckets[j])
+        np.testing.assert_array_equal(ids[l], ref.ids(j), err_msg=f"table {l}")
+        np.testing.assert_array_equal(starts[l, :B], ref.starts(j), err_msg=f"table {l}")
+        np.testing.assert_array_equal(sizes[l, :B], ref.sizes(j), err_msg=f"table {l}")
+        np.testing.assert_array_equal(codes[l, :B * M].reshape(M, B), ref.codes(j), err_msg=f"table {l}")
+    del ref
+
+    rng = np.random.default_rng(7)
+    pts = np.sort(rng.choice(N, 20_000, replace=False))
+    P = np.floor(oracle.project(X[pts], A, b, W))
+    pos = np.empty(N, np.int64)
+    for l in range(L):
+        B = int(buckets[l])
+        pos[ids[l]] = np.arange(N)
+        bucket = np.searchsorted(starts[l, :B], pos[pts], side="right") - 1
+        np.testing.assert_array_equal(codes[l, :B * M].reshape(M, B)[:, bucket], P[l * M:(l + 1) * M],
+                                      err_msg=f"table {l}")
+
+    idx = oracle.Index(N, D, L, M, W, A, b, buckets, ids, starts, sizes, codes)
+    # near-data queries: at the serving workload's W = 5 with M = 14 even a
+    # point 0.5 away per coordinate rarely shares a bucket, so those stay closer
+    noise = 0.5 if config == 4 else 0.05
+    near = (X[rng.integers(0, N, 200)] + rng.normal(0, noise, (200, D))).astype(np.float32)
+    queries = np.ascontiguousarray(np.concatenate([Qm[:300], near]))
+    Q = queries.shape[0]
+    st = culsh.SearchTables()
+    runs = [(cfg.K, cfg.T), (cfg.K, 1)] if config == 4 else [(10, 8), (100, 32)]
+    for K, T in runs:
+        st.reset(ht, K, T)
+        st.search(queries, dataset=X)
+        want = oracle.search(idx, X, queries, K, T)
+        np.testing.assert_array_equal(st.getKnnIds(), want["knn_ids"], err_msg=f"K={K} T={T}")
+        np.testing.assert_array_equal(st.getKnnDistances(), want["knn_dists"], err_msg=f"K={K} T={T}")
+        for l in range(L):
+            np.testing.assert_array_equal(st.getQueryBuckets(l), want["qbuckets"][l].reshape(Q, T))
+        assert st.getTotalCandidates_unique() == int(want["unique"].sum())
+        assert st.getTotalCandidates_nonUnique() == int(want["nonunique"].sum())
         assert st.getTotalCandidates_unique() > 0
