@@ -491,6 +491,17 @@ def named_point(culsh, torch, dev, Xt, d, A, b, Qm, steps, warmup):
     ht = culsh.HashTables()
     ht.reset(N, D, L, M, d["W"], A=A, b=b)
     ht.index_device(Xt.data_ptr(), sp)
+    # the index build at this W (every point its own bucket: 96-bit keys)
+    build_ms = []
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        ht.index_device(Xt.data_ptr(), sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        build_ms.append(e0.elapsed_time(e1))
+    build_profile = ht.profile()
     qt = torch.from_numpy(Qm).to(dev)
     torch.cuda.synchronize()
     ids = torch.empty((Q, K), dtype=torch.int32, device=dev)
@@ -505,7 +516,11 @@ def named_point(culsh, torch, dev, Xt, d, A, b, Qm, steps, warmup):
     ms = timed_searches(st, torch, stream, sp, qt, Q, ids, dists, flush, steps)
     return ht, {"workload": f"int-features-1m-d128 N={N} L={L} M={M} W={d['W']:g} T={T} K={K} Q={Q}",
                 "qps": round(Q / (ms / 1e3), 1), "ms_per_step": round(ms, 4),
-                "candidates_unique_per_query": st.getTotalCandidates_unique() / Q}
+                "candidates_unique_per_query": st.getTotalCandidates_unique() / Q,
+                "index_build_ms": round(statistics.median(build_ms), 3),
+                "index_build_stages_ms": {k: (round(v, 4) if isinstance(v, float) else v)
+                                          for k, v in build_profile.items()},
+                "buckets_per_table": int(np.median(ht.getBuckets()))}
 
 
 def run_culsh(args):

@@ -72,7 +72,8 @@ class _Tuning(ctypes.Structure):
 class _IndexProfile(ctypes.Structure):
     _fields_ = [("project_ms", ctypes.c_float), ("pack_ms", ctypes.c_float), ("sort_ms", ctypes.c_float),
                 ("bucket_ms", ctypes.c_float), ("total_ms", ctypes.c_float), ("tensor_cores", ctypes.c_int),
-                ("recomputed", ctypes.c_longlong), ("key_words", ctypes.c_int), ("sort_passes", ctypes.c_int)]
+                ("recomputed", ctypes.c_longlong), ("key_words", ctypes.c_int), ("sort_passes", ctypes.c_int),
+                ("sort_form", ctypes.c_int)]
 
 
 class _ServerConfig(ctypes.Structure):

@@ -187,6 +187,12 @@ struct culsh_index {
     cudaEvent_t bev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};   // build stage boundaries
     bool built_once = false;
     DevBuf<uint32_t> ws_keys[2], ws_vals, ws_hist, ws_base, ws_status, ws_tcnt, ws_toff, ws_nb;
+    PinBuf<uint32_t> h_sort_hist;
+    DevBuf<unsigned long long> ws_run_pos;
+    DevBuf<uint32_t> ws_run_len;
+    DevBuf<unsigned int> ws_run_cnt;
+    PinBuf<unsigned int> h_run_cnt;
+    int sort_form = 0;   // 1: top-word passes + run ordering, 2: that form fell back to all words, 0: all words
 
     ~culsh_index() {
         for (auto& e : bev)
@@ -571,6 +577,80 @@ int project_tensor_cores(culsh_index* ix, const float* dX, cudaStream_t st, bool
     return CULSH_OK;
 }
 
+// Orders every table's points by packed key (ties by id), the order of the
+// reference's LSD row sort (cuLSH_Indexing.cu:71-93). Multi-word keys first
+// take the digit passes over the top word alone (moving 8 bytes per point a
+// pass instead of 4 (KW + 1)), gather the lower words into sorted order, and
+// order each run of equal top words by (lower words, id); a run longer than
+// run_max_len() or more runs than the lists hold sends the build through the
+// passes over every word instead. On return *skeys holds the sorted keys
+// ([KW][L*N]) and ix->ids the sorted ids.
+int sort_keys(culsh_index* ix, int N, int passes, cudaStream_t st, const uint32_t** skeys) {
+    const int L = ix->L, KW = ix->KW;
+    const size_t LN = (size_t)L * N;
+    SortBuffers sb;
+    sb.keys[0] = ix->ws_keys[0].p;
+    sb.keys[1] = ix->ws_keys[1].p;
+    sb.vals[0] = ix->ids.p;
+    sb.vals[1] = ix->ws_vals.p;
+    sb.hist = ix->ws_hist.p;
+    sb.base = ix->ws_base.p;
+    sb.status = ix->ws_status.p;
+    sb.err = ix->err.p;
+    sb.h_hist = ix->h_sort_hist.p;
+    sb.h_hist_words = ix->h_sort_hist.n;
+    const int top_passes = passes - 4 * (KW - 1);
+    ix->sort_form = 0;
+    if (KW >= 2 && top_passes >= 1 && !getenv("CULSH_SORT_ALL_WORDS")) {
+        SortBuffers sa = sb;
+        sa.keys[0] = ix->ws_keys[0].p + (KW - 1) * LN;   // read first, then a ping-pong slot
+        sa.keys[1] = ix->ws_keys[1].p + (KW - 1) * LN;
+        bool alt = false;
+        CU_TRY(run_segmented_sort(sa, N, L, 1, top_passes, &alt, st));
+        const uint32_t* top = alt ? sa.keys[1] : sa.keys[0];
+        if (alt) ix->ids.swap(ix->ws_vals);
+        // ws_keys[0]'s lower words are still in point order; its top slot may
+        // hold sorted top words (read before being overwritten: other buffer)
+        CU_TRY(launch_gather_lower(ix->ws_keys[0].p, ix->ids.p, top, N, L, KW, ix->ws_keys[1].p, st));
+        const unsigned int scap = (unsigned int)std::min<size_t>(LN / 2 + 1, (size_t)1 << 22);
+        const unsigned int lcap = (unsigned int)std::min<size_t>(LN / 33 + 1, (size_t)1 << 18);
+        CU_TRY(ix->ws_run_pos.reserve((size_t)scap + lcap));
+        CU_TRY(ix->ws_run_len.reserve((size_t)scap + lcap));
+        CU_TRY(ix->ws_run_cnt.reserve(4));
+        CU_TRY(ix->h_run_cnt.reserve(4));
+        RunLists rl;
+        rl.spos = ix->ws_run_pos.p;
+        rl.slen = ix->ws_run_len.p;
+        rl.scap = scap;
+        rl.lpos = ix->ws_run_pos.p + scap;
+        rl.llen = ix->ws_run_len.p + scap;
+        rl.lcap = lcap;
+        rl.cnt = ix->ws_run_cnt.p;
+        const uint32_t* stop = ix->ws_keys[1].p + (KW - 1) * LN;
+        CU_TRY(launch_run_find(stop, N, L, rl, st));
+        CU_TRY(cudaMemcpyAsync(ix->h_run_cnt.p, rl.cnt, 4 * sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
+        CU_TRY(cudaStreamSynchronize(st));
+        const unsigned int* hc = ix->h_run_cnt.p;
+        if (hc[2] == 0) {
+            CU_TRY(launch_run_sorts(rl, hc[0], hc[1], N, L, KW, ix->ws_keys[1].p, ix->ids.p, st));
+            ix->sort_form = 1;
+            *skeys = ix->ws_keys[1].p;
+            return CULSH_OK;
+        }
+        // a run too long to order in shared memory: repack, sort every word
+        CU_TRY(launch_pack_keys(ix->ws_codes.p, N, L, ix->M, KW, ix->cmin.p, ix->fbits.p, ix->foff.p,
+                                ix->ws_keys[0].p, ix->ids.p, st));
+        sb.vals[0] = ix->ids.p;
+        sb.vals[1] = ix->ws_vals.p;
+        ix->sort_form = 2;
+    }
+    bool alt = false;
+    CU_TRY(run_segmented_sort(sb, N, L, KW, passes, &alt, st));
+    *skeys = ix->ws_keys[alt ? 1 : 0].p;
+    if (alt) ix->ids.swap(ix->ws_vals);
+    return CULSH_OK;
+}
+
 // Index build from a device-resident dataset (cuLSH_HashTables.cu:486-520).
 int build_device(culsh_index* ix, const float* dX, cudaStream_t st, FILE* dbg) {
     const int N = ix->N, D = ix->D, L = ix->L, M = ix->M, LM = L * M;
@@ -621,21 +701,11 @@ int build_device(culsh_index* ix, const float* dX, cudaStream_t st, FILE* dbg) {
     CU_TRY(ix->ws_hist.reserve((size_t)L * hp * 256));
     CU_TRY(ix->ws_base.reserve((size_t)L * hp * 256));
     CU_TRY(ix->ws_status.reserve(sort_status_words(N, L)));
-    SortBuffers sb;
-    sb.keys[0] = ix->ws_keys[0].p;
-    sb.keys[1] = ix->ws_keys[1].p;
-    sb.vals[0] = ix->ids.p;
-    sb.vals[1] = ix->ws_vals.p;
-    sb.hist = ix->ws_hist.p;
-    sb.base = ix->ws_base.p;
-    sb.status = ix->ws_status.p;
-    sb.err = ix->err.p;
-    bool alt = false;
+    CU_TRY(ix->h_sort_hist.reserve((size_t)L * hp * 256));
     CU_TRY(cudaEventRecord(ix->bev[2], st));
-    CU_TRY(run_segmented_sort(sb, N, L, ix->KW, passes, &alt, st));
+    const uint32_t* skeys = nullptr;
+    TRY(sort_keys(ix, N, passes, st, &skeys));
     CU_TRY(cudaEventRecord(ix->bev[3], st));
-    const uint32_t* skeys = ix->ws_keys[alt ? 1 : 0].p;
-    if (alt) ix->ids.swap(ix->ws_vals);
 
     // Run-length bucketing.
     const int tiles = (N + 4095) / 4096;
@@ -1765,6 +1835,7 @@ int culsh_index_profile_get(culsh_index* ix, culsh_index_profile* out) {
     out->recomputed = ix->tc_recomputed;
     out->key_words = ix->KW;
     out->sort_passes = ix->sort_passes;
+    out->sort_form = ix->sort_form;
     return CULSH_OK;
 }
 

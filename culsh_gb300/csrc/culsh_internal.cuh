@@ -219,10 +219,31 @@ struct SortBuffers {
     uint32_t* base;      // [L][passes][256]
     uint32_t* status;    // [L*tiles][256] + counter
     int* err;
+    uint32_t* h_hist = nullptr;   // pinned host copy of hist (allocated per call when absent or short)
+    size_t h_hist_words = 0;
 };
 size_t sort_status_words(int64_t N, int L);
 cudaError_t run_segmented_sort(SortBuffers& sb, int64_t N, int L, int KW, int passes, bool* result_in_alt,
                                cudaStream_t st);
+
+// Top-word-first ordering (sort.cu): after the digit passes over the top key
+// word, gather the lower words into sorted order, find the runs of equal top
+// words and order each run by (lower words, id).
+struct RunLists {
+    unsigned long long* spos;   // runs of 2..32: first sorted position (table * N + i)
+    uint32_t* slen;
+    unsigned int scap;
+    unsigned long long* lpos;   // runs of 33..run_max_len()
+    uint32_t* llen;
+    unsigned int lcap;
+    unsigned int* cnt;          // [4]: small runs, large runs, overflow flags (1 run too long, 2 list full)
+};
+cudaError_t launch_gather_lower(const uint32_t* keys0, const uint32_t* ids, const uint32_t* top, int64_t N, int L,
+                                int KW, uint32_t* skeys, cudaStream_t st);
+cudaError_t launch_run_find(const uint32_t* top, int64_t N, int L, const RunLists& rl, cudaStream_t st);
+cudaError_t launch_run_sorts(const RunLists& rl, unsigned int nsmall, unsigned int nlarge, int64_t N, int L, int KW,
+                             uint32_t* skeys, uint32_t* ids, cudaStream_t st);
+int run_max_len();
 
 // Run-length bucketing of sorted keys. Two phases: count (per table bucket
 // totals, written to nb[L]) and write (starts, ukeys).

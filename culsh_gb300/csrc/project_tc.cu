@@ -730,8 +730,10 @@ cudaError_t launch_tc_recompute(const float* X, int64_t N, int D, int LM, const 
         if (e != cudaSuccess) return e;
     }
     // Grid: a multiple of the region count, so that every block has a region.
+    // 512 threads: with A staged (up to ~100 KB at L*M = 192, D = 128) two
+    // blocks fit an SM, 32 warps to cover the latency of the X row loads.
     const int grid = regions * (stage_a ? 2 : 8);
-    k_tc_recompute<<<grid, 256, stage_a ? smem : 0, st>>>(
+    k_tc_recompute<<<grid, 512, stage_a ? smem : 0, st>>>(
         X, N, D, A, b, W, list, cap, cnt, regions, LM, stage_a, codes, cmin, cmax, err);
     return cudaGetLastError();
 }

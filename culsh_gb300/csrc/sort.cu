@@ -33,6 +33,7 @@ constexpr uint32_t ST_PRE = 2u << 30;       // inclusive prefix published
 constexpr uint32_t ST_CNT = (1u << 30) - 1;
 constexpr int HIST_CHUNK = 8192;
 constexpr uint32_t kSpinLimit = 1u << 22;
+constexpr int kRunMax = 2048;               // longest run of equal top words ordered in shared memory
 
 __device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
     uint32_t v;
@@ -262,6 +263,174 @@ __global__ void __launch_bounds__(NT, 3) k_sort_pass(const uint32_t* __restrict_
     }
 }
 
+// ---- Top-word-first ordering ----
+// The digit passes can run over the key's top word alone (its leading
+// columns), moving that word and the ids. The lower words of every sorted
+// position are then gathered from the packed keys in point order, and each run
+// of equal top words is ordered by (lower words, id): the LSD passes leave a
+// run's ids ascending, so this is the order the full sort produces.
+
+// skeys[w][i] = keys0[w][table + ids[i]] for the lower words w < KW - 1; the
+// sorted top words are copied into skeys' top slot unless they are there.
+__global__ void k_gather_lower(const uint32_t* __restrict__ keys0, const uint32_t* __restrict__ ids,
+                               const uint32_t* top, int64_t N, int L, int KW, uint32_t* skeys) {
+    const int64_t LN = (int64_t)L * N;
+    uint32_t* stop = skeys + (int64_t)(KW - 1) * LN;
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < LN;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t seg = (idx / N) * N;
+        const uint32_t id = ids[idx];
+        for (int w = 0; w < KW - 1; ++w) skeys[w * LN + idx] = __ldg(keys0 + w * LN + seg + id);
+        if (top != stop) stop[idx] = top[idx];
+    }
+}
+
+// Runs of two or more equal top words, found from their first element: runs
+// of up to 32 go to the small list, longer ones up to kRunMax to the large
+// list; a longer run or a full list sets *over (the caller then sorts all
+// words instead).
+__global__ void k_run_find(const uint32_t* __restrict__ top, int64_t N, int L, unsigned long long* __restrict__ spos,
+                           uint32_t* __restrict__ slen, unsigned int scap, unsigned long long* __restrict__ lpos,
+                           uint32_t* __restrict__ llen, unsigned int lcap, unsigned int* __restrict__ cnt) {
+    const int64_t LN = (int64_t)L * N;
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < LN;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = idx % N;
+        if (i + 1 >= N) continue;
+        const uint32_t v = top[idx];
+        if (top[idx + 1] != v || (i > 0 && top[idx - 1] == v)) continue;
+        int64_t j = i + 2;
+        while (j < N && j - i <= kRunMax && top[idx + (j - i)] == v) ++j;
+        const int64_t len = j - i;
+        if (len > kRunMax) {
+            atomicOr(cnt + 2, 1u);
+            continue;
+        }
+        if (len <= 32) {
+            const unsigned int k = atomicAdd(cnt + 0, 1u);
+            if (k < scap) {
+                spos[k] = (unsigned long long)idx;
+                slen[k] = (uint32_t)len;
+            } else {
+                atomicOr(cnt + 2, 2u);
+            }
+        } else {
+            const unsigned int k = atomicAdd(cnt + 1, 1u);
+            if (k < lcap) {
+                lpos[k] = (unsigned long long)idx;
+                llen[k] = (uint32_t)len;
+            } else {
+                atomicOr(cnt + 2, 2u);
+            }
+        }
+    }
+}
+
+// (lower words from the most significant down, then id) of a < of b
+template <int KWL>
+__device__ __forceinline__ bool run_less(const uint32_t (&a)[KWL + 1], const uint32_t (&b)[KWL + 1]) {
+#pragma unroll
+    for (int k = KWL - 1; k >= 0; --k)
+        if (a[k] != b[k]) return a[k] < b[k];
+    return a[KWL] < b[KWL];
+}
+
+// One warp per run of at most 32: a bitonic sort across the lanes (missing
+// lanes hold all-ones, above every element: ids are below 2^32 - 1).
+template <int KWL>
+__global__ void k_run_sort_small(const unsigned long long* __restrict__ spos, const uint32_t* __restrict__ slen,
+                                 const unsigned int* __restrict__ cnt, unsigned int scap, int64_t LN,
+                                 uint32_t* __restrict__ skeys, uint32_t* __restrict__ ids) {
+    const int lane = threadIdx.x & 31;
+    const unsigned int nrun = min(cnt[0], scap);
+    for (unsigned int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < nrun;
+         r += (gridDim.x * blockDim.x) >> 5) {
+        const int64_t pos = (int64_t)spos[r];
+        const int len = (int)slen[r];
+        uint32_t e[KWL + 1];
+#pragma unroll
+        for (int k = 0; k <= KWL; ++k) e[k] = 0xFFFFFFFFu;
+        if (lane < len) {
+#pragma unroll
+            for (int k = 0; k < KWL; ++k) e[k] = skeys[k * LN + pos + lane];
+            e[KWL] = ids[pos + lane];
+        }
+#pragma unroll
+        for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                uint32_t o[KWL + 1];
+#pragma unroll
+                for (int c = 0; c <= KWL; ++c) o[c] = __shfl_xor_sync(0xffffffffu, e[c], j);
+                const bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
+                const bool o_less = run_less<KWL>(o, e);
+                if (o_less == keep_min) {
+#pragma unroll
+                    for (int c = 0; c <= KWL; ++c) e[c] = o[c];
+                }
+            }
+        }
+        if (lane < len) {
+#pragma unroll
+            for (int k = 0; k < KWL; ++k) skeys[k * LN + pos + lane] = e[k];
+            ids[pos + lane] = e[KWL];
+        }
+    }
+}
+
+// One block per run of 33 to kRunMax elements: a bitonic sort in shared memory.
+template <int KWL>
+__global__ void __launch_bounds__(NT) k_run_sort_large(const unsigned long long* __restrict__ lpos,
+                                                      const uint32_t* __restrict__ llen,
+                                                      const unsigned int* __restrict__ cnt, unsigned int lcap,
+                                                      int64_t LN, uint32_t* __restrict__ skeys,
+                                                      uint32_t* __restrict__ ids) {
+    __shared__ uint32_t sv[KWL + 1][kRunMax];
+    const unsigned int nrun = min(cnt[1], lcap);
+    for (unsigned int r = blockIdx.x; r < nrun; r += gridDim.x) {
+        const int64_t pos = (int64_t)lpos[r];
+        const int len = (int)llen[r];
+        int n2 = 64;
+        while (n2 < len) n2 <<= 1;
+        for (int t = threadIdx.x; t < n2; t += NT) {
+#pragma unroll
+            for (int k = 0; k < KWL; ++k) sv[k][t] = t < len ? skeys[k * LN + pos + t] : 0xFFFFFFFFu;
+            sv[KWL][t] = t < len ? ids[pos + t] : 0xFFFFFFFFu;
+        }
+        __syncthreads();
+        for (int k = 2; k <= n2; k <<= 1) {
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int t = threadIdx.x; t < n2; t += NT) {
+                    const int u = t ^ j;
+                    if (u > t) {
+                        uint32_t a[KWL + 1], b[KWL + 1];
+#pragma unroll
+                        for (int c = 0; c <= KWL; ++c) {
+                            a[c] = sv[c][t];
+                            b[c] = sv[c][u];
+                        }
+                        const bool asc = (t & k) == 0;
+                        if (run_less<KWL>(b, a) == asc) {
+#pragma unroll
+                            for (int c = 0; c <= KWL; ++c) {
+                                sv[c][t] = b[c];
+                                sv[c][u] = a[c];
+                            }
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        for (int t = threadIdx.x; t < len; t += NT) {
+#pragma unroll
+            for (int k = 0; k < KWL; ++k) skeys[k * LN + pos + t] = sv[k][t];
+            ids[pos + t] = sv[KWL][t];
+        }
+        __syncthreads();
+    }
+}
+
 __device__ __forceinline__ bool key_differs(const uint32_t* keys, int64_t LN, int64_t a, int64_t b, int KW) {
     for (int w = 0; w < KW; ++w)
         if (keys[w * LN + a] != keys[w * LN + b]) return true;
@@ -298,31 +467,42 @@ __global__ void k_rl_scan(const uint32_t* __restrict__ tile_cnt, int tiles, uint
     if (threadIdx.x == 0) nb[l] = carry;
 }
 
+// Bucket starts and unique keys of one tile of 4,096 sorted positions: warp w
+// takes positions [512 w, 512 w + 512) as 16 rows of 32 lanes (coalesced key
+// loads), ranks its flagged positions with ballots, and the block scans the
+// warp totals; flagged positions are written in order.
 __global__ void k_rl_write(const uint32_t* __restrict__ keys, int64_t N, int L, int KW,
                            const uint32_t* __restrict__ tile_off, const uint64_t* __restrict__ boff,
                            uint32_t* __restrict__ starts, uint32_t* __restrict__ ukeys) {
     __shared__ uint32_t ws[SP_WARPS];
     const int l = blockIdx.y, tile = blockIdx.x, tiles = gridDim.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t LN = (int64_t)L * N, seg = (int64_t)l * N;
-    const int64_t i0 = (int64_t)tile * SP_TILE + threadIdx.x * SP_ITEMS;
-    uint32_t flags = 0, c = 0;
+    const int64_t w0 = (int64_t)tile * SP_TILE + (int64_t)warp * (32 * SP_ITEMS);
+    uint32_t ball[SP_ITEMS];
+    uint32_t c = 0;
 #pragma unroll
     for (int k = 0; k < SP_ITEMS; ++k) {
-        const int64_t i = i0 + k;
-        if (i < N && (i == 0 || key_differs(keys, LN, seg + i, seg + i - 1, KW))) {
-            flags |= 1u << k;
-            ++c;
-        }
+        const int64_t i = w0 + k * 32 + lane;
+        const bool f = i < N && (i == 0 || key_differs(keys, LN, seg + i, seg + i - 1, KW));
+        ball[k] = __ballot_sync(0xffffffffu, f);
+        c += __popc(ball[k]);
     }
-    uint32_t r = tile_off[(int64_t)l * tiles + tile] + block_excl_scan(c, ws, nullptr);
+    if (lane == 0) ws[warp] = c;
+    __syncthreads();
+    uint32_t r = tile_off[(int64_t)l * tiles + tile];
+    for (int w = 0; w < warp; ++w) r += ws[w];
     const uint64_t bo = boff[l];
-    while (flags) {
-        const int k = __ffs(flags) - 1;
-        flags &= flags - 1;
-        const int64_t i = i0 + k;
-        const uint64_t g = bo + r++;
-        starts[g] = (uint32_t)i;
-        for (int w = 0; w < KW; ++w) ukeys[g * KW + w] = keys[w * LN + seg + i];
+    const uint32_t below = (1u << lane) - 1u;
+#pragma unroll
+    for (int k = 0; k < SP_ITEMS; ++k) {
+        if ((ball[k] >> lane) & 1u) {
+            const int64_t i = w0 + k * 32 + lane;
+            const uint64_t g = bo + r + __popc(ball[k] & below);
+            starts[g] = (uint32_t)i;
+            for (int w = 0; w < KW; ++w) ukeys[g * KW + w] = keys[w * LN + seg + i];
+        }
+        r += __popc(ball[k]);
     }
 }
 
@@ -338,8 +518,17 @@ __global__ void k_bucket_sizes(const uint64_t* __restrict__ boff, const uint32_t
         sz = (uint32_t)(end - (int64_t)starts[g]);
         sizes[g] = sz;
     }
-    const uint32_t wmax = __reduce_max_sync(0xffffffffu, sz);   // largest bucket, one atomic per warp
-    if ((threadIdx.x & 31) == 0 && wmax) atomicMax(max_size, wmax);
+    // largest bucket: one atomic per block (one per warp serialises on the
+    // single address when every bucket is small and there are millions)
+    __shared__ uint32_t smax[SP_WARPS];
+    const uint32_t wmax = __reduce_max_sync(0xffffffffu, sz);
+    if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = wmax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t m = 0;
+        for (int w = 0; w < SP_WARPS; ++w) m = max(m, smax[w]);
+        if (m) atomicMax(max_size, m);
+    }
 }
 
 __global__ void k_hash_build(const uint64_t* __restrict__ boff, const uint32_t* __restrict__ ukeys, int M, int KW,
@@ -528,13 +717,14 @@ cudaError_t run_segmented_sort(SortBuffers& sb, int64_t N, int L, int KW, int pa
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     // Skip digit passes that are constant over every table (a stable pass
     // with one occupied bin is the identity).
-    uint32_t* h_hist = nullptr;
-    const size_t hbytes = sizeof(uint32_t) * L * passes * 256;
-    if ((e = cudaMallocHost(&h_hist, hbytes)) != cudaSuccess) return e;
+    const size_t hwords = (size_t)L * passes * 256, hbytes = sizeof(uint32_t) * hwords;
+    const bool own = sb.h_hist == nullptr || sb.h_hist_words < hwords;
+    uint32_t* h_hist = own ? nullptr : sb.h_hist;
+    if (own && (e = cudaMallocHost(&h_hist, hbytes)) != cudaSuccess) return e;
     if ((e = cudaMemcpyAsync(h_hist, sb.hist, hbytes, cudaMemcpyDeviceToHost, st)) == cudaSuccess)
         e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
-        cudaFreeHost(h_hist);
+        if (own) cudaFreeHost(h_hist);
         return e;
     }
     int cur = 0;
@@ -556,9 +746,52 @@ cudaError_t run_segmented_sort(SortBuffers& sb, int64_t N, int L, int KW, int pa
         if ((e = cudaGetLastError()) != cudaSuccess) break;
         cur ^= 1;
     }
-    cudaFreeHost(h_hist);
+    if (own) cudaFreeHost(h_hist);
     *result_in_alt = cur == 1;
     return e;
+}
+
+cudaError_t launch_gather_lower(const uint32_t* keys0, const uint32_t* ids, const uint32_t* top, int64_t N, int L,
+                                int KW, uint32_t* skeys, cudaStream_t st) {
+    const int64_t LN = (int64_t)L * N;
+    const int grid = (int)std::min<int64_t>((LN + NT - 1) / NT, 152 * 16);
+    k_gather_lower<<<grid, NT, 0, st>>>(keys0, ids, top, N, L, KW, skeys);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_run_find(const uint32_t* top, int64_t N, int L, const RunLists& rl, cudaStream_t st) {
+    const int64_t LN = (int64_t)L * N;
+    cudaError_t e = cudaMemsetAsync(rl.cnt, 0, 4 * sizeof(unsigned int), st);
+    if (e != cudaSuccess) return e;
+    const int grid = (int)std::min<int64_t>((LN + NT - 1) / NT, 152 * 16);
+    k_run_find<<<grid, NT, 0, st>>>(top, N, L, rl.spos, rl.slen, rl.scap, rl.lpos, rl.llen, rl.lcap, rl.cnt);
+    return cudaGetLastError();
+}
+
+int run_max_len() { return kRunMax; }
+
+cudaError_t launch_run_sorts(const RunLists& rl, unsigned int nsmall, unsigned int nlarge, int64_t N, int L, int KW,
+                             uint32_t* skeys, uint32_t* ids, cudaStream_t st) {
+    const int64_t LN = (int64_t)L * N;
+    const unsigned gs = (unsigned)std::min<unsigned long long>(((unsigned long long)nsmall * 32 + NT - 1) / NT, 152 * 32);
+    const unsigned gl = (unsigned)std::min<unsigned int>(nlarge, 152 * 4);
+    switch (KW - 1) {
+    case 1:
+        if (gs) k_run_sort_small<1><<<gs, NT, 0, st>>>(rl.spos, rl.slen, rl.cnt, rl.scap, LN, skeys, ids);
+        if (gl) k_run_sort_large<1><<<gl, NT, 0, st>>>(rl.lpos, rl.llen, rl.cnt, rl.lcap, LN, skeys, ids);
+        break;
+    case 2:
+        if (gs) k_run_sort_small<2><<<gs, NT, 0, st>>>(rl.spos, rl.slen, rl.cnt, rl.scap, LN, skeys, ids);
+        if (gl) k_run_sort_large<2><<<gl, NT, 0, st>>>(rl.lpos, rl.llen, rl.cnt, rl.lcap, LN, skeys, ids);
+        break;
+    case 3:
+        if (gs) k_run_sort_small<3><<<gs, NT, 0, st>>>(rl.spos, rl.slen, rl.cnt, rl.scap, LN, skeys, ids);
+        if (gl) k_run_sort_large<3><<<gl, NT, 0, st>>>(rl.lpos, rl.llen, rl.cnt, rl.lcap, LN, skeys, ids);
+        break;
+    default:
+        return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
 }
 
 cudaError_t launch_rl_count(const uint32_t* keys, int64_t N, int L, int KW, uint32_t* tile_cnt, uint32_t* tile_off,

@@ -111,6 +111,10 @@ typedef struct culsh_index_profile {
     long long recomputed;  /* codes its error bound left to the FP32 recomputation */
     int key_words;         /* 32-bit words of a packed bucket key                  */
     int sort_passes;       /* 8-bit digit passes over the keys                     */
+    int sort_form;         /* 1: passes over the top key word, then each run of    */
+                           /* equal top words ordered by its lower words and id;   */
+                           /* 2: that form met a run too long and sorted all words */
+                           /* again; 0: passes over all words (one-word keys)      */
 } culsh_index_profile;
 int culsh_index_profile_get(culsh_index* ix, culsh_index_profile* out);
 
