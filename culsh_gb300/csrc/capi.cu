@@ -612,18 +612,23 @@ int sort_keys(culsh_index* ix, int N, int passes, cudaStream_t st, const uint32_
         // ws_keys[0]'s lower words are still in point order; its top slot may
         // hold sorted top words (read before being overwritten: other buffer)
         CU_TRY(launch_gather_lower(ix->ws_keys[0].p, ix->ids.p, top, N, L, KW, ix->ws_keys[1].p, st));
-        const unsigned int scap = (unsigned int)std::min<size_t>(LN / 2 + 1, (size_t)1 << 22);
+        const unsigned int tcap = (unsigned int)std::min<size_t>(LN / 2 + 1, (size_t)1 << 23);
+        const unsigned int scap = (unsigned int)std::min<size_t>(LN / 9 + 1, (size_t)1 << 21);
         const unsigned int lcap = (unsigned int)std::min<size_t>(LN / 33 + 1, (size_t)1 << 18);
-        CU_TRY(ix->ws_run_pos.reserve((size_t)scap + lcap));
-        CU_TRY(ix->ws_run_len.reserve((size_t)scap + lcap));
+        const size_t rcap = (size_t)tcap + scap + lcap;
+        CU_TRY(ix->ws_run_pos.reserve(rcap));
+        CU_TRY(ix->ws_run_len.reserve(rcap));
         CU_TRY(ix->ws_run_cnt.reserve(4));
         CU_TRY(ix->h_run_cnt.reserve(4));
         RunLists rl;
-        rl.spos = ix->ws_run_pos.p;
-        rl.slen = ix->ws_run_len.p;
+        rl.tpos = ix->ws_run_pos.p;
+        rl.tlen = ix->ws_run_len.p;
+        rl.tcap = tcap;
+        rl.spos = ix->ws_run_pos.p + tcap;
+        rl.slen = ix->ws_run_len.p + tcap;
         rl.scap = scap;
-        rl.lpos = ix->ws_run_pos.p + scap;
-        rl.llen = ix->ws_run_len.p + scap;
+        rl.lpos = ix->ws_run_pos.p + tcap + scap;
+        rl.llen = ix->ws_run_len.p + tcap + scap;
         rl.lcap = lcap;
         rl.cnt = ix->ws_run_cnt.p;
         const uint32_t* stop = ix->ws_keys[1].p + (KW - 1) * LN;
@@ -631,8 +636,8 @@ int sort_keys(culsh_index* ix, int N, int passes, cudaStream_t st, const uint32_
         CU_TRY(cudaMemcpyAsync(ix->h_run_cnt.p, rl.cnt, 4 * sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
         CU_TRY(cudaStreamSynchronize(st));
         const unsigned int* hc = ix->h_run_cnt.p;
-        if (hc[2] == 0) {
-            CU_TRY(launch_run_sorts(rl, hc[0], hc[1], N, L, KW, ix->ws_keys[1].p, ix->ids.p, st));
+        if (hc[3] == 0) {
+            CU_TRY(launch_run_sorts(rl, hc, N, L, KW, ix->ws_keys[1].p, ix->ids.p, st));
             ix->sort_form = 1;
             *skeys = ix->ws_keys[1].p;
             return CULSH_OK;

@@ -230,19 +230,22 @@ cudaError_t run_segmented_sort(SortBuffers& sb, int64_t N, int L, int KW, int pa
 // word, gather the lower words into sorted order, find the runs of equal top
 // words and order each run by (lower words, id).
 struct RunLists {
-    unsigned long long* spos;   // runs of 2..32: first sorted position (table * N + i)
+    unsigned long long* tpos;   // runs of 2..8: first sorted position (table * N + i)
+    uint32_t* tlen;
+    unsigned int tcap;
+    unsigned long long* spos;   // runs of 9..32
     uint32_t* slen;
     unsigned int scap;
     unsigned long long* lpos;   // runs of 33..run_max_len()
     uint32_t* llen;
     unsigned int lcap;
-    unsigned int* cnt;          // [4]: small runs, large runs, overflow flags (1 run too long, 2 list full)
+    unsigned int* cnt;          // [4]: tiny, small and large runs; overflow flags (1 run too long, 2 list full)
 };
 cudaError_t launch_gather_lower(const uint32_t* keys0, const uint32_t* ids, const uint32_t* top, int64_t N, int L,
                                 int KW, uint32_t* skeys, cudaStream_t st);
 cudaError_t launch_run_find(const uint32_t* top, int64_t N, int L, const RunLists& rl, cudaStream_t st);
-cudaError_t launch_run_sorts(const RunLists& rl, unsigned int nsmall, unsigned int nlarge, int64_t N, int L, int KW,
-                             uint32_t* skeys, uint32_t* ids, cudaStream_t st);
+cudaError_t launch_run_sorts(const RunLists& rl, const unsigned int* counts, int64_t N, int L, int KW, uint32_t* skeys,
+                             uint32_t* ids, cudaStream_t st);
 int run_max_len();
 
 // Run-length bucketing of sorted keys. Two phases: count (per table bucket

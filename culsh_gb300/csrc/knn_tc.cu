@@ -486,6 +486,12 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
                 tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)((acc * MH + hq) * BN + ch * CW);
             uint32_t r[64];
             tmem_ld64(tbase, r);
+            // the accumulator slice is in registers: release it to the MMA
+            // warp now, so that the next products into it overlap this
+            // tile's key work
+            fence_before();
+            __syncwarp();
+            if (lane == 0) bar_arrive(tempty + acc);
             // keys t = w - 2 q.x (packed FMA, in place)
 #pragma unroll
             for (int j = 0; j < 64; j += 4) {
@@ -542,12 +548,8 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
                 }
             }
             if (kExact && n == Kl && thr < ext) atomicMin(a.qbound + gq, key_enc(thr));
-            fence_before();
             __syncwarp();
-            if (lane == 0) {
-                bar_arrive(tempty + acc);
-                bar_arrive(empty_ep + e);
-            }
+            if (lane == 0) bar_arrive(empty_ep + e);
         }
         if (cur_qt >= 0 && !*abort_flag) flush(cur_qt);
     }

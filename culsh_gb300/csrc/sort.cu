@@ -285,44 +285,52 @@ __global__ void k_gather_lower(const uint32_t* __restrict__ keys0, const uint32_
     }
 }
 
-// Runs of two or more equal top words, found from their first element: runs
-// of up to 32 go to the small list, longer ones up to kRunMax to the large
-// list; a longer run or a full list sets *over (the caller then sorts all
-// words instead).
-__global__ void k_run_find(const uint32_t* __restrict__ top, int64_t N, int L, unsigned long long* __restrict__ spos,
-                           uint32_t* __restrict__ slen, unsigned int scap, unsigned long long* __restrict__ lpos,
-                           uint32_t* __restrict__ llen, unsigned int lcap, unsigned int* __restrict__ cnt) {
+// Runs of two or more equal top words, found from their first element, go to
+// three lists by length: 2..8 (tiny), 9..32 (small), 33..kRunMax (large); a
+// longer run or a full list sets cnt[3] (the caller then sorts all words
+// instead). List slots are claimed with one atomic per warp and class.
+__device__ __forceinline__ void run_push(bool mine, unsigned int* cnt, unsigned long long* pos, uint32_t* len,
+                                         unsigned int cap, unsigned long long p, uint32_t n, unsigned int* over) {
+    const unsigned int act = __activemask();
+    const unsigned int m = __ballot_sync(act, mine);
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs((int)m) - 1;
+    unsigned int base = 0;
+    if (lane == leader) base = atomicAdd(cnt, (unsigned int)__popc(m));
+    base = __shfl_sync(act, base, leader);
+    if (mine) {
+        const unsigned int k = base + __popc(m & ((1u << lane) - 1u));
+        if (k < cap) {
+            pos[k] = p;
+            len[k] = n;
+        } else {
+            atomicOr(over, 2u);
+        }
+    }
+}
+
+__global__ void k_run_find(const uint32_t* __restrict__ top, int64_t N, int L, RunLists rl) {
     const int64_t LN = (int64_t)L * N;
     for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < LN;
          idx += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = idx % N;
-        if (i + 1 >= N) continue;
-        const uint32_t v = top[idx];
-        if (top[idx + 1] != v || (i > 0 && top[idx - 1] == v)) continue;
-        int64_t j = i + 2;
-        while (j < N && j - i <= kRunMax && top[idx + (j - i)] == v) ++j;
-        const int64_t len = j - i;
-        if (len > kRunMax) {
-            atomicOr(cnt + 2, 1u);
-            continue;
-        }
-        if (len <= 32) {
-            const unsigned int k = atomicAdd(cnt + 0, 1u);
-            if (k < scap) {
-                spos[k] = (unsigned long long)idx;
-                slen[k] = (uint32_t)len;
-            } else {
-                atomicOr(cnt + 2, 2u);
-            }
-        } else {
-            const unsigned int k = atomicAdd(cnt + 1, 1u);
-            if (k < lcap) {
-                lpos[k] = (unsigned long long)idx;
-                llen[k] = (uint32_t)len;
-            } else {
-                atomicOr(cnt + 2, 2u);
+        const int64_t i = idx - (idx / N) * N;
+        int64_t len = 0;
+        if (i + 1 < N) {
+            const uint32_t v = top[idx];
+            if (top[idx + 1] == v && !(i > 0 && top[idx - 1] == v)) {
+                int64_t j = i + 2;
+                while (j < N && j - i <= kRunMax && top[idx + (j - i)] == v) ++j;
+                len = j - i;
             }
         }
+        if (len > kRunMax) atomicOr(rl.cnt + 3, 1u);
+        run_push(len >= 2 && len <= 8, rl.cnt + 0, rl.tpos, rl.tlen, rl.tcap, (unsigned long long)idx, (uint32_t)len,
+                 rl.cnt + 3);
+        run_push(len > 8 && len <= 32, rl.cnt + 1, rl.spos, rl.slen, rl.scap, (unsigned long long)idx, (uint32_t)len,
+                 rl.cnt + 3);
+        run_push(len > 32 && len <= kRunMax, rl.cnt + 2, rl.lpos, rl.llen, rl.lcap, (unsigned long long)idx,
+                 (uint32_t)len, rl.cnt + 3);
     }
 }
 
@@ -335,6 +343,52 @@ __device__ __forceinline__ bool run_less(const uint32_t (&a)[KWL + 1], const uin
     return a[KWL] < b[KWL];
 }
 
+// One thread per run of 2 to 8: an odd-even transposition sort over eight
+// register slots (missing slots hold all-ones, above every element).
+template <int KWL>
+__global__ void k_run_sort_tiny(const unsigned long long* __restrict__ tpos, const uint32_t* __restrict__ tlen,
+                                const unsigned int* __restrict__ cnt, unsigned int tcap, int64_t LN,
+                                uint32_t* __restrict__ skeys, uint32_t* __restrict__ ids) {
+    const unsigned int nrun = min(cnt[0], tcap);
+    for (unsigned int r = blockIdx.x * blockDim.x + threadIdx.x; r < nrun; r += gridDim.x * blockDim.x) {
+        const int64_t pos = (int64_t)tpos[r];
+        const int len = (int)tlen[r];
+        uint32_t e[8][KWL + 1];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+#pragma unroll
+            for (int k = 0; k <= KWL; ++k) e[t][k] = 0xFFFFFFFFu;
+            if (t < len) {
+#pragma unroll
+                for (int k = 0; k < KWL; ++k) e[t][k] = skeys[k * LN + pos + t];
+                e[t][KWL] = ids[pos + t];
+            }
+        }
+#pragma unroll
+        for (int ph = 0; ph < 8; ++ph) {
+#pragma unroll
+            for (int t = ph & 1; t + 1 < 8; t += 2) {
+                if (run_less<KWL>(e[t + 1], e[t])) {
+#pragma unroll
+                    for (int k = 0; k <= KWL; ++k) {
+                        const uint32_t x = e[t][k];
+                        e[t][k] = e[t + 1][k];
+                        e[t + 1][k] = x;
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            if (t < len) {
+#pragma unroll
+                for (int k = 0; k < KWL; ++k) skeys[k * LN + pos + t] = e[t][k];
+                ids[pos + t] = e[t][KWL];
+            }
+        }
+    }
+}
+
 // One warp per run of at most 32: a bitonic sort across the lanes (missing
 // lanes hold all-ones, above every element: ids are below 2^32 - 1).
 template <int KWL>
@@ -342,7 +396,7 @@ __global__ void k_run_sort_small(const unsigned long long* __restrict__ spos, co
                                  const unsigned int* __restrict__ cnt, unsigned int scap, int64_t LN,
                                  uint32_t* __restrict__ skeys, uint32_t* __restrict__ ids) {
     const int lane = threadIdx.x & 31;
-    const unsigned int nrun = min(cnt[0], scap);
+    const unsigned int nrun = min(cnt[1], scap);
     for (unsigned int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < nrun;
          r += (gridDim.x * blockDim.x) >> 5) {
         const int64_t pos = (int64_t)spos[r];
@@ -386,7 +440,7 @@ __global__ void __launch_bounds__(NT) k_run_sort_large(const unsigned long long*
                                                       int64_t LN, uint32_t* __restrict__ skeys,
                                                       uint32_t* __restrict__ ids) {
     __shared__ uint32_t sv[KWL + 1][kRunMax];
-    const unsigned int nrun = min(cnt[1], lcap);
+    const unsigned int nrun = min(cnt[2], lcap);
     for (unsigned int r = blockIdx.x; r < nrun; r += gridDim.x) {
         const int64_t pos = (int64_t)lpos[r];
         const int len = (int)llen[r];
@@ -764,32 +818,31 @@ cudaError_t launch_run_find(const uint32_t* top, int64_t N, int L, const RunList
     cudaError_t e = cudaMemsetAsync(rl.cnt, 0, 4 * sizeof(unsigned int), st);
     if (e != cudaSuccess) return e;
     const int grid = (int)std::min<int64_t>((LN + NT - 1) / NT, 152 * 16);
-    k_run_find<<<grid, NT, 0, st>>>(top, N, L, rl.spos, rl.slen, rl.scap, rl.lpos, rl.llen, rl.lcap, rl.cnt);
+    k_run_find<<<grid, NT, 0, st>>>(top, N, L, rl);
     return cudaGetLastError();
 }
 
 int run_max_len() { return kRunMax; }
 
-cudaError_t launch_run_sorts(const RunLists& rl, unsigned int nsmall, unsigned int nlarge, int64_t N, int L, int KW,
-                             uint32_t* skeys, uint32_t* ids, cudaStream_t st) {
-    const int64_t LN = (int64_t)L * N;
+template <int KWL>
+void launch_run_sorts_w(const RunLists& rl, unsigned int ntiny, unsigned int nsmall, unsigned int nlarge, int64_t LN,
+                        uint32_t* skeys, uint32_t* ids, cudaStream_t st) {
+    const unsigned gt = (unsigned)std::min<unsigned long long>(((unsigned long long)ntiny + NT - 1) / NT, 152 * 16);
     const unsigned gs = (unsigned)std::min<unsigned long long>(((unsigned long long)nsmall * 32 + NT - 1) / NT, 152 * 32);
     const unsigned gl = (unsigned)std::min<unsigned int>(nlarge, 152 * 4);
+    if (gt) k_run_sort_tiny<KWL><<<gt, NT, 0, st>>>(rl.tpos, rl.tlen, rl.cnt, rl.tcap, LN, skeys, ids);
+    if (gs) k_run_sort_small<KWL><<<gs, NT, 0, st>>>(rl.spos, rl.slen, rl.cnt, rl.scap, LN, skeys, ids);
+    if (gl) k_run_sort_large<KWL><<<gl, NT, 0, st>>>(rl.lpos, rl.llen, rl.cnt, rl.lcap, LN, skeys, ids);
+}
+
+cudaError_t launch_run_sorts(const RunLists& rl, const unsigned int* counts, int64_t N, int L, int KW, uint32_t* skeys,
+                             uint32_t* ids, cudaStream_t st) {
+    const int64_t LN = (int64_t)L * N;
     switch (KW - 1) {
-    case 1:
-        if (gs) k_run_sort_small<1><<<gs, NT, 0, st>>>(rl.spos, rl.slen, rl.cnt, rl.scap, LN, skeys, ids);
-        if (gl) k_run_sort_large<1><<<gl, NT, 0, st>>>(rl.lpos, rl.llen, rl.cnt, rl.lcap, LN, skeys, ids);
-        break;
-    case 2:
-        if (gs) k_run_sort_small<2><<<gs, NT, 0, st>>>(rl.spos, rl.slen, rl.cnt, rl.scap, LN, skeys, ids);
-        if (gl) k_run_sort_large<2><<<gl, NT, 0, st>>>(rl.lpos, rl.llen, rl.cnt, rl.lcap, LN, skeys, ids);
-        break;
-    case 3:
-        if (gs) k_run_sort_small<3><<<gs, NT, 0, st>>>(rl.spos, rl.slen, rl.cnt, rl.scap, LN, skeys, ids);
-        if (gl) k_run_sort_large<3><<<gl, NT, 0, st>>>(rl.lpos, rl.llen, rl.cnt, rl.lcap, LN, skeys, ids);
-        break;
-    default:
-        return cudaErrorInvalidValue;
+    case 1: launch_run_sorts_w<1>(rl, counts[0], counts[1], counts[2], LN, skeys, ids, st); break;
+    case 2: launch_run_sorts_w<2>(rl, counts[0], counts[1], counts[2], LN, skeys, ids, st); break;
+    case 3: launch_run_sorts_w<3>(rl, counts[0], counts[1], counts[2], LN, skeys, ids, st); break;
+    default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
 }

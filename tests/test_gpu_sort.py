@@ -4,7 +4,7 @@ then each run of equal top words ordered by its lower words and id (sort form
 (form 2, and forced with CULSH_SORT_ALL_WORDS), against the oracle. The data
 put points in clusters that share the leading columns' codes exactly and
 differ in the trailing columns, with cluster sizes across every run class:
-single points, 2 to 32, 33 to 2,048, and one of 2,049 where asked."""
+single points, 2 to 8, 9 to 32, 33 to 2,048, and one of 2,049 where asked."""
 
 import os
 
@@ -55,7 +55,7 @@ def check(culsh, X, A, b, W):
     return ht.profile()
 
 
-SIZES = [1] * 800 + [2] * 200 + [3] * 60 + [7] * 40 + [32] * 12 + [33] * 6 + [100] * 6 + [700] * 2 + [2048]
+SIZES = [1] * 800 + [2] * 200 + [3] * 60 + [7] * 40 + [8] * 10 + [9] * 10 + [20] * 6 + [32] * 12 + [33] * 6 + [100] * 6 + [700] * 2 + [2048]
 
 
 def test_top_word_then_runs(culsh):
