@@ -404,6 +404,79 @@ def timed_searches(st, torch, stream, sp, qt, Q, ids, dists, flush, steps):
     return statistics.median(e0.elapsed_time(e1) for e0, e1 in ev)
 
 
+def precision_d960(culsh, torch, dev, n=100_000, nq=400):
+    """The high-dimensional precision workload's shapes (unit vectors,
+    D = 960, L = 32, M = 16, W = 0.25, T = 64, K = 10) at a bounded 100,000
+    points: the index built on the tensor cores (forced; with the default
+    gate it takes the FP32 SIMT projection, the bound leaving about 14 % of
+    the codes open) and on the SIMT kernel, every point's code in every table
+    compared between them (mismatches must be 0), and the search's returned
+    distances against FP64 for 200 held-out queries and 200 queries a small
+    step from indexed points."""
+    from culsh_gb300 import synth
+    X, Qm, A, b, cfg = synth.dataset(3, n=n, q=nq // 2)
+    N, D, L, M, W, T, K = X.shape[0], cfg.D, cfg.L, cfg.M, cfg.W, cfg.T, cfg.K
+    rng = np.random.default_rng(5)
+    near = X[rng.integers(0, N, nq // 2)] + rng.normal(0, 0.001, (nq // 2, D)).astype(np.float32)
+    near /= np.linalg.norm(near, axis=1, keepdims=True)
+    queries = np.ascontiguousarray(np.concatenate([Qm, near]).astype(np.float32))
+    Xt = torch.from_numpy(X).to(dev)
+    stream = torch.cuda.Stream(dev)
+    sp = stream.cuda_stream
+    out, idx = {}, {}
+    for form, env in (("tensor_cores", "CULSH_PROJECT_TC"), ("fp32_simt", "CULSH_PROJECT_SIMT")):
+        os.environ[env] = "1"
+        try:
+            ht = culsh.HashTables()
+            ht.reset(N, D, L, M, W, A=A, b=b)
+            ht.index_device(Xt.data_ptr(), sp)
+            ms = []
+            for _ in range(3):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                torch.cuda.synchronize()
+                e0.record(stream)
+                ht.index_device(Xt.data_ptr(), sp)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms.append(e0.elapsed_time(e1))
+        finally:
+            del os.environ[env]
+        p = ht.profile()
+        out[form] = {"index_build_ms": round(statistics.median(ms), 3), "project_ms": round(p["project_ms"], 3),
+                     "recomputed_codes": p["recomputed"]}
+        idx[form] = ht
+    # every point's code row in every table, from the bucket arrays
+    mism = 0
+    for l in range(L):
+        rows = []
+        for form in ("tensor_cores", "fp32_simt"):
+            ht = idx[form]
+            ids, starts, codes = ht.getBuckets_totalIndices(l), ht.getBuckets_startingIndices(l), ht.getBuckets_codes(l)
+            pos = np.empty(N, np.int64)
+            pos[ids] = np.arange(N)
+            rows.append(codes[:, np.searchsorted(starts, pos, side="right") - 1])
+        mism += int(np.count_nonzero(rows[0] != rows[1]))
+    total = L * M * N
+    st = culsh.SearchTables()
+    st.reset(idx["tensor_cores"], K, T)
+    st.search(queries, dataset=X)
+    kid, kd = st.getKnnIds(), st.getKnnDistances()
+    ok = kid >= 0
+    qi = np.nonzero(ok)[0]
+    d64 = ((queries[qi].astype(np.float64) - X[kid[ok]].astype(np.float64)) ** 2).sum(axis=1)
+    err = np.abs(kd[ok].astype(np.float64) - d64)
+    rel = err / np.maximum(d64, np.finfo(np.float64).tiny)
+    return {"workload": f"unit-sphere-d960 N={N} L={L} M={M} W={W:g} T={T} K={K} Q={queries.shape[0]} "
+                        "(200 held-out + 200 near indexed points)",
+            "code_mismatches": mism, "codes_compared": total,
+            "forms": out,
+            "distance_error_vs_fp64": {"pairs": int(ok.sum()), "max_abs": float(err.max()) if err.size else 0.0,
+                                       "mean_abs": float(err.mean()) if err.size else 0.0,
+                                       "max_rel": float(rel.max()) if rel.size else 0.0,
+                                       "mean_rel": float(rel.mean()) if rel.size else 0.0},
+            "candidates_unique_per_query": st.getTotalCandidates_unique() / queries.shape[0]}
+
+
 def recall_point(culsh, torch, dev, steps, warmup, autotune=True, fixed=None):
     """The Gaussian-mixture generator (100 centres ~N(0,10^2), unit noise) at
     1M x 128, L=8, M=8, T=16, K=10, W=32, where LSH reaches recall@10 >= 0.90
@@ -736,7 +809,7 @@ def run_culsh(args):
     ns = min(args.recall_sample, Q)
     rec = recall_at_k(found[:ns], X, Qm[:ns], K) if ns > 0 else None
 
-    named = rpoint = serving = None
+    named = rpoint = serving = precision = None
     if not args.no_side and rank == 0:
         from culsh_gb300 import synth
         cfg = synth.CONFIGS[args.config]
@@ -746,15 +819,32 @@ def run_culsh(args):
             ht_named, named = named_point(culsh, torch, dev, Xt, dict(d, W=cfg.W), An, bn, Qm,
                                           max(3, min(args.steps, 10)), max(args.warmup, 3))
         rpoint = recall_point(culsh, torch, dev, max(3, min(args.steps, 10)), max(args.warmup, 3))
+        precision = precision_d960(culsh, torch, dev)
         rates = [float(r) for r in args.serve_rates.split(",") if r.strip()]
         if rates:
-            pool = synth.dataset(args.config, n=16, q=max(65536, Q))[1]
-            Ks = sorted({K, 10, 100})
-            Ts = [1, 8, 32] if args.config == 5 else sorted({1, T})   # the serving workload's T mix
+            # the serving workload itself: a resident 10M x 96 Gaussian-mixture
+            # index (L=20, M=14, W=5), requests of 1..4,096 queries from the
+            # same mixture with K in {10, 100} and T in {1, 8, 32}
+            del ht_named
+            scfg = synth.CONFIGS[5]
+            Xs, pool, As, bs, _ = synth.dataset(5, q=65536)
+            Xst = torch.from_numpy(Xs).to(dev)
+            torch.cuda.synchronize()
+            ht_s = culsh.HashTables()
+            ht_s.reset(Xs.shape[0], scfg.D, scfg.L, scfg.M, scfg.W, A=As, b=bs)
+            sst = torch.cuda.Stream(dev)
+            t_b = time.perf_counter()
+            ht_s.index_device(Xst.data_ptr(), sst.cuda_stream)
+            torch.cuda.synchronize()
+            t_b = time.perf_counter() - t_b
+            Ks, Ts = [10, 100], [1, 8, 32]
             serving = {"arrivals": "Poisson", "request_queries": "log-uniform 1..4096", "K": Ks, "T": Ts,
-                       "slots": 4, "index": f"{cfg.name} at W={cfg.W:g} (the named configuration)",
-                       "runs": [serve_run(culsh, ht_named, pool, r, args.serve_seconds, Ks, Ts, seed=17 + i)
+                       "slots": 4,
+                       "index": f"{scfg.name} N={Xs.shape[0]} L={scfg.L} M={scfg.M} W={scfg.W:g} (resident; "
+                                f"built in {t_b * 1e3:.1f} ms)",
+                       "runs": [serve_run(culsh, ht_s, pool, r, args.serve_seconds, Ks, Ts, seed=17 + i)
                                 for i, r in enumerate(rates)]}
+            del ht_s, Xst
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -787,7 +877,7 @@ def run_culsh(args):
                 "fp32_form": fp32, "index_build_ms": round(statistics.median(build_ms), 3),
                 "index_build_stages_ms": {k: (round(v, 4) if isinstance(v, float) else v)
                                           for k, v in build_profile.items()},
-                "named_w": named, "recall_point_gauss": rpoint, "serving": serving,
+                "named_w": named, "recall_point_gauss": rpoint, "precision_d960": precision, "serving": serving,
                 "reference_build": REFERENCE_BUILD_NOTE}
         print(json.dumps(line), flush=True)
     if dist is not None:

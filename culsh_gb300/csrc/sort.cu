@@ -274,11 +274,10 @@ __global__ void __launch_bounds__(NT, 3) k_sort_pass(const uint32_t* __restrict_
 // sorted top words are copied into skeys' top slot unless they are there.
 __global__ void k_gather_lower(const uint32_t* __restrict__ keys0, const uint32_t* __restrict__ ids,
                                const uint32_t* top, int64_t N, int L, int KW, uint32_t* skeys) {
-    const int64_t LN = (int64_t)L * N;
+    const int64_t LN = (int64_t)L * N, seg = (int64_t)blockIdx.y * N;
     uint32_t* stop = skeys + (int64_t)(KW - 1) * LN;
-    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < LN;
-         idx += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t seg = (idx / N) * N;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t idx = seg + i;
         const uint32_t id = ids[idx];
         for (int w = 0; w < KW - 1; ++w) skeys[w * LN + idx] = __ldg(keys0 + w * LN + seg + id);
         if (top != stop) stop[idx] = top[idx];
@@ -310,27 +309,28 @@ __device__ __forceinline__ void run_push(bool mine, unsigned int* cnt, unsigned 
     }
 }
 
-__global__ void k_run_find(const uint32_t* __restrict__ top, int64_t N, int L, RunLists rl) {
-    const int64_t LN = (int64_t)L * N;
-    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < LN;
-         idx += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = idx - (idx / N) * N;
+// Block (x, table y); each thread examines RUN_ITEMS consecutive positions.
+constexpr int RUN_ITEMS = 8;
+__global__ void k_run_find(const uint32_t* __restrict__ top, int64_t N, RunLists rl) {
+    const uint32_t* t = top + (int64_t)blockIdx.y * N;
+    const int64_t i0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * RUN_ITEMS;
+#pragma unroll
+    for (int k = 0; k < RUN_ITEMS; ++k) {
+        const int64_t i = i0 + k;
         int64_t len = 0;
         if (i + 1 < N) {
-            const uint32_t v = top[idx];
-            if (top[idx + 1] == v && !(i > 0 && top[idx - 1] == v)) {
+            const uint32_t v = t[i];
+            if (t[i + 1] == v && !(i > 0 && t[i - 1] == v)) {
                 int64_t j = i + 2;
-                while (j < N && j - i <= kRunMax && top[idx + (j - i)] == v) ++j;
+                while (j < N && j - i <= kRunMax && t[j] == v) ++j;
                 len = j - i;
             }
         }
+        const unsigned long long p = (unsigned long long)((int64_t)blockIdx.y * N + i);
         if (len > kRunMax) atomicOr(rl.cnt + 3, 1u);
-        run_push(len >= 2 && len <= 8, rl.cnt + 0, rl.tpos, rl.tlen, rl.tcap, (unsigned long long)idx, (uint32_t)len,
-                 rl.cnt + 3);
-        run_push(len > 8 && len <= 32, rl.cnt + 1, rl.spos, rl.slen, rl.scap, (unsigned long long)idx, (uint32_t)len,
-                 rl.cnt + 3);
-        run_push(len > 32 && len <= kRunMax, rl.cnt + 2, rl.lpos, rl.llen, rl.lcap, (unsigned long long)idx,
-                 (uint32_t)len, rl.cnt + 3);
+        run_push(len >= 2 && len <= 8, rl.cnt + 0, rl.tpos, rl.tlen, rl.tcap, p, (uint32_t)len, rl.cnt + 3);
+        run_push(len > 8 && len <= 32, rl.cnt + 1, rl.spos, rl.slen, rl.scap, p, (uint32_t)len, rl.cnt + 3);
+        run_push(len > 32 && len <= kRunMax, rl.cnt + 2, rl.lpos, rl.llen, rl.lcap, p, (uint32_t)len, rl.cnt + 3);
     }
 }
 
@@ -807,8 +807,7 @@ cudaError_t run_segmented_sort(SortBuffers& sb, int64_t N, int L, int KW, int pa
 
 cudaError_t launch_gather_lower(const uint32_t* keys0, const uint32_t* ids, const uint32_t* top, int64_t N, int L,
                                 int KW, uint32_t* skeys, cudaStream_t st) {
-    const int64_t LN = (int64_t)L * N;
-    const int grid = (int)std::min<int64_t>((LN + NT - 1) / NT, 152 * 16);
+    const dim3 grid((unsigned)std::min<int64_t>((N + NT - 1) / NT, 152 * 4), (unsigned)L);
     k_gather_lower<<<grid, NT, 0, st>>>(keys0, ids, top, N, L, KW, skeys);
     return cudaGetLastError();
 }
@@ -817,8 +816,9 @@ cudaError_t launch_run_find(const uint32_t* top, int64_t N, int L, const RunList
     const int64_t LN = (int64_t)L * N;
     cudaError_t e = cudaMemsetAsync(rl.cnt, 0, 4 * sizeof(unsigned int), st);
     if (e != cudaSuccess) return e;
-    const int grid = (int)std::min<int64_t>((LN + NT - 1) / NT, 152 * 16);
-    k_run_find<<<grid, NT, 0, st>>>(top, N, L, rl);
+    (void)LN;
+    const dim3 grid((unsigned)((N + (int64_t)NT * RUN_ITEMS - 1) / ((int64_t)NT * RUN_ITEMS)), (unsigned)L);
+    k_run_find<<<grid, NT, 0, st>>>(top, N, rl);
     return cudaGetLastError();
 }
 

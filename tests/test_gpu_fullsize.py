@@ -2,7 +2,10 @@
 1M x 128 integer-feature workload, index and search compared bit for bit
 against the CPU oracle, plus size-independent properties of the index; the
 4M x 128 Zipf-cluster and 10M x 96 serving workloads through whole-table,
-sampled-point and search comparisons."""
+sampled-point and search comparisons; the D = 960 unit-sphere workload's
+shapes at 100,000 points on both projection kernels."""
+
+import functools
 
 import numpy as np
 import pytest
@@ -149,3 +152,51 @@ def test_full_size_large_configs(culsh, config):
         assert st.getTotalCandidates_unique() == int(want["unique"].sum())
         assert st.getTotalCandidates_nonUnique() == int(want["nonunique"].sum())
         assert st.getTotalCandidates_unique() > 0
+
+
+@functools.lru_cache(maxsize=1)
+def sphere_case():
+    """100,000 unit vectors of the D = 960 workload, its 200 held-out queries
+    plus 200 queries a small step from indexed points, and the oracle's index
+    and search (built once for both parametrisations)."""
+    X, Qm, A, b, cfg = synth.dataset(3, n=100_000, q=200)
+    rng = np.random.default_rng(5)
+    near = X[rng.integers(0, X.shape[0], 200)] + rng.normal(0, 0.001, (200, cfg.D)).astype(np.float32)
+    near /= np.linalg.norm(near, axis=1, keepdims=True)
+    queries = np.ascontiguousarray(np.concatenate([Qm, near]).astype(np.float32))
+    ref = oracle.build_index(X, A, b, cfg.W)
+    want = oracle.search(ref, X, queries, cfg.K, cfg.T)
+    return X, A, b, cfg, queries, ref, want
+
+
+@pytest.mark.parametrize("force_tc", [False, True])
+def test_unit_sphere_d960_shapes(culsh, force_tc, monkeypatch):
+    """The high-dimensional precision workload's shapes at 100,000 points:
+    unit vectors, D = 960, L = 32, M = 16, W = 0.25, T = 64, K = 10. By
+    default the index takes the FP32 SIMT projection (the tensor-core bound
+    would leave about 14 % of the codes open here); forced onto the tensor
+    cores (CULSH_PROJECT_TC) it must produce the same codes, recomputing the
+    open ones in the canonical order. Index and search against the oracle."""
+    if force_tc:
+        monkeypatch.setenv("CULSH_PROJECT_TC", "1")
+    X, A, b, cfg, queries, ref, want = sphere_case()
+    N, D, L, M, W = X.shape[0], cfg.D, cfg.L, cfg.M, cfg.W
+    ht = culsh.HashTables()
+    ht.reset(N, D, L, M, W, A=A, b=b)
+    ht.index(X)
+    p = ht.profile()
+    assert p["tensor_cores"] == (1 if force_tc else 0)
+    if force_tc:
+        assert p["recomputed"] > 0
+    np.testing.assert_array_equal(ht.getBuckets(), ref.buckets)
+    for l in range(L):
+        np.testing.assert_array_equal(ht.getBuckets_totalIndices(l), ref.ids(l), err_msg=f"table {l}")
+        np.testing.assert_array_equal(ht.getBuckets_startingIndices(l), ref.starts(l), err_msg=f"table {l}")
+        np.testing.assert_array_equal(ht.getBuckets_codes(l), ref.codes(l), err_msg=f"table {l}")
+    st = culsh.SearchTables()
+    st.reset(ht, cfg.K, cfg.T)
+    st.search(queries, dataset=X)
+    np.testing.assert_array_equal(st.getKnnIds(), want["knn_ids"])
+    np.testing.assert_array_equal(st.getKnnDistances(), want["knn_dists"])
+    assert st.getTotalCandidates_unique() == int(want["unique"].sum())
+    assert st.getTotalCandidates_unique() > 0
