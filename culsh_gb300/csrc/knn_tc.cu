@@ -153,19 +153,6 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr)
-        : "memory");
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
-
 // The 64 accumulator columns [taddr, taddr + 64) of this thread's TMEM lane,
 // loaded and waited for in one statement, so that no use of r can be
 // scheduled before the wait.
@@ -349,8 +336,13 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
         long long cur_qt = -1;
         int j = -1;
         long long i = 0;
+        // (query tile, point tile) of pair p and both rings' stage and round
+        // parity, advanced incrementally (no 64-bit division per tile)
+        long long qt = p0 / ntp, pt = p0 - qt * ntp;
+        int s = 0, e = 0;
+        uint32_t spar = 0, epar = 0;
+        long long issued_op = 0, issued_ep = 0;   // copies issued into each ring
         for (long long p = p0; p < p1 && !*abort_flag; ++p, ++i) {
-            const long long qt = p / ntp, pt = p - qt * ntp;
             if (qt != cur_qt) {
                 ++j;
                 cur_qt = qt;
@@ -361,30 +353,32 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
                     if (need_ql) tma_2d(sQl + (size_t)k * MQ * 128, &tm_ql, a_full, k * 64, (int)(qt * MQ));
                 }
             }
-            const int s = (int)(i % ops);
-            if (i >= ops && !bar_wait(empty_op + s, (uint32_t)((i / ops - 1) & 1), abort_flag, a.err)) break;
+            if (i >= ops && !bar_wait(empty_op + s, spar ^ 1u, abort_flag, a.err)) break;
             unsigned char* xs = sX + (size_t)s * op_stride;
             bar_expect_tx(full_op + s, xbytes * (need_xl ? 2u : 1u));
             for (int k = 0; k < atoms; ++k) {
                 tma_2d(xs + (size_t)k * BN * 128, &tm_xh, full_op + s, k * 64, (int)(pt * BN));
                 if (need_xl) tma_2d(xs + xbytes + (size_t)k * BN * 128, &tm_xl, full_op + s, k * 64, (int)(pt * BN));
             }
-            const int e = (int)(i % eps);
-            if (i >= eps && !bar_wait(empty_ep + e, (uint32_t)((i / eps - 1) & 1), abort_flag, a.err)) break;
+            ++issued_op;
+            if (i >= eps && !bar_wait(empty_ep + e, epar ^ 1u, abort_flag, a.err)) break;
             unsigned char* es = sE + (size_t)e * ep_stride;
             bar_expect_tx(full_ep + e, ep_stride);
             tma_2d(es, &tm_bm, full_ep + e, (int)(pt * BW), (int)(qt * MQ));
             bulk_copy(es + bm_bytes, (kExact ? a.w_exact : a.w_bound) + pt * BN, w_bytes, full_ep + e);
+            ++issued_ep;
+            if (++s == ops) { s = 0; spar ^= 1u; }
+            if (++e == eps) { e = 0; epar ^= 1u; }
+            if (++pt == ntp) { pt = 0; ++qt; }
         }
         // Drain: every copy issued into a ring stage completes before exit.
-        const long long issued = i;
-        for (int s = 0; s < ops && s < issued; ++s) {
-            const long long last = s + ((issued - 1 - s) / ops) * ops;
-            bar_drain(full_op + s, (uint32_t)((last / ops) & 1), a.err);
+        for (int st = 0; st < ops && st < issued_op; ++st) {
+            const long long last = st + ((issued_op - 1 - st) / ops) * ops;
+            bar_drain(full_op + st, (uint32_t)((last / ops) & 1), a.err);
         }
-        for (int e = 0; e < eps && e < issued; ++e) {
-            const long long last = e + ((issued - 1 - e) / eps) * eps;
-            bar_drain(full_ep + e, (uint32_t)((last / eps) & 1), a.err);
+        for (int et = 0; et < eps && et < issued_ep; ++et) {
+            const long long last = et + ((issued_ep - 1 - et) / eps) * eps;
+            bar_drain(full_ep + et, (uint32_t)((last / eps) & 1), a.err);
         }
         if (j >= 0) bar_drain(a_full, (uint32_t)(j & 1), a.err);
     } else if (warp == 1 && lane == 0) {
@@ -397,18 +391,20 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
         long long cur_qt = -1;
         int j = -1;
         long long i = 0;
+        long long qt = p0 / ntp, pt = p0 - qt * ntp;
+        int s = 0;
+        uint32_t spar = 0;
         for (long long p = p0; p < p1; ++p, ++i) {
-            const long long qt = p / ntp;
             if (qt != cur_qt) {
                 if (j >= 0) mma_commit(a_empty);
                 ++j;
                 cur_qt = qt;
                 if (!bar_wait(a_full, (uint32_t)(j & 1), abort_flag, a.err)) break;
             }
+            if (++pt == ntp) { pt = 0; ++qt; }
             const int acc = (int)(i & 1);
             if (i >= 2 && !bar_wait(tempty + acc, (uint32_t)(((i >> 1) - 1) & 1), abort_flag, a.err)) break;
-            const int s = (int)(i % ops);
-            if (!bar_wait(full_op + s, (uint32_t)((i / ops) & 1), abort_flag, a.err)) break;
+            if (!bar_wait(full_op + s, spar, abort_flag, a.err)) break;
             fence_after();
             // descriptors advance by adding the byte offset / 16 to their
             // start-address field (shared addresses stay below 2^18: no carry)
@@ -428,6 +424,7 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
             }
             mma_commit(empty_op + s);
             mma_commit(tfull + acc);
+            if (++s == ops) { s = 0; spar ^= 1u; }
         }
         // every product has landed before TMEM is released
         mma_commit(done_bar);
@@ -460,8 +457,10 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
             }
             a.part_n[lst * MQ + row] = n;
         };
+        long long qt = p0 / ntp, pt = p0 - qt * ntp;
+        int e = 0;
+        uint32_t epar = 0;
         for (long long p = p0; p < p1; ++p, ++i) {
-            const long long qt = p / ntp, pt = p - qt * ntp;
             if (qt != cur_qt) {
                 if (cur_qt >= 0) flush(cur_qt);
                 cur_qt = qt;
@@ -469,11 +468,10 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
                 thr = INFINITY;
             }
             const int acc = (int)(i & 1);
-            const int e = (int)(i % eps);
             // every lane waits (and so sees the copied data); the warp leaves
             // together if any lane gave up, since tcgen05.ld is warp-wide
             const bool ok = bar_wait(tfull + acc, (uint32_t)((i >> 1) & 1), abort_flag, a.err) &&
-                            bar_wait(full_ep + e, (uint32_t)((i / eps) & 1), abort_flag, a.err);
+                            bar_wait(full_ep + e, epar, abort_flag, a.err);
             if (!__all_sync(0xffffffffu, ok)) break;
             fence_after();
             const unsigned char* es = sE + (size_t)e * ep_stride;
@@ -550,6 +548,8 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
             if (kExact && n == Kl && thr < ext) atomicMin(a.qbound + gq, key_enc(thr));
             __syncwarp();
             if (lane == 0) bar_arrive(empty_ep + e);
+            if (++e == eps) { e = 0; epar ^= 1u; }
+            if (++pt == ntp) { pt = 0; ++qt; }
         }
         if (cur_qt >= 0 && !*abort_flag) flush(cur_qt);
     }
