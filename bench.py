@@ -192,6 +192,18 @@ def tensor_peak():
         return 1900.0, "fallback"
 
 
+# How to read a stage's roofline where the algorithmic figure is not the
+# traffic that bounds it.
+STAGE_NOTES = {
+    "membership": "algorithmic bytes are the 4 * C_nu bucket-id reads (each query reads its candidates' ids) "
+                  "plus the N/8-byte membership row written per query; about 90 % of the id reads hit L2 "
+                  "(the 64 MB of id arrays stay resident), so this is the rate seen at L2, not DRAM (measured "
+                  "DRAM traffic in `traffic`); the stage is bound by the shared-memory atomicOr of each id",
+    "knn": "flops of the dense GEMM the kernel runs (2 * D * N per dense query); the candidates' own distance "
+           "work is the unique-candidate share of it",
+}
+
+
 def ncu_traffic(kernel: str, workload: str):
     """DRAM bytes per launch of `kernel` on `workload` from the committed ncu
     summary (profiles/ncu_traffic.json): not measured in this run; the entry
@@ -732,6 +744,7 @@ def run_culsh(args):
                                 "probe_bytes": sb["probe"], "project_bytes": sb["project"],
                                 "candidates_bytes": sb["candidates"]},
                 "peak_source": f"{peak_kind} hbm_gbs" if rf["bound"] == "hbm" else f"{tpeak_kind} bf16_tflops (burst)",
+                "note": STAGE_NOTES.get(dom),
                 "stage_ms_median": {k: round(v, 4) for k, v in med.items()},
                 "all_stages": {k: {"achieved": round(v["achieved"], 2), "unit": v["unit"],
                                    "frac": round(v["achieved"] / v["peak"], 5)} for k, v in rooflines.items()}}
