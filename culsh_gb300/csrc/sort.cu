@@ -287,50 +287,58 @@ __global__ void k_gather_lower(const uint32_t* __restrict__ keys0, const uint32_
 // Runs of two or more equal top words, found from their first element, go to
 // three lists by length: 2..8 (tiny), 9..32 (small), 33..kRunMax (large); a
 // longer run or a full list sets cnt[3] (the caller then sorts all words
-// instead). List slots are claimed with one atomic per warp and class.
-__device__ __forceinline__ void run_push(bool mine, unsigned int* cnt, unsigned long long* pos, uint32_t* len,
-                                         unsigned int cap, unsigned long long p, uint32_t n, unsigned int* over) {
-    const unsigned int act = __activemask();
-    const unsigned int m = __ballot_sync(act, mine);
-    if (!m) return;
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs((int)m) - 1;
-    unsigned int base = 0;
-    if (lane == leader) base = atomicAdd(cnt, (unsigned int)__popc(m));
-    base = __shfl_sync(act, base, leader);
-    if (mine) {
-        const unsigned int k = base + __popc(m & ((1u << lane) - 1u));
-        if (k < cap) {
-            pos[k] = p;
-            len[k] = n;
-        } else {
-            atomicOr(over, 2u);
-        }
-    }
-}
-
-// Block (x, table y); each thread examines RUN_ITEMS consecutive positions.
+// instead). Block (x, table y); each thread examines RUN_ITEMS consecutive
+// positions. List slots are claimed per block (shared counters, then one
+// global atomic per block and class): with tens of thousands of runs per
+// table, one global atomic per run or per warp serialises on the counters.
 constexpr int RUN_ITEMS = 8;
-__global__ void k_run_find(const uint32_t* __restrict__ top, int64_t N, RunLists rl) {
+__global__ void __launch_bounds__(NT) k_run_find(const uint32_t* __restrict__ top, int64_t N, RunLists rl) {
+    __shared__ unsigned int sc[3], sbase[3];
+    if (threadIdx.x < 3) sc[threadIdx.x] = 0;
+    __syncthreads();
     const uint32_t* t = top + (int64_t)blockIdx.y * N;
     const int64_t i0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * RUN_ITEMS;
+    uint32_t len[RUN_ITEMS];
+    unsigned int mine[3] = {0u, 0u, 0u};
 #pragma unroll
     for (int k = 0; k < RUN_ITEMS; ++k) {
         const int64_t i = i0 + k;
-        int64_t len = 0;
+        len[k] = 0;
         if (i + 1 < N) {
             const uint32_t v = t[i];
             if (t[i + 1] == v && !(i > 0 && t[i - 1] == v)) {
                 int64_t j = i + 2;
                 while (j < N && j - i <= kRunMax && t[j] == v) ++j;
-                len = j - i;
+                if (j - i > kRunMax) atomicOr(rl.cnt + 3, 1u);
+                else len[k] = (uint32_t)(j - i);
             }
         }
-        const unsigned long long p = (unsigned long long)((int64_t)blockIdx.y * N + i);
-        if (len > kRunMax) atomicOr(rl.cnt + 3, 1u);
-        run_push(len >= 2 && len <= 8, rl.cnt + 0, rl.tpos, rl.tlen, rl.tcap, p, (uint32_t)len, rl.cnt + 3);
-        run_push(len > 8 && len <= 32, rl.cnt + 1, rl.spos, rl.slen, rl.scap, p, (uint32_t)len, rl.cnt + 3);
-        run_push(len > 32 && len <= kRunMax, rl.cnt + 2, rl.lpos, rl.llen, rl.lcap, p, (uint32_t)len, rl.cnt + 3);
+        const uint32_t n = len[k];
+        mine[0] += (n >= 2 && n <= 8) ? 1u : 0u;
+        mine[1] += (n > 8 && n <= 32) ? 1u : 0u;
+        mine[2] += n > 32 ? 1u : 0u;
+    }
+    unsigned int off[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) off[c] = mine[c] ? atomicAdd(&sc[c], mine[c]) : 0u;
+    __syncthreads();
+    if (threadIdx.x < 3) sbase[threadIdx.x] = sc[threadIdx.x] ? atomicAdd(rl.cnt + threadIdx.x, sc[threadIdx.x]) : 0u;
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < RUN_ITEMS; ++k) {
+        const uint32_t n = len[k];
+        if (n < 2) continue;
+        const int c = n <= 8 ? 0 : (n <= 32 ? 1 : 2);
+        const unsigned int slot = sbase[c] + off[c]++;
+        const unsigned int cap = c == 0 ? rl.tcap : (c == 1 ? rl.scap : rl.lcap);
+        unsigned long long* pos = c == 0 ? rl.tpos : (c == 1 ? rl.spos : rl.lpos);
+        uint32_t* lens = c == 0 ? rl.tlen : (c == 1 ? rl.slen : rl.llen);
+        if (slot < cap) {
+            pos[slot] = (unsigned long long)((int64_t)blockIdx.y * N + i0 + k);
+            lens[slot] = n;
+        } else {
+            atomicOr(rl.cnt + 3, 2u);
+        }
     }
 }
 
