@@ -81,17 +81,18 @@ __global__ void k_pack_keys(const int32_t* __restrict__ codes, int64_t N, int L,
          idx += (int64_t)gridDim.x * blockDim.x) {
         const int l = (int)(idx / N);
         const int64_t n = idx - (int64_t)l * N;
-        uint32_t key[kMaxKW];
-#pragma unroll
-        for (int w = 0; w < kMaxKW; ++w) key[w] = 0;
+        // fields are contiguous, column M - 1 at bit 0 and column 0 on top:
+        // shift each column in after the previous one (registers only)
+        unsigned __int128 kk = 0;
         for (int m = 0; m < M; ++m) {
             const int c = l * M + m;
-            const int bits = fbits[c];
-            if (bits) key_put(key, foff[c], bits, (uint32_t)(codes[(int64_t)c * N + n] - cmin[c]));
+            const int bits = __ldg(fbits + c);
+            if (!bits) continue;
+            kk = (kk << bits) | (uint32_t)(codes[(int64_t)c * N + n] - __ldg(cmin + c));
         }
 #pragma unroll
         for (int w = 0; w < kMaxKW; ++w)
-            if (w < KW) keys[w * LN + idx] = key[w];
+            if (w < KW) keys[w * LN + idx] = (uint32_t)(kk >> (32 * w));
         vals[idx] = (uint32_t)n;
     }
 }
@@ -604,13 +605,17 @@ __global__ void k_hash_build(const uint64_t* __restrict__ boff, const uint32_t* 
     const int64_t B = (int64_t)(boff[l + 1] - boff[l]);
     if (j >= B) return;
     const uint32_t* key = ukeys + (boff[l] + j) * KW;
-    uint32_t k[kMaxKW];
-    for (int w = 0; w < KW; ++w) k[w] = key[w];
+    unsigned __int128 kk = 0;
+    for (int w = KW - 1; w >= 0; --w) kk = (kk << 32) | key[w];
     const uint32_t gmask = hmask[l];
     uint64_t hs = 0;   // additive lookup hash over the key's fields
-    for (int m = 0; m < M; ++m) {
+    // fields are contiguous from bit 0 (column M - 1) upwards
+    for (int m = M - 1; m >= 0; --m) {
         const int c = l * M + m;
-        hs += (uint64_t)key_get(k, __ldg(foff + c), __ldg(fbits + c)) * __ldg(rmul + c);
+        const int bits = __ldg(fbits + c);
+        const uint32_t f = bits ? (uint32_t)kk & (bits == 32 ? 0xFFFFFFFFu : ((1u << bits) - 1u)) : 0u;
+        kk >>= bits;
+        hs += (uint64_t)f * __ldg(rmul + c);
     }
     const uint64_t hh = hash_finish(hs);
     const uint32_t h = (uint32_t)hh;
