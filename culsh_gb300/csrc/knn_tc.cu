@@ -477,6 +477,9 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
             const unsigned char* es = sE + (size_t)e * ep_stride;
             const int gq = (int)qt * MQ + row;   // dense position of this lane's query
             const float ext = kExact ? key_dec(__ldcg(a.qbound + gq)) : INFINITY;
+            // a key enters iff key < thr and key <= ext, i.e. key < lim
+            const float ext_up = nextafterf(ext, INFINITY);
+            float lim = fminf(thr, ext_up);
             const uint2 mw = *reinterpret_cast<const uint2*>(es + (size_t)row * BW * 4 + ch * 8);   // 2 words: 64 columns
             const float* wv = reinterpret_cast<const float*>(es + bm_bytes) + ch * CW;
             const uint32_t id0 = (uint32_t)(pt * BN + ch * CW);
@@ -516,20 +519,17 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
                 mm[10] = fminf(__uint_as_float(rc[30]), __uint_as_float(rc[31]));
                 const float m = fmin3(fmin3(mm[0], mm[1], mm[2]), fmin3(mm[3], mm[4], mm[5]),
                                       fmin3(fmin3(mm[6], mm[7], mm[8]), mm[9], mm[10]));
-                if (m < thr && !(m > ext) && mbits) {
+                if (m < lim && mbits) {
                     // this lane's candidate columns whose key beats its list;
                     // lanes insert in parallel, each into its own sorted list
                     uint32_t pm = 0;
 #pragma unroll
-                    for (int k = 0; k < 32; ++k) {
-                        const float v = __uint_as_float(rc[k]);
-                        pm |= (v < thr && !(v > ext) ? 1u : 0u) << k;
-                    }
+                    for (int k = 0; k < 32; ++k) pm |= (__uint_as_float(rc[k]) < lim ? 1u : 0u) << k;
                     pm &= mbits;
                     for (; pm; pm &= pm - 1) {
                         const int k = __ffs((int)pm) - 1;
                         const float key = select32(rc, k);
-                        if (!(key < thr) || key > ext) continue;
+                        if (!(key < lim)) continue;
                         // ids arrive in ascending order, so a key equal to a
                         // listed one goes after it
                         int pos = n < Kl ? n : Kl - 1;
@@ -541,7 +541,10 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
                         mk[pos * NT] = key;
                         mi[pos * NT] = id0 + (uint32_t)(c * 32 + k);
                         if (n < Kl) ++n;
-                        if (n == Kl) thr = mk[(Kl - 1) * NT];
+                        if (n == Kl) {
+                            thr = mk[(Kl - 1) * NT];
+                            lim = fminf(thr, ext_up);
+                        }
                     }
                 }
             }
