@@ -164,3 +164,44 @@ def test_graph_replay_and_autotune_keep_results(culsh, all_dense):
     tuned = st.autotune(q.data_ptr(), q.shape[0], ids.data_ptr(), d.data_ptr(), sp)
     assert tuned["dense_tc"] in (0, 1)
     np.testing.assert_array_equal(ids.cpu().numpy(), c["knn_ids"])
+
+
+@pytest.mark.parametrize("K,T,Q", [(1, 1, 1), (20, 16, 257), (10, 8, 513), (64, 4, 96)])
+def test_edge_shapes_exact_form(culsh, all_dense, K, T, Q):
+    """Edge shapes of the exact form: N not a multiple of the 128-point tile
+    (ragged last tile), Q crossing the 256-query tile (one query alone in its
+    tile, or a tile of one), K = 1, T = 1. At K = 64 the per-query lists no
+    longer fit shared memory beside the operand rings at D = 128, so the
+    dense queries take the SIMT bitmap kernel instead; results are the same."""
+    from culsh_gb300 import synth
+    X, Qm, _, _, _ = synth.dataset(2, n=5_003, q=Q)
+    L, M, W = 6, 8, 600.0
+    A, b = synth.projection(L, M, X.shape[1], W, 3002)
+    want = _oracle_case(X, Qm, A, b, W, K, T)
+    ht = culsh.HashTables()
+    ht.reset(X.shape[0], X.shape[1], L, M, W, A=A, b=b)
+    ht.index(X)
+    st = _search(culsh, ht, Qm, X, K, T, dense_tc=1)
+    _check_against(st, want, Q, X)
+    pr = st.profile()
+    assert pr["knn_queries"] == (int((want["nonunique"] > 0).sum()) if K <= 20 else 0)
+    assert pr["knn_fallback"] == 0
+
+
+@pytest.mark.parametrize("K", [1, 20, 64])
+def test_edge_k_bound_form(culsh, all_dense, K):
+    """The bound form (real-valued data) at K = 1, 20 and 64 (its lists hold
+    K plus a margin; at 64 they do not fit shared memory and the SIMT kernel
+    serves the dense queries), N ragged, Q crossing the 128-query tile; K
+    above a query's candidate count pads with (-1, FLT_MAX)."""
+    from culsh_gb300 import synth
+    X, Qm, _, _, _ = synth.dataset(1, n=4_999, q=130)
+    L, M, T, W = 6, 6, 8, 40.0
+    A, b = synth.projection(L, M, X.shape[1], W, 3001)
+    want = _oracle_case(X, Qm, A, b, W, K, T)
+    ht = culsh.HashTables()
+    ht.reset(X.shape[0], X.shape[1], L, M, W, A=A, b=b)
+    ht.index(X)
+    st = _search(culsh, ht, Qm, X, K, T, dense_tc=1)
+    _check_against(st, want, Qm.shape[0], X)
+    assert st.profile()["knn_queries"] == (int((want["nonunique"] > 0).sum()) if K <= 20 else 0)
