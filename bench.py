@@ -281,10 +281,12 @@ def cpu_baseline(X, Qm, A, b, d, seconds=12.0):
     t0 = time.perf_counter()
     idx = oracle.build_index(X, A, b, d["W"])
     t_index = time.perf_counter() - t0
+    # calibrate on two queries per host thread so that every thread is busy
+    nc = min(Qm.shape[0], 2 * oracle.num_threads())
     t0 = time.perf_counter()
-    oracle.search(idx, X, Qm[:16], d["K"], d["T"])
-    per_q = max((time.perf_counter() - t0) / 16, 1e-7)
-    nq = int(min(Qm.shape[0], max(16, seconds / per_q)))
+    oracle.search(idx, X, Qm[:nc], d["K"], d["T"])
+    per_q = max((time.perf_counter() - t0) / nc, 1e-7)
+    nq = int(min(Qm.shape[0], max(nc, seconds / per_q)))
     t0 = time.perf_counter()
     oracle.search(idx, X, Qm[:nq], d["K"], d["T"])
     el = time.perf_counter() - t0
@@ -311,11 +313,13 @@ def run_reference(args):
     t0 = time.perf_counter()
     idx = oracle.build_index(X, A, b, d["W"])
     t_index = time.perf_counter() - t0
-    # bounded sample per step: as many queries as take about one second
+    # bounded sample per step: as many queries as take about one second on all
+    # host threads (calibrated on two queries per thread)
+    nc = min(Qm.shape[0], 2 * oracle.num_threads())
     t0 = time.perf_counter()
-    oracle.search(idx, X, Qm[:8], d["K"], d["T"])
-    per_q = max((time.perf_counter() - t0) / 8, 1e-7)
-    nq = int(min(Qm.shape[0], max(8, 1.0 / per_q)))
+    oracle.search(idx, X, Qm[:nc], d["K"], d["T"])
+    per_q = max((time.perf_counter() - t0) / nc, 1e-7)
+    nq = int(min(Qm.shape[0], max(nc, 1.0 / per_q)))
     sample = Qm[:nq]
     for _ in range(args.warmup):
         oracle.search(idx, X, sample, d["K"], d["T"])

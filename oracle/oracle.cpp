@@ -367,7 +367,7 @@ void oracle_search(const float* X, int N, int D, int L, int M, float W, const fl
         std::vector<float> vq(M), rows((size_t)T * M);
         std::vector<uint32_t> cand;
         std::vector<float> dist;
-#pragma omp for schedule(dynamic, 16)
+#pragma omp for schedule(dynamic, 1)  // one query per claim: a small sample still spreads over every thread
         for (int q = 0; q < Q; ++q) {
             uint64_t nu = 0;
             cand.clear();
