@@ -198,7 +198,9 @@ STAGE_NOTES = {
     "membership": "algorithmic bytes are the 4 * C_nu bucket-id reads (each query reads its candidates' ids) "
                   "plus the N/8-byte membership row written per query; about 90 % of the id reads hit L2 "
                   "(the 64 MB of id arrays stay resident), so this is the rate seen at L2, not DRAM (measured "
-                  "DRAM traffic in `traffic`); the stage is bound by the shared-memory atomicOr of each id",
+                  "DRAM traffic in `traffic`); buckets of at least N/64 ids are ORed in as whole N-bit bucket "
+                  "rows (L2-resident) instead of id by id, so part of those id bytes is never read and the "
+                  "rate can exceed the HBM peak; the rest is bound by the shared-memory atomicOr of each id",
     "knn": "flops of the dense GEMM the kernel runs (2 * D * N per dense query); the candidates' own distance "
            "work is the unique-candidate share of it",
 }

@@ -58,7 +58,7 @@ class _Profile(ctypes.Structure):
                 ("candidates_mode", ctypes.c_int), ("graph_mode", ctypes.c_int), ("rechecked", ctypes.c_longlong),
                 ("dense_queries", ctypes.c_int), ("host_path", ctypes.c_int), ("stage_times", ctypes.c_int),
                 ("knn_queries", ctypes.c_int), ("knn_fallback", ctypes.c_int),
-                ("membership_ms", ctypes.c_float), ("knn_ms", ctypes.c_float)]
+                ("membership_ms", ctypes.c_float), ("knn_ms", ctypes.c_float), ("bucket_rows", ctypes.c_int)]
 
 
 class _Tuning(ctypes.Structure):

@@ -574,17 +574,38 @@ __global__ void __launch_bounds__(DT, 1) k_candidates_dense(WsArgs a) {
 // buckets are cut into units of at most BSEG consecutive ids; warp w takes
 // units w, w + 32, ..., loads 32 x BU ids at a time (coalesced: a bucket's
 // ids are contiguous, BU loads in flight per lane) and ORs their bits in.
+// A matched bucket that has a bucket row (a.big_rows; up to BROWS of them
+// per query) sets no bits: its row is ORed into the words as they are copied
+// out, which replaces one shared-memory atomic per id by one 16-byte load
+// per four words. The set is the same either way.
 constexpr int BT = 1024;
 constexpr int BU = 8;
 constexpr uint32_t BSEG = 1024;
 constexpr int BCH = 256;   // (table, probe) slots per compaction chunk
+constexpr uint32_t BROWS = 64;
 
 struct BitmapSmem {
     uint64_t base[BCH];     // ids offset of each matched bucket
     uint32_t size[BCH];
     uint32_t upre[BCH + 1]; // units before each matched bucket
     uint32_t n;
+    uint32_t nrow;          // matched buckets with a bucket row (may exceed BROWS)
+    uint32_t row[BROWS];    // their rows
 };
+
+// Row of global bucket gi among the n ascending bucket numbers of big_gi, -1
+// if it has none.
+__device__ __forceinline__ int big_row(const uint64_t* __restrict__ big_gi, int n, uint64_t gi) {
+    int lo = 0, hi = n - 1;
+    while (lo <= hi) {
+        const int mid = (lo + hi) >> 1;
+        const uint64_t v = __ldg(big_gi + mid);
+        if (v == gi) return mid;
+        if (v < gi) lo = mid + 1;
+        else hi = mid - 1;
+    }
+    return -1;
+}
 
 __global__ void __launch_bounds__(BT, 1) k_cand_bitmap(WsArgs a, uint32_t* __restrict__ bm, int nwp) {
     extern __shared__ __align__(16) uint32_t bits[];
@@ -607,7 +628,10 @@ __global__ void __launch_bounds__(BT, 1) k_cand_bitmap(WsArgs a, uint32_t* __res
         for (int i = tid * 4; i < nwp; i += BT * 4) *reinterpret_cast<uint4*>(bits + i) = make_uint4(0u, 0u, 0u, 0u);
         for (int c0 = 0; c0 < LT; c0 += BCH) {
             // matched buckets of this chunk of (table, probe) slots, with sizes
-            if (tid == 0) g.n = 0;
+            if (tid == 0) {
+                g.n = 0;
+                if (c0 == 0) g.nrow = 0;
+            }
             __syncthreads();
             const int c1 = min(LT, c0 + BCH);
             for (int e = c0 + tid; e < c1; e += BT) {
@@ -616,6 +640,16 @@ __global__ void __launch_bounds__(BT, 1) k_cand_bitmap(WsArgs a, uint32_t* __res
                 if (j >= 0) {
                     const uint64_t gi = __ldg(a.boff + l) + (uint32_t)j;
                     const uint32_t st = __ldg(a.starts + gi), sz = __ldg(a.sizes + gi);
+                    if (a.nbig > 0 && sz >= a.big_min) {
+                        const int r = big_row(a.big_gi, a.nbig, gi);
+                        if (r >= 0) {
+                            const uint32_t kr = atomicAdd(&g.nrow, 1u);
+                            if (kr < BROWS) {
+                                g.row[kr] = (uint32_t)r;
+                                continue;
+                            }
+                        }
+                    }
                     if (sz) {
                         const uint32_t kk = atomicAdd(&g.n, 1u);
                         g.base[kk] = (uint64_t)l * (uint64_t)a.N + st;
@@ -675,9 +709,18 @@ __global__ void __launch_bounds__(BT, 1) k_cand_bitmap(WsArgs a, uint32_t* __res
             __syncthreads();
         }
         uint32_t* row = bm + (int64_t)k * nwp;
+        const uint32_t nrow = min(g.nrow, BROWS);
         unsigned long long cnt = 0;
         for (int i = tid * 4; i < nwp; i += BT * 4) {
-            const uint4 v = *reinterpret_cast<const uint4*>(bits + i);
+            uint4 v = *reinterpret_cast<const uint4*>(bits + i);
+#pragma unroll 4
+            for (uint32_t r = 0; r < nrow; ++r) {
+                const uint4 w = __ldg(reinterpret_cast<const uint4*>(a.big_rows + (size_t)g.row[r] * nwp + i));
+                v.x |= w.x;
+                v.y |= w.y;
+                v.z |= w.z;
+                v.w |= w.w;
+            }
             *reinterpret_cast<uint4*>(row + i) = v;
             cnt += __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
         }
@@ -697,6 +740,51 @@ __global__ void __launch_bounds__(BT, 1) k_cand_bitmap(WsArgs a, uint32_t* __res
 }
 
 size_t bitmap_smem_bytes(int64_t N) { return 4 * (size_t)((((N + 31) >> 5) + 3) & ~3ll); }
+
+__global__ void k_big_find(const uint32_t* __restrict__ sizes, uint64_t totB, uint32_t big_min, uint64_t* gi,
+                           uint32_t* sz, unsigned int* cnt, unsigned int cap) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < totB; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t s = sizes[i];
+        if (s >= big_min) {
+            const unsigned int k = atomicAdd(cnt, 1u);
+            if (k < cap) {
+                gi[k] = i;
+                sz[k] = s;
+            }
+        }
+    }
+}
+
+// Row r (blockIdx.y) gets the bits of bucket gi[r]'s ids (table tl[r]).
+__global__ void k_big_fill(const uint64_t* __restrict__ gi, const int32_t* __restrict__ tl,
+                           const uint32_t* __restrict__ starts, const uint32_t* __restrict__ sizes,
+                           const uint32_t* __restrict__ ids, int64_t N, uint32_t* rows, int nwp) {
+    const int r = blockIdx.y;
+    const uint64_t b = gi[r];
+    const uint32_t st = starts[b], sz = sizes[b];
+    const uint32_t* src = ids + (uint64_t)tl[r] * N + st;
+    uint32_t* row = rows + (size_t)r * nwp;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < sz; j += gridDim.x * blockDim.x) {
+        const uint32_t v = src[j];
+        atomicOr(row + (v >> 5), 1u << (v & 31));
+    }
+}
+
+cudaError_t launch_big_find(const uint32_t* sizes, uint64_t totB, uint32_t big_min, uint64_t* gi, uint32_t* sz,
+                            unsigned int* cnt, unsigned int cap, cudaStream_t st) {
+    if (totB == 0) return cudaSuccess;
+    const unsigned g = (unsigned)std::min<uint64_t>((totB + 255) / 256, 4096);
+    k_big_find<<<g, 256, 0, st>>>(sizes, totB, big_min, gi, sz, cnt, cap);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_big_fill(const uint64_t* gi, const int32_t* tl, int nbig, const uint32_t* starts,
+                            const uint32_t* sizes, const uint32_t* ids, int64_t N, uint32_t* rows, int nwp,
+                            cudaStream_t st) {
+    if (nbig <= 0) return cudaSuccess;
+    k_big_fill<<<dim3(16, (unsigned)nbig), 256, 0, st>>>(gi, tl, starts, sizes, ids, N, rows, nwp);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_cand_bitmap(const WsArgs& a, uint32_t* bm, int nwp, int grid, cudaStream_t st) {
     static std::atomic<size_t> cap{0};

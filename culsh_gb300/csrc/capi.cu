@@ -148,6 +148,15 @@ struct culsh_index {
     DevBuf<KnnState> kstate;
     KnnState h_kstate{};
     bool kx_valid = false;
+    // bucket rows of the largest buckets (membership rows of the tensor-core
+    // path), made on first use after each build or load
+    DevBuf<uint64_t> big_gi;
+    DevBuf<int32_t> big_tl;
+    DevBuf<uint32_t> big_sz, big_rows;
+    DevBuf<unsigned int> big_cnt;
+    int nbig = 0;
+    uint32_t big_min = UINT32_MAX;
+    bool big_valid = false;
     int KW = 1;
     std::vector<int32_t> h_cmin, h_cmax;
     std::vector<uint8_t> h_fbits;
@@ -253,6 +262,7 @@ struct culsh_search {
     DevBuf<uint32_t> kpart_id;
     DevBuf<int> kpart_n, kfallback;
     int knn_queries = 0, knn_fallback = 0;   // last search: dense queries on the tensor cores, re-run
+    int bucket_rows = 0;                     // last search: bucket rows its membership rows could use
     int sms = 0, smem_optin = 0, ws_used = 0, ws_overflow = 0;
     long long occ_key = -1;
     int occ_val = 1;
@@ -315,6 +325,7 @@ void clear_index_state(culsh_index* ix) {
     ix->proj_on_dev = false;
     ix->xb_valid = false;
     ix->kx_valid = false;
+    ix->big_valid = false;
 }
 
 int upload_projection(culsh_index* ix, cudaStream_t st) {
@@ -660,6 +671,7 @@ int sort_keys(culsh_index* ix, int N, int passes, cudaStream_t st, const uint32_
 int build_device(culsh_index* ix, const float* dX, cudaStream_t st, FILE* dbg) {
     const int N = ix->N, D = ix->D, L = ix->L, M = ix->M, LM = L * M;
     const double t0 = seconds_now();
+    ix->big_valid = false;
     for (auto& e : ix->bev)
         if (!e) CU_TRY(cudaEventCreate(&e));
     CU_TRY(cudaEventRecord(ix->bev[0], st));
@@ -791,6 +803,7 @@ int ensure_device(culsh_index* ix, cudaStream_t st) {
     if (ix->dev_valid) return upload_projection(ix, st);
     if (!ix->host_valid) return fail(CULSH_ERR_STATE, "No index: have you performed indexing or loaded a file???");
     const int L = ix->L, N = ix->N, M = ix->M, LM = L * M;
+    ix->big_valid = false;
     TRY(upload_projection(ix, st));
     CU_TRY(ix->err.reserve(1));
     CU_TRY(cudaMemsetAsync(ix->err.p, 0, sizeof(int), st));
@@ -968,6 +981,78 @@ int ensure_knn_rows(culsh_index* ix, cudaStream_t st) {
     return CULSH_OK;
 }
 
+// Bucket rows: every bucket of at least big_min ids gets an N-bit row (nwp
+// words), which the membership kernel ORs into a dense query's row instead of
+// setting the bucket's bits id by id. big_min = max(1024, N/64), where a row
+// (N/8 bytes) is at most twice the bucket's ids (4 bytes each); there are then
+// at most 64 L rows. CULSH_BIG_ROWS_MIN overrides big_min (0: no rows). Rows
+// beyond kBigRowsBytes keep only the largest buckets. Made once per index; the
+// stream is drained before they are published.
+constexpr size_t kBigRowsBytes = size_t(1) << 30;
+
+int ensure_big_rows(culsh_index* ix, int nwp, cudaStream_t st) {
+    if (ix->big_valid) return CULSH_OK;
+    const int L = ix->L, N = ix->N;
+    ix->nbig = 0;
+    ix->big_min = UINT32_MAX;
+    long long bmin = std::max(1024ll, (long long)N / 64);
+    if (const char* e = getenv("CULSH_BIG_ROWS_MIN")) bmin = atoll(e);
+    if (bmin <= 0 || (long long)ix->max_bucket < bmin) {
+        ix->big_valid = true;
+        return CULSH_OK;
+    }
+    const uint64_t totB = ix->h_boff[L];
+    const unsigned int cap = (unsigned int)std::min<long long>((long long)L * (N / bmin) + 1, 1ll << 20);
+    CU_TRY(ix->big_gi.reserve(cap));
+    CU_TRY(ix->big_sz.reserve(cap));
+    CU_TRY(ix->big_cnt.reserve(1));
+    CU_TRY(cudaMemsetAsync(ix->big_cnt.p, 0, sizeof(unsigned int), st));
+    CU_TRY(launch_big_find(ix->sizes.p, totB, (uint32_t)bmin, ix->big_gi.p, ix->big_sz.p, ix->big_cnt.p, cap, st));
+    unsigned int cnt = 0;
+    CU_TRY(cudaMemcpyAsync(&cnt, ix->big_cnt.p, sizeof(cnt), cudaMemcpyDeviceToHost, st));
+    CU_TRY(cudaStreamSynchronize(st));
+    cnt = std::min(cnt, cap);
+    std::vector<uint64_t> gi(cnt);
+    std::vector<uint32_t> sz(cnt);
+    CU_TRY(cudaMemcpyAsync(gi.data(), ix->big_gi.p, 8 * (size_t)cnt, cudaMemcpyDeviceToHost, st));
+    CU_TRY(cudaMemcpyAsync(sz.data(), ix->big_sz.p, 4 * (size_t)cnt, cudaMemcpyDeviceToHost, st));
+    CU_TRY(cudaStreamSynchronize(st));
+    std::vector<uint32_t> ord(cnt);
+    for (uint32_t i = 0; i < cnt; ++i) ord[i] = i;
+    const size_t row_bytes = 4 * (size_t)nwp;
+    const size_t keep = std::min<size_t>({(size_t)cnt, kBigRowsBytes / row_bytes, 65535});
+    uint32_t kept_min = (uint32_t)bmin;
+    if (keep < cnt) {
+        // the largest buckets; a bucket of the smallest kept size without a
+        // row is still served id by id
+        std::sort(ord.begin(), ord.end(), [&](uint32_t x, uint32_t y) { return sz[x] > sz[y]; });
+        ord.resize(keep);
+        kept_min = keep ? sz[ord.back()] : UINT32_MAX;
+    }
+    std::sort(ord.begin(), ord.end(), [&](uint32_t x, uint32_t y) { return gi[x] < gi[y]; });
+    std::vector<uint64_t> hg(keep);
+    std::vector<int32_t> ht(keep);
+    for (size_t r = 0; r < keep; ++r) {
+        hg[r] = gi[ord[r]];
+        ht[r] = (int32_t)(std::upper_bound(ix->h_boff.begin(), ix->h_boff.begin() + L + 1, hg[r]) -
+                          ix->h_boff.begin()) - 1;
+    }
+    if (keep > 0) {
+        CU_TRY(ix->big_tl.reserve(keep));
+        CU_TRY(ix->big_rows.reserve(keep * (size_t)nwp));
+        CU_TRY(cudaMemcpyAsync(ix->big_gi.p, hg.data(), 8 * keep, cudaMemcpyHostToDevice, st));
+        CU_TRY(cudaMemcpyAsync(ix->big_tl.p, ht.data(), 4 * keep, cudaMemcpyHostToDevice, st));
+        CU_TRY(cudaMemsetAsync(ix->big_rows.p, 0, keep * row_bytes, st));
+        CU_TRY(launch_big_fill(ix->big_gi.p, ix->big_tl.p, (int)keep, ix->starts.p, ix->sizes.p, ix->ids.p, N,
+                               ix->big_rows.p, nwp, st));
+        CU_TRY(cudaStreamSynchronize(st));
+    }
+    ix->nbig = (int)keep;
+    ix->big_min = keep ? kept_min : UINT32_MAX;
+    ix->big_valid = true;
+    return CULSH_OK;
+}
+
 // Whether the dataset's values allow the exact form (integers of magnitude
 // <= 256, D max|v|^2 < 2^24 and D (max - min)^2 < 2^24); the queries must
 // qualify too, which the kernels check on the device.
@@ -1000,6 +1085,7 @@ int plan_knn(culsh_search* s, SearchPlan& P, int Q, int32_t* d_ids, float* d_d, 
     if (4 * bm_words > kKnnMaxBitmapBytes) return CULSH_OK;
     TRY(ensure_knn_rows(ix, st));
     if (ix->h_kstate.flags & kKnnNonFinite) return CULSH_OK;
+    TRY(ensure_big_rows(ix, k.nwp, st));
     k.exact_possible = knn_dataset_exact(ix) && k.ops_exact > 0;
     k.C = knn_bound_factor(ix->D);
     CU_TRY(s->kbm.reserve(bm_words));
@@ -1256,6 +1342,14 @@ int plan_search(culsh_search* s, const float* dQ, int Q, int32_t* d_ids, float* 
             a.dense_q = s->dense_q.p;
             P.dense_grid = s->sms;
             if (P.use_knn) P.kn.dense_q = s->dense_q.p;
+        }
+        a.nbig = 0;
+        a.big_min = UINT32_MAX;
+        if (P.use_knn && ix->nbig > 0 && !getenv("CULSH_NO_BIG_ROWS")) {
+            a.big_gi = ix->big_gi.p;
+            a.big_rows = ix->big_rows.p;
+            a.nbig = ix->nbig;
+            a.big_min = ix->big_min;
         }
         if (tu.ws_order) {
             CU_TRY(s->qorder.reserve(Q));
@@ -1522,11 +1616,12 @@ int finish_search(culsh_search* s, const SearchPlan& P, cudaStream_t st) {
     }
     s->tot_unique = s->h_stats.p[0];
     s->tot_nonunique = s->h_stats.p[1];
-    s->knn_queries = s->knn_fallback = 0;
+    s->knn_queries = s->knn_fallback = s->bucket_rows = 0;
     if (P.use_knn && !s->ws_overflow) {
         if ((s->h_stats.p[11] & 0xffffffffu) != 0)
             return fail(CULSH_ERR_DEVICE, "tensor-core k-NN: a bounded device wait gave up");
         s->knn_queries = (int)(s->h_stats.p[7] & 0xffffffffu);
+        s->bucket_rows = P.wa.nbig;
         // queries whose bound-form lists could not prove their top-K: the
         // exact per-query kernel (their counts were taken already)
         const unsigned int nfb = (unsigned int)(s->h_stats.p[10] & 0xffffffffu);
@@ -2386,6 +2481,7 @@ int culsh_search_profile_get(culsh_search* s, culsh_search_profile* out) {
     out->host_path = s->host_path;
     out->knn_queries = s->knn_queries;
     out->knn_fallback = s->knn_fallback;
+    out->bucket_rows = s->bucket_rows;
     return CULSH_OK;
 }
 

@@ -370,6 +370,15 @@ struct WsArgs {
     // with shared candidates run close together and share rows in L2.
     uint32_t* order;                   // [Q] queries in that order; nullptr: index order
     uint32_t* order_bins;              // [kOrderBins + 1] counting-sort bins
+    // Bucket rows (tensor-core path): the index's largest buckets as N-bit
+    // rows, ORed into a dense query's membership row instead of setting the
+    // bits of their ids one by one. big_gi holds their global bucket numbers
+    // (boff[l] + j) in ascending order; every bucket of big_min ids or more
+    // has a row. nbig == 0: none.
+    const uint64_t* big_gi;
+    const uint32_t* big_rows;          // [nbig][nwp]
+    int nbig;
+    uint32_t big_min;
 };
 constexpr int kOrderBins = 4096;
 cudaError_t launch_order_queries(const WsArgs& a, cudaStream_t st);   // 3 kernels + 1 memset
@@ -379,6 +388,14 @@ size_t ws_smem_bytes(int D, int K, int wt, int bf16, int slots);
 int ws_blocks_per_sm(int D, int K, int wt, int bf16, int slots);
 cudaError_t launch_bf16_rows(const float* X, int64_t N, int D, uint16_t* xb, uint8_t* flag, cudaStream_t st);
 cudaError_t launch_plan_items(const WsArgs& a, cudaStream_t st);
+// Bucket rows: the global numbers and sizes of the buckets of at least
+// big_min ids (at most cap, in no order; *cnt counts them), then their rows
+// (rows zeroed beforehand; tl[r] is bucket r's table).
+cudaError_t launch_big_find(const uint32_t* sizes, uint64_t totB, uint32_t big_min, uint64_t* gi, uint32_t* sz,
+                            unsigned int* cnt, unsigned int cap, cudaStream_t st);
+cudaError_t launch_big_fill(const uint64_t* gi, const int32_t* tl, int nbig, const uint32_t* starts,
+                            const uint32_t* sizes, const uint32_t* ids, int64_t N, uint32_t* rows, int nwp,
+                            cudaStream_t st);
 cudaError_t launch_candidates_ws(const WsArgs& a, int grid, cudaStream_t st);
 
 // ---------------------------------------------------------------------------

@@ -238,6 +238,9 @@ typedef struct culsh_search_profile {
                             candidate membership rows ...                   */
     float knn_ms;        /* ... and the tensor-core distances, top-K lists
                             and merge (0 unless measured)                   */
+    int bucket_rows;     /* tensor-core path: index buckets kept as N-bit rows
+                            and ORed whole into the membership rows (buckets
+                            of at least max(1024, N/64) ids); 0: none       */
 } culsh_search_profile;
 int culsh_search_profile_get(culsh_search* s, culsh_search_profile* out);
 

@@ -205,3 +205,34 @@ def test_edge_k_bound_form(culsh, all_dense, K):
     st = _search(culsh, ht, Qm, X, K, T, dense_tc=1)
     _check_against(st, want, Qm.shape[0], X)
     assert st.profile()["knn_queries"] == (int((want["nonunique"] > 0).sum()) if K <= 20 else 0)
+
+
+@pytest.mark.parametrize("W,big_min", [(825.0, None), (825.0, "64"), (825.0, "1"), (825.0, "0"), (600.0, "1")])
+def test_bucket_rows(culsh, all_dense, monkeypatch, W, big_min):
+    """Membership rows with the index's largest buckets ORed in whole (bucket
+    rows) hold the same sets as rows built id by id. Thresholds: the default
+    max(1024, N/64) (one bucket here), 64 ids (hundreds of rows), 1 (every
+    bucket has a row: a query matches more of them than a block keeps, the
+    rest go id by id), none; at W = 600 more buckets than the row cap, so
+    only the largest keep rows. Ids, distances and both candidate totals
+    equal the oracle's."""
+    from culsh_gb300 import synth
+    if big_min is not None:
+        monkeypatch.setenv("CULSH_BIG_ROWS_MIN", big_min)
+    X, Qm, _, _, _ = synth.dataset(2, n=20_000, q=300)
+    L, M, T, K = 16, 12, 16, 10
+    A, b = synth.projection(L, M, X.shape[1], W, 3002)
+    want = _oracle_case(X, Qm, A, b, W, K, T)
+    ht = culsh.HashTables()
+    ht.reset(X.shape[0], X.shape[1], L, M, W, A=A, b=b)
+    ht.index(X)
+    st = _search(culsh, ht, Qm, X, K, T, dense_tc=1)
+    _check_against(st, want, Qm.shape[0], X)
+    pr = st.profile()
+    assert pr["knn_queries"] == int((want["nonunique"] > 0).sum())
+    if big_min == "0":
+        assert pr["bucket_rows"] == 0
+    elif big_min == "1" and W == 600.0:
+        assert pr["bucket_rows"] == 65535
+    else:
+        assert pr["bucket_rows"] > 0
