@@ -468,6 +468,10 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
                 thr = INFINITY;
             }
             const int acc = (int)(i & 1);
+            const int gq = (int)qt * MQ + row;   // dense position of this lane's query
+            // the shared bound is read before the waits (its latency overlaps
+            // them): it only decreases, so an earlier value is still a bound
+            const uint32_t ext_enc = kExact ? __ldcg(a.qbound + gq) : 0u;
             // every lane waits (and so sees the copied data); the warp leaves
             // together if any lane gave up, since tcgen05.ld is warp-wide
             const bool ok = bar_wait(tfull + acc, (uint32_t)((i >> 1) & 1), abort_flag, a.err) &&
@@ -475,8 +479,7 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
             if (!__all_sync(0xffffffffu, ok)) break;
             fence_after();
             const unsigned char* es = sE + (size_t)e * ep_stride;
-            const int gq = (int)qt * MQ + row;   // dense position of this lane's query
-            const float ext = kExact ? key_dec(__ldcg(a.qbound + gq)) : INFINITY;
+            const float ext = kExact ? key_dec(ext_enc) : INFINITY;
             // a key enters iff key < thr and key <= ext, i.e. key < lim
             const float ext_up = nextafterf(ext, INFINITY);
             float lim = fminf(thr, ext_up);
