@@ -2393,6 +2393,7 @@ int culsh_search_autotune(culsh_search* s, const float* d_queries, int Q, int* d
         const unsigned long long N = (unsigned long long)s->ix->N;
         const int mins[3] = {0, (int)std::max(1024ull, N / 1024), (int)std::max(1024ull, N / 64)};
         const SearchTune base_t = best;
+        float t_simt = -1.0f;   // the SIMT form (dense_tc = 0) at the chosen gather settings
         for (int tc = 0; tc < 2; ++tc)
             for (int mi = 0; mi < 3; ++mi) {
                 if ((tc == 0 && mi > 0) || (tc == base_t.dense_tc && mins[mi] == base_t.dense_min)) continue;
@@ -2405,11 +2406,42 @@ int culsh_search_autotune(culsh_search* s, const float* d_queries, int Q, int* d
                     s->tune = start;
                     return rc;
                 }
+                if (tc == 0) t_simt = stage[2];
                 if (stage[2] < best_t) {
                     best = t;
                     best_t = stage[2];
                 }
             }
+        if (base_t.dense_tc == 0) t_simt = best_t;
+        // The gather settings above were chosen with the tensor-core path
+        // taking the dense queries; without it every query is gathered and
+        // another set and partition size may win. Where the SIMT form came
+        // within 4x of the best, its set sizes and orders are tried again.
+        if (best.dense_tc == 1 && best.cand_ws && t_simt > 0.0f && t_simt < 4.0f * best_t) {
+            const int sets[7][2] = {{4096, 1024}, {4096, 2048}, {8192, 1024}, {8192, 2048},
+                                    {8192, 4096}, {16384, 4096}, {16384, 8192}};
+            const SearchTune simt_base = base_t;
+            for (int o = 0; o < 2; ++o)
+                for (int b = 0; b < 7; ++b) {
+                    SearchTune t = simt_base;
+                    t.dense_tc = 0;
+                    t.dense_min = 0;
+                    t.ws_slots = sets[b][0];
+                    t.ws_chunk = sets[b][1];
+                    t.ws_order = o;
+                    t.ws_bps = 0;
+                    s->tune = t;
+                    const int rc = measure(stage);
+                    if (rc != CULSH_OK) {
+                        s->tune = start;
+                        return rc;
+                    }
+                    if (stage[2] < best_t) {
+                        best = t;
+                        best_t = stage[2];
+                    }
+                }
+        }
     }
     s->tune = best;
     const int rc = measure(stage);
