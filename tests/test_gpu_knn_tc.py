@@ -236,3 +236,32 @@ def test_bucket_rows(culsh, all_dense, monkeypatch, W, big_min):
         assert pr["bucket_rows"] == 65535
     else:
         assert pr["bucket_rows"] > 0
+
+
+def test_bucket_rows_follow_rebuilds_and_loads(culsh, all_dense, monkeypatch, tmp_path):
+    """Bucket rows belong to one build of the index: when the same object
+    indexes another dataset, and when a saved index is loaded into a new
+    object, the rows are made again from the new buckets (stale rows would
+    add candidates and change the unique counts)."""
+    from culsh_gb300 import synth
+    monkeypatch.setenv("CULSH_BIG_ROWS_MIN", "64")
+    Xa, Qm, _, _, _ = synth.dataset(2, n=40_000, q=200)
+    X1, X2 = np.ascontiguousarray(Xa[:20_000]), np.ascontiguousarray(Xa[20_000:])
+    L, M, T, K, W = 16, 12, 16, 10, 825.0
+    A, b = synth.projection(L, M, X1.shape[1], W, 3002)
+    ht = culsh.HashTables()
+    ht.reset(X1.shape[0], X1.shape[1], L, M, W, A=A, b=b)
+    want = None
+    for X in (X1, X2):
+        want = _oracle_case(X, Qm, A, b, W, K, T)
+        ht.index(X)
+        st = _search(culsh, ht, Qm, X, K, T, dense_tc=1)
+        _check_against(st, want, Qm.shape[0], X)
+        assert st.profile()["bucket_rows"] > 0
+    path = str(tmp_path / "rows.index")
+    ht.save(path)
+    ht2 = culsh.HashTables()
+    ht2.load(path)
+    st = _search(culsh, ht2, Qm, X2, K, T, dense_tc=1)
+    _check_against(st, want, Qm.shape[0], X2)
+    assert st.profile()["bucket_rows"] > 0
