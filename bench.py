@@ -535,25 +535,28 @@ def recall_point(culsh, torch, dev, steps, warmup, autotune=True, fixed=None):
         if fixed and ("distance_bf16" in fixed and fixed["distance_bf16"] != bf or
                       "dense_tc" in fixed and fixed["dense_tc"] != tc):
             continue
-        # each gather form at its own best set size, partition size, item order
-        # and resident items per SM (untimed selection among a few; the tuner's
-        # choice is one of them, but it may have tuned another form)
+        # each gather form at its own best set size, partition size, item order,
+        # resident items per SM and item width (untimed selection among a few;
+        # the tuner's choice is one of them, but it may have tuned another form)
         t0 = st.get_tuning()
-        best = (0.0, t0["ws_set_slots"], t0["ws_chunk"], t0["ws_order"], t0["ws_blocks_per_sm"])
+        best = (0.0, t0["ws_set_slots"], t0["ws_chunk"], t0["ws_order"], t0["ws_blocks_per_sm"],
+                t0["ws_threads"])
         grid = () if (fixed or tc) else ((4096, 2048), (8192, 4096), (16384, 8192))
         for sl, ch in grid:
             for order in (0, 1):
                 for bps in (0, 1):
-                    st.set_tuning(candidates_mode=1, distance_bf16=bf, dense_tc=tc, dense_min=0,
-                                  ws_set_slots=sl, ws_chunk=ch, ws_order=order, ws_blocks_per_sm=bps)
-                    t = []
-                    for _ in range(3):
-                        st.search_device(qt.data_ptr(), Q, ids.data_ptr(), dists.data_ptr(), sp)
-                        t.append(st.profile()["candidates_ms"])
-                    if best[0] == 0.0 or statistics.median(t) < best[0]:
-                        best = (statistics.median(t), sl, ch, order, bps)
+                    for wt in (256, 512):
+                        st.set_tuning(candidates_mode=1, distance_bf16=bf, dense_tc=tc, dense_min=0,
+                                      ws_set_slots=sl, ws_chunk=ch, ws_order=order, ws_blocks_per_sm=bps,
+                                      ws_threads=wt)
+                        t = []
+                        for _ in range(3):
+                            st.search_device(qt.data_ptr(), Q, ids.data_ptr(), dists.data_ptr(), sp)
+                            t.append(st.profile()["candidates_ms"])
+                        if best[0] == 0.0 or statistics.median(t) < best[0]:
+                            best = (statistics.median(t), sl, ch, order, bps, wt)
         st.set_tuning(candidates_mode=1, distance_bf16=bf, dense_tc=tc, ws_set_slots=best[1], ws_chunk=best[2],
-                      ws_order=best[3], ws_blocks_per_sm=best[4], dense_min=(1024 if tc else 0))
+                      ws_order=best[3], ws_blocks_per_sm=best[4], ws_threads=best[5], dense_min=(1024 if tc else 0))
         for _ in range(warmup):
             st.search_device(qt.data_ptr(), Q, ids.data_ptr(), dists.data_ptr(), sp)
         ms = timed_searches(st, torch, stream, sp, qt, Q, ids, dists, flush, steps)
@@ -566,7 +569,8 @@ def recall_point(culsh, torch, dev, steps, warmup, autotune=True, fixed=None):
                        "tensor_core_queries": int(pr["knn_queries"]), "fallback_queries": int(pr["knn_fallback"]),
                        "identical_to_fp32": bool(np.array_equal(out, ref))}
         if not tc:
-            forms[name].update({"set_slots": best[1], "chunk": best[2], "order": best[3], "blocks_per_sm": best[4]})
+            forms[name].update({"set_slots": best[1], "chunk": best[2], "order": best[3], "blocks_per_sm": best[4],
+                                "threads": best[5]})
     uniq = st.getTotalCandidates_unique() / Q
     rec = recall_at_k(ref[:200], X, Qm[:200], K)
     return {"workload": f"gauss-mixture-1m-d128 N={N} L={L} M={M} W={W} T={T} K={K} Q={Q}",

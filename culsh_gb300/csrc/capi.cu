@@ -2416,16 +2416,22 @@ int culsh_search_autotune(culsh_search* s, const float* d_queries, int Q, int* d
         // The gather settings above were chosen with the tensor-core path
         // taking the dense queries; without it every query is gathered and
         // another set and partition size may win. Where the SIMT form came
-        // within 4x of the best, its set sizes and orders are tried again.
+        // within 4x of the best, its item widths, set sizes, orders and
+        // distance forms are tried again (the grid above, 112 configurations).
         if (best.dense_tc == 1 && best.cand_ws && t_simt > 0.0f && t_simt < 4.0f * best_t) {
             const int sets[7][2] = {{4096, 1024}, {4096, 2048}, {8192, 1024}, {8192, 2048},
                                     {8192, 4096}, {16384, 4096}, {16384, 8192}};
+            const int wts[4] = {64, 128, 256, 512};
             const SearchTune simt_base = base_t;
-            for (int o = 0; o < 2; ++o)
+            for (int f = 0; f < 2; ++f)
+              for (int o = 0; o < 2; ++o)
+               for (int w = 0; w < 4; ++w)
                 for (int b = 0; b < 7; ++b) {
                     SearchTune t = simt_base;
                     t.dense_tc = 0;
                     t.dense_min = 0;
+                    t.dist_bf16 = f;
+                    t.ws_wt = wts[w];
                     t.ws_slots = sets[b][0];
                     t.ws_chunk = sets[b][1];
                     t.ws_order = o;
