@@ -1,6 +1,7 @@
 """Full-size parity: the 100k x 128 Gaussian-mixture workload and the
 1M x 128 integer-feature workload, index and search compared bit for bit
-against the CPU oracle, plus size-independent properties of the index; the
+against the CPU oracle (the latter also at its recall operating point,
+W = 825), plus size-independent properties of the index; the
 4M x 128 Zipf-cluster and 10M x 96 serving workloads through whole-table,
 sampled-point and search comparisons; the D = 960 unit-sphere workload's
 shapes at 100,000 points on both projection kernels."""
@@ -73,6 +74,39 @@ def test_full_size_against_oracle(culsh, config):
     # every near-data query of the mixture workload finds candidates
     if config == 1:
         assert st.getTotalCandidates_unique() > 0
+
+
+def test_full_size_recall_point(culsh):
+    """The headline operating point at full size: the 1M x 128 integer
+    features at W = 825 (recall@10 above 0.9), where a held-out query's
+    candidates are half the dataset. Its dense queries take the tensor-core
+    exact form with bucket rows; ids, distances, query buckets and both
+    candidate totals must equal the oracle's for held-out and near-data
+    queries."""
+    X, Qm, _, _, cfg = synth.dataset(2)
+    N, D, L, M, W, K, T = X.shape[0], cfg.D, cfg.L, cfg.M, 825.0, cfg.K, cfg.T
+    A, b = synth.projection(L, M, D, W, 3002)
+    ht = culsh.HashTables()
+    ht.reset(N, D, L, M, W, A=A, b=b)
+    ht.index(X)
+    ref = oracle.build_index(X, A, b, W)
+    np.testing.assert_array_equal(ht.getBuckets(), ref.buckets)
+    rng = np.random.default_rng(825)
+    near = np.clip(np.rint(X[rng.integers(0, N, 100)] + rng.normal(0, 2.0, (100, D))), 0, 255).astype(np.float32)
+    queries = np.concatenate([Qm[:200], near])
+    Q = queries.shape[0]
+    st = culsh.SearchTables()
+    st.reset(ht, K, T)
+    st.search(queries, dataset=X)
+    want = oracle.search(ref, X, queries, K, T)
+    np.testing.assert_array_equal(st.getKnnIds(), want["knn_ids"])
+    np.testing.assert_array_equal(st.getKnnDistances(), want["knn_dists"])
+    for l in range(L):
+        np.testing.assert_array_equal(st.getQueryBuckets(l), want["qbuckets"][l].reshape(Q, T))
+    assert st.getTotalCandidates_unique() == int(want["unique"].sum())
+    assert st.getTotalCandidates_nonUnique() == int(want["nonunique"].sum())
+    pr = st.profile()
+    assert pr["knn_queries"] > 0.9 * Q and pr["knn_fallback"] == 0 and pr["bucket_rows"] > 0
 
 
 def gpu_index_arrays(ht, N, L, M):
