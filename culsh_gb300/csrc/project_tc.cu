@@ -488,6 +488,19 @@ __global__ void k_tc_recompute(const float* __restrict__ X, int64_t N, int D, co
         } else if (stage_a) {
             const float* av = sA + (int64_t)c * Dq;
             for (int d = 0; d < D; ++d) acc = __fmaf_rn(__ldg(x + d), av[d], acc);
+        } else if ((D & 3) == 0) {
+            // A too large for shared memory (high D): 16-byte loads of the
+            // row and of the column's A row from L2, same FMA order
+            const float* av = A + (int64_t)c * D;
+#pragma unroll 4
+            for (int d = 0; d < D; d += 4) {
+                const float4 x4 = __ldg(reinterpret_cast<const float4*>(x + d));
+                const float4 a4 = __ldg(reinterpret_cast<const float4*>(av + d));
+                acc = __fmaf_rn(x4.x, a4.x, acc);
+                acc = __fmaf_rn(x4.y, a4.y, acc);
+                acc = __fmaf_rn(x4.z, a4.z, acc);
+                acc = __fmaf_rn(x4.w, a4.w, acc);
+            }
         } else {
             const float* av = A + (int64_t)c * D;
             for (int d = 0; d < D; ++d) acc = __fmaf_rn(__ldg(x + d), __ldg(av + d), acc);
