@@ -153,24 +153,18 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-// The 64 accumulator columns [taddr, taddr + 64) of this thread's TMEM lane,
+// The 32 accumulator columns [taddr, taddr + 32) of this thread's TMEM lane,
 // loaded and waited for in one statement, so that no use of r can be
 // scheduled before the wait.
-__device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t (&r)[64]) {
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%64];\n\t"
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%32, %33, %34, %35, %36, %37, %38, %39, %40, %41, %42, %43, %44, "
-        "%45, %46, %47, %48, %49, %50, %51, %52, %53, %54, %55, %56, %57, %58, %59, %60, %61, %62, %63}, [%64+32];\n\t"
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n\t"
         "tcgen05.wait::ld.sync.aligned;"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
           "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
           "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]),
-          "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]),
-          "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]),
-          "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]), "=r"(r[56]),
-          "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
         : "r"(taddr)
         : "memory");
 }
@@ -488,33 +482,37 @@ __global__ void __launch_bounds__(64 + 32 * NEPI, 1)
             const uint32_t id0 = (uint32_t)(pt * BN + ch * CW);
             const uint32_t tbase =
                 tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)((acc * MH + hq) * BN + ch * CW);
-            uint32_t r[64];
-            tmem_ld64(tbase, r);
-            // the accumulator slice is in registers: release it to the MMA
-            // warp now, so that the next products into it overlap this
-            // tile's key work
-            fence_before();
-            __syncwarp();
-            if (lane == 0) bar_arrive(tempty + acc);
-            // keys t = w - 2 q.x (packed FMA, in place)
-#pragma unroll
-            for (int j = 0; j < 64; j += 4) {
-                const float4 w4 = *reinterpret_cast<const float4*>(wv + j);
-                const float2 a = __ffma2_rn(make_float2(-2.0f, -2.0f),
-                                            make_float2(__uint_as_float(r[j]), __uint_as_float(r[j + 1])),
-                                            make_float2(w4.x, w4.y));
-                const float2 b = __ffma2_rn(make_float2(-2.0f, -2.0f),
-                                            make_float2(__uint_as_float(r[j + 2]), __uint_as_float(r[j + 3])),
-                                            make_float2(w4.z, w4.w));
-                r[j] = __float_as_uint(a.x);
-                r[j + 1] = __float_as_uint(a.y);
-                r[j + 2] = __float_as_uint(b.x);
-                r[j + 3] = __float_as_uint(b.y);
-            }
 #pragma unroll
             for (int c = 0; c < 2; ++c) {
+                // The slice's two 32-column halves are loaded and ranked in
+                // turn, so that only 32 keys are live at a time; the
+                // accumulator goes back to the MMA warp as soon as the second
+                // half is in registers (the next products into it overlap the
+                // rest of this tile's key work).
+                uint32_t rc[32];
+                if (c == 1) __syncwarp();   // tcgen05.ld is warp-collective: reconverge after the inserts
+                tmem_ld32(tbase + (uint32_t)(c * 32), rc);
+                if (c == 1) {
+                    fence_before();
+                    __syncwarp();
+                    if (lane == 0) bar_arrive(tempty + acc);
+                }
+                // keys t = w - 2 q.x (packed FMA, in place)
+#pragma unroll
+                for (int j = 0; j < 32; j += 4) {
+                    const float4 w4 = *reinterpret_cast<const float4*>(wv + c * 32 + j);
+                    const float2 a2 = __ffma2_rn(make_float2(-2.0f, -2.0f),
+                                                 make_float2(__uint_as_float(rc[j]), __uint_as_float(rc[j + 1])),
+                                                 make_float2(w4.x, w4.y));
+                    const float2 b2 = __ffma2_rn(make_float2(-2.0f, -2.0f),
+                                                 make_float2(__uint_as_float(rc[j + 2]), __uint_as_float(rc[j + 3])),
+                                                 make_float2(w4.z, w4.w));
+                    rc[j] = __float_as_uint(a2.x);
+                    rc[j + 1] = __float_as_uint(a2.y);
+                    rc[j + 2] = __float_as_uint(b2.x);
+                    rc[j + 3] = __float_as_uint(b2.y);
+                }
                 const uint32_t mbits = c == 0 ? mw.x : mw.y;
-                const uint32_t* rc = r + c * 32;
                 float mm[11];
 #pragma unroll
                 for (int k = 0; k < 10; ++k)
