@@ -265,3 +265,55 @@ def test_bucket_rows_follow_rebuilds_and_loads(culsh, all_dense, monkeypatch, tm
     st = _search(culsh, ht2, Qm, X2, K, T, dense_tc=1)
     _check_against(st, want, Qm.shape[0], X2)
     assert st.profile()["bucket_rows"] > 0
+
+
+def test_bucket_rows_bound_form(culsh, all_dense, monkeypatch):
+    """Bucket rows under the bound form (real-valued Gaussian-mixture data):
+    certified keys, exact recomputation and the fallback see the same
+    membership rows; results equal the oracle's."""
+    from culsh_gb300 import synth
+    monkeypatch.setenv("CULSH_BIG_ROWS_MIN", "64")
+    X, Qm, _, _, _ = synth.dataset(1, n=30_000, q=300)
+    L, M, T, K, W = 8, 8, 16, 10, 32.0
+    A, b = synth.projection(L, M, X.shape[1], W, 3001)
+    want = _oracle_case(X, Qm, A, b, W, K, T)
+    ht = culsh.HashTables()
+    ht.reset(X.shape[0], X.shape[1], L, M, W, A=A, b=b)
+    ht.index(X)
+    st = _search(culsh, ht, Qm, X, K, T, dense_tc=1)
+    _check_against(st, want, Qm.shape[0], X)
+    pr = st.profile()
+    assert pr["knn_queries"] == int((want["nonunique"] > 0).sum()) and pr["bucket_rows"] > 0
+
+
+def test_bucket_rows_graph_replay(culsh, all_dense, monkeypatch):
+    """Captured and replayed searches whose membership rows use bucket rows
+    return the oracle's results on every replay."""
+    torch = pytest.importorskip("torch")
+    from culsh_gb300 import synth
+    monkeypatch.setenv("CULSH_BIG_ROWS_MIN", "64")
+    Xn, Qn, _, _, _ = synth.dataset(2, n=20_000, q=256)
+    L, M, T, K, W = 16, 12, 16, 10, 825.0
+    A, b = synth.projection(L, M, Xn.shape[1], W, 3002)
+    want = _oracle_case(Xn, Qn, A, b, W, K, T)
+    X = torch.from_numpy(np.ascontiguousarray(Xn)).cuda()
+    q = torch.from_numpy(np.ascontiguousarray(Qn)).cuda()
+    ht = culsh.HashTables()
+    ht.reset(Xn.shape[0], Xn.shape[1], L, M, W, A=A, b=b)
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    ht.index_device(X.data_ptr(), sp)
+    ids = torch.empty((q.shape[0], K), dtype=torch.int32, device="cuda")
+    d = torch.empty((q.shape[0], K), dtype=torch.float32, device="cuda")
+    st = culsh.SearchTables()
+    st.reset(ht, K, T)
+    st.set_tuning(dense_tc=1)
+    modes = []
+    for _ in range(3):
+        st.search_device(q.data_ptr(), q.shape[0], ids.data_ptr(), d.data_ptr(), sp)
+        stream.synchronize()
+        np.testing.assert_array_equal(ids.cpu().numpy(), want["knn_ids"])
+        np.testing.assert_array_equal(d.cpu().numpy(), want["knn_dists"])
+        modes.append(st.profile()["graph_mode"])
+        assert st.profile()["bucket_rows"] > 0
+    assert modes[0] == 1 and modes[-1] == 2
