@@ -136,3 +136,35 @@ def test_server_needs_resident_dataset(culsh, tmp_path):
     with pytest.raises(culsh.CulshError) as ei:
         culsh.Server(ht2)
     assert ei.value.code == culsh.ERR_STATE
+
+
+def test_dense_requests_on_tensor_cores(culsh, monkeypatch):
+    """Requests whose queries are dense (every query, CULSH_DENSE_MIN=1) run
+    the membership rows with bucket rows and the tensor-core k-NN in several
+    slots at once; each request's ids and distances equal the oracle's."""
+    import oracle
+    from culsh_gb300 import synth
+    monkeypatch.setenv("CULSH_DENSE_MIN", "1")
+    monkeypatch.setenv("CULSH_BIG_ROWS_MIN", "64")
+    X, Qm, _, _, _ = synth.dataset(2, n=20_000, q=600)
+    L, M, W = 16, 12, 825.0
+    A, b = synth.projection(L, M, X.shape[1], W, 3002)
+    ht = culsh.HashTables()
+    ht.reset(X.shape[0], X.shape[1], L, M, W, A=A, b=b)
+    ht.index(X)
+    ref_index = oracle.build_index(X, A, b, W)
+    rng = np.random.default_rng(23)
+    reqs = []
+    for _ in range(24):
+        lo = int(rng.integers(0, Qm.shape[0] - 1))
+        hi = int(min(Qm.shape[0], lo + rng.integers(1, 200)))
+        reqs.append((np.ascontiguousarray(Qm[lo:hi]), int(rng.choice([1, 5, 10, 20])), int(rng.choice([1, 8, 16]))))
+    with culsh.Server(ht, slots=4, max_batch_queries=256) as srv:
+        tickets = [srv.submit(q, K, T) for q, K, T in reqs]
+        for t, (q, K, T) in zip(tickets, reqs):
+            ids, d = srv.wait(t, timeout=120)
+            want = oracle.search(ref_index, X, q, K, T)
+            np.testing.assert_array_equal(ids, want["knn_ids"])
+            np.testing.assert_array_equal(d, want["knn_dists"])
+        st = srv.stats()
+    assert st["requests"] == len(reqs) and st["failed"] == 0
