@@ -616,15 +616,20 @@ __global__ void __launch_bounds__(BT, 1) k_cand_bitmap(WsArgs a, uint32_t* __res
     constexpr int NW = BT / 32;
     const unsigned int ndense = *a.n_dense;
     const int T = a.T, LT = a.L * a.T;
+    // Thread 0 claims the next query while the block works on the current
+    // one (the claim's round trip overlaps the work) and publishes it at the
+    // end of the query, before the block's last barrier.
+    if (tid == 0) {
+        const unsigned int k = atomicAdd(a.dense_next, 1u);
+        s_k = (int)k;
+        s_q = k < ndense ? a.dense_q[k] : -1;
+    }
+    __syncthreads();
     for (;;) {
-        if (tid == 0) {
-            const unsigned int k = atomicAdd(a.dense_next, 1u);
-            s_k = (int)k;
-            s_q = k < ndense ? a.dense_q[k] : -1;
-        }
-        __syncthreads();
         const int q = s_q, k = s_k;
         if (q < 0) break;
+        unsigned int knext = 0;
+        if (tid == 0) knext = atomicAdd(a.dense_next, 1u);
         for (int i = tid * 4; i < nwp; i += BT * 4) *reinterpret_cast<uint4*>(bits + i) = make_uint4(0u, 0u, 0u, 0u);
         for (int c0 = 0; c0 < LT; c0 += BCH) {
             // matched buckets of this chunk of (table, probe) slots, with sizes
@@ -734,6 +739,8 @@ __global__ void __launch_bounds__(BT, 1) k_cand_bitmap(WsArgs a, uint32_t* __res
             a.cu[q] = U;
             atomicAdd(a.totals + 0, U);
             atomicAdd(a.totals + 1, a.cnu[q]);
+            s_k = (int)knext;
+            s_q = knext < ndense ? a.dense_q[knext] : -1;
         }
         __syncthreads();
     }
